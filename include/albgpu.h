@@ -1,0 +1,194 @@
+/*
+ * albgpu.h - C ABI of the GB300 photon-tracing / photon-mapping waveform engine.
+ *
+ * Plain pointers and sizes only. Host pointers are caller-owned; the context owns every
+ * device buffer. Calls on one context are not re-entrant. All functions return ALB_OK (0)
+ * or a negative ALB_ERR_* code; alb_last_error() gives the message of the last failure.
+ *
+ * Each entry point replaces one step of the reference's pure-Python driver
+ * (alb_sim/execution/linear.py:77-117 run_linear, alb_sim/execution/parallel.py:186-284
+ * run_parallel):
+ *
+ *   alb_create        Simulation(config, rng) + SimulationModel(config)
+ *                     (alb_sim/core/simulation.py:29-69, physics/models/simulation.py:21-43)
+ *   alb_trace pass 0  Simulation.simulate_batch(n, forward=True)
+ *                     (core/simulation.py:71-107 with store_photons :113-130)
+ *   alb_build_maps    build_photon_map_data + PhotonMapIndex(KDTree)
+ *                     (photon_mapping/build_photon_map_data.py:8-62, photon_map_index.py:6-17)
+ *   alb_trace pass 1  Simulation.simulate_batch(n, forward=False) including the k-NN
+ *                     gathers and waveform accumulation (core/simulation.py:132-214)
+ *   alb_get_waveform  Simulation.return_waveform[type] (core/simulation.py:46-49)
+ *   alb_export_map    PhotonMapData of one type (photon_mapping/photon_map_data.py:6-15)
+ *   alb_knn           KDTree(points).query(x, k) (photon_map_index.py:17,
+ *                     core/simulation.py:139-142), exposed for neighbour-set checks
+ */
+#ifndef ALBGPU_H
+#define ALBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ALB_MAX_LAYERS 8
+#define ALB_PHASE_DIVISIONS 18000
+#define ALB_CHANNELS 4
+
+/* status codes */
+#define ALB_OK 0
+#define ALB_ERR_INVALID (-1)      /* bad argument or configuration (ValueError) */
+#define ALB_ERR_TOO_FEW (-2)      /* photon map smaller than k at a gather (IndexError) */
+#define ALB_ERR_CAPACITY (-3)     /* a device buffer bound was exceeded */
+#define ALB_ERR_CUDA (-4)         /* CUDA runtime failure */
+#define ALB_ERR_ITER_CAP (-5)     /* a device loop hit its iteration cap */
+#define ALB_ERR_REPLAY (-6)       /* a replay stream ran out of variates */
+#define ALB_ERR_STATE (-7)        /* call order violated (e.g. gather before maps) */
+
+/* channels = PhotonType in the reference's enum order (photon_mapping/photon_type.py:7-10) */
+#define ALB_BOTTOM_REFLECTION 0
+#define ALB_SCATTER 1
+#define ALB_SURFACE_REFLECTION 2
+#define ALB_SURFACE_TRANSMISSION_UP 3
+
+/* passes */
+#define ALB_FORWARD 0
+#define ALB_BACKWARD 1
+
+/* options (alb_set_option) */
+#define ALB_OPT_KEEP_EXIT_STATES 1 /* keep per-photon final states of the next trace */
+#define ALB_OPT_KEEP_RECORD_IDS 2  /* store the emitting photon id with every record/query */
+#define ALB_OPT_PRECISE 3          /* 1: float64 event geometry (replay-exact), 0: fast fp32 */
+#define ALB_OPT_MAP_CAPACITY 4     /* records per channel to pre-allocate (0 = automatic) */
+#define ALB_OPT_SORT_QUERIES 5     /* 1: sort gather queries spatially before the gather */
+#define ALB_OPT_STREAM 6           /* cudaStream_t (as integer) used for every launch */
+
+/* One homogeneous water layer. The tables are host pointers read once by alb_create. */
+typedef struct AlbLayer {
+    double bottom_depth;          /* depth of the layer's lower boundary below the surface */
+    double speed;                 /* c / n rounded to float32, m/s */
+    float alpha;                  /* Churnside lidar attenuation (float32), 1/m */
+    float ssa;                    /* single-scattering albedo (alpha - a) / alpha, float32 */
+    double absorption;            /* absorption a, 1/m (adjoint only) */
+    double bin_width;             /* angular bin width of the gather weight (float32 value) */
+    const double* phase_theta;    /* ALB_PHASE_DIVISIONS scattering angles */
+    const double* phase_cdf;      /* ALB_PHASE_DIVISIONS normalised CDF values */
+    const double* phase_slope;    /* ALB_PHASE_DIVISIONS-1 interpolation slopes d theta/d cdf */
+    const double* scatter_weight; /* ALB_PHASE_DIVISIONS CDF mass per angular bin */
+} AlbLayer;
+
+/* Scene constants derived on the host from SimulationConfig. */
+typedef struct AlbSceneParams {
+    double dt;                    /* integrator step, s */
+    int64_t steps;                /* waveform samples of SimulationModel.steps; bins = 2*steps */
+    int32_t sample_multiplier;    /* integrator steps per waveform sample */
+    int32_t k;                    /* photon_mapping_k */
+    double surface_y;             /* y of the mean water surface */
+    double floor_y;               /* y of the seafloor */
+    double speed_air;             /* float32-rounded speed of light in air */
+    double n_water;               /* refractive index of the top layer at the surface */
+    double f0;                    /* Schlick base reflectance */
+    double seafloor_albedo;
+    double surface_albedo;
+    double roughness;             /* SeaSurfaceConfig.roughness (GGX alpha = roughness^2) */
+    double laser_dir[3];
+    float laser_rot[9];           /* float32 row-major rotation +z -> laser axis */
+    double divergence;            /* beam half-angle, rad */
+    double fov;                   /* receiver half-angle, rad */
+    double aperture_radius;       /* m */
+    double pulse_sigma;           /* s */
+    double effective_rate;        /* sample_multiplier * sample_rate, Hz */
+    int32_t n_layers;
+    int32_t heatmap_enabled;
+    int32_t heatmap_bins;
+    int32_t reserved0;
+    double heatmap_water_extent;
+    double heatmap_floor_extent;
+    double water_center[3];
+    double floor_center[3];
+    AlbLayer layers[ALB_MAX_LAYERS];
+} AlbSceneParams;
+
+/* Caller-supplied variates (replay mode): photon i consumes values[offsets[i] ..
+ * offsets[i+1]) in the reference's draw order; tau[j] = -log(float32(values[j])) formed as
+ * the reference forms it (used where a value is an optical-depth target). */
+typedef struct AlbReplay {
+    const int64_t* offsets;       /* n + 1 entries */
+    const double* values;
+    const float* tau;
+    uint64_t n_values;
+} AlbReplay;
+
+typedef struct AlbCtx AlbCtx;
+
+/* Simulation(config, rng): validate the scene, upload tables, allocate the context. */
+int alb_create(const AlbSceneParams* scene, int device, AlbCtx** out);
+void alb_destroy(AlbCtx* ctx);
+const char* alb_last_error(const AlbCtx* ctx);
+int alb_set_option(AlbCtx* ctx, int key, int64_t value);
+
+/* simulate_batch(n, forward=pass==ALB_FORWARD). Philox mode when replay == NULL: photon i
+ * of this call uses stream (seed, first_photon + i). Forward calls append records to the
+ * photon maps; backward calls trace, gather and accumulate into the waveform. */
+int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint64_t first_photon,
+              const AlbReplay* replay);
+
+/* build_photon_map_data + PhotonMapIndex: sort every channel's records into the spatial
+ * index used by the gather. Must follow the forward traces and precede backward ones. */
+int alb_build_maps(AlbCtx* ctx);
+
+/* Records of one channel (after alb_build_maps: in index order). fwi/sfi (float[3n],
+ * nullable) are the first-water / seafloor interaction points, stored only when the
+ * scene's heatmaps are enabled (NaN otherwise), as PhotonMapData carries them. */
+int alb_map_size(AlbCtx* ctx, int channel, uint64_t* out);
+int alb_export_map(AlbCtx* ctx, int channel, float* pos, float* dir, float* energy,
+                   float* time, float* fwi, float* sfi, int64_t* photon_id, size_t n);
+
+/* Sampled heatmaps (alb_sim/math/accumulate_heatmap.py:6-124): water and seafloor energy
+ * heatmaps (float64 [bins*bins]) and the forward scatter-radius counts (float32). */
+int alb_get_heatmaps(AlbCtx* ctx, double* water, double* seafloor, float* radius, size_t bins2);
+
+/* return_waveform[type] as float32 (reference units), or its exact float64 value. */
+int alb_get_waveform(AlbCtx* ctx, int channel, float* out, size_t nbins);
+int alb_get_waveform_f64(AlbCtx* ctx, int channel, double* out, size_t nbins);
+int alb_reset_waveform(AlbCtx* ctx);
+
+/* Start a new simulation on the same context: empty photon maps, queries, waveform and
+ * heatmaps; device allocations are kept for reuse (a new Simulation(config, rng)). */
+int alb_reset(AlbCtx* ctx);
+
+/* Per-photon final states of the last trace (needs ALB_OPT_KEEP_EXIT_STATES):
+ * pos/dir double[3n], energy/tau/tau_target/time float[n], fwi/sfi float[3n]. */
+int alb_export_exit_states(AlbCtx* ctx, double* pos, double* dir, float* energy, float* tau,
+                           float* tau_target, float* time, float* fwi, float* sfi, size_t n);
+
+/* Backward queries of the last backward trace for one query kind (0 bottom, 1 scatter,
+ * 2 surface): pos double[3n], dir float[3n], energy/time float[n], photon ids, k-th
+ * neighbour distance r_k double[n] per map gathered (surface queries gather twice:
+ * rk2 is the transmission map's, NULL allowed). */
+int alb_query_count(AlbCtx* ctx, int kind, uint64_t* out);
+int alb_export_queries(AlbCtx* ctx, int kind, double* pos, float* dir, float* energy,
+                       float* time, int64_t* photon_id, double* rk, double* rk2, size_t n);
+
+/* KDTree(points).query(queries, k): exact k nearest neighbours on the device.
+ * points float[3m] host, queries double[3q] host; out idx int32[q*k] sorted by distance,
+ * dist double[q*k]. */
+int alb_knn(AlbCtx* ctx, const float* points, uint64_t m, const double* queries, uint64_t q,
+            int k, int32_t* idx, double* dist);
+
+/* Device-side counters of the last trace / gather (events, records, queries, launches). */
+int alb_stats(AlbCtx* ctx, int64_t* out, int n);
+
+/* Accumulated device time (ms, CUDA events on the context's stream) and call counts per
+ * phase since the last reset: 0 forward trace, 1 map build, 2 backward trace,
+ * 3 query sort, 4..7 gather of channel 0..3. out_ms/out_calls hold ALB_PHASES entries;
+ * gathers[4] (nullable) receives the number of queries gathered per channel.
+ * reset != 0 clears the accumulators after reading. */
+#define ALB_PHASES 8
+int alb_phase_times(AlbCtx* ctx, double* out_ms, int64_t* out_calls, int64_t* gathers, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALBGPU_H */

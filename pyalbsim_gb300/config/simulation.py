@@ -1,0 +1,28 @@
+"""Top-level simulation settings; fields and defaults as ``alb_sim/config/simulation.py:12-60``."""
+
+from dataclasses import dataclass, field
+
+from pyalbsim_gb300.config.heatmap import HeatmapConfig
+from pyalbsim_gb300.config.laser import LaserConfig
+from pyalbsim_gb300.config.scene import SceneConfig
+from pyalbsim_gb300.config.sea_floor import SeaFloorConfig
+from pyalbsim_gb300.config.sea_surface import SeaSurfaceConfig
+from pyalbsim_gb300.config.sensor import SensorConfig
+from pyalbsim_gb300.config.water import WaterConfig
+
+
+@dataclass(frozen=True)
+class SimulationConfig:
+    sample_multiplier: int = field(
+        default=10, metadata={"description": "Integrator sub-steps per waveform sample"}
+    )
+    photon_mapping_k: int = field(
+        default=100, metadata={"description": "Neighbours per photon-map density estimate"}
+    )
+    scene: SceneConfig = field(default_factory=SceneConfig)
+    water: WaterConfig = field(default_factory=WaterConfig)
+    laser: LaserConfig = field(default_factory=LaserConfig)
+    sensor: SensorConfig = field(default_factory=SensorConfig)
+    sea_floor: SeaFloorConfig = field(default_factory=SeaFloorConfig)
+    sea_surface: SeaSurfaceConfig = field(default_factory=SeaSurfaceConfig)
+    heatmap: HeatmapConfig = field(default_factory=HeatmapConfig)

@@ -1,0 +1,859 @@
+// C ABI of the GB300 photon-tracing / photon-mapping engine (declared in include/albgpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "albgpu.h"
+#include "internal.h"
+
+using namespace alb;
+
+#include <atomic>
+static std::atomic<long long> g_launches{0};
+namespace alb {
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launches_total() { return g_launches.load(); }
+}  // namespace alb
+
+// ------------------------------------------------------------------------------------------
+// Workspace
+// ------------------------------------------------------------------------------------------
+
+Workspace::~Workspace() {
+    for (void* p : temps_) cudaFree(p);
+    if (box_) cudaFree(box_);
+}
+
+void* Workspace::take_bytes(uint64_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (cudaMallocAsync(&p, bytes, st_) != cudaSuccess) {
+        failed_ = true;
+        cudaGetLastError();
+        return nullptr;
+    }
+    temps_.push_back(p);
+    return p;
+}
+
+void Workspace::release(size_t m) {
+    while (temps_.size() > m) {
+        cudaFreeAsync(temps_.back(), st_);
+        temps_.pop_back();
+    }
+}
+
+unsigned* Workspace::scratch_box() {
+    if (!box_) {
+        if (cudaMalloc(&box_, 64 * sizeof(unsigned)) != cudaSuccess) {
+            failed_ = true;
+            cudaGetLastError();
+        }
+    }
+    return box_;
+}
+
+static void* grow(void* old, uint64_t& cap, uint64_t n, size_t elem, bool& failed) {
+    if (cap >= n && old) return old;
+    if (old) {
+        cudaDeviceSynchronize();
+        cudaFree(old);
+    }
+    uint64_t want = std::max<uint64_t>(n + n / 8, 256);
+    void* p = nullptr;
+    if (cudaMalloc(&p, want * elem) != cudaSuccess) {
+        cudaGetLastError();
+        failed = true;
+        cap = 0;
+        return nullptr;
+    }
+    cap = want;
+    return p;
+}
+
+void* Workspace::alloc_persistent(void* old, uint64_t& cap, uint64_t n) { return grow(old, cap, n, 16, failed_); }
+void* Workspace::alloc_persistent_u32(void* old, uint64_t& cap, uint64_t n) { return grow(old, cap, n, 4, failed_); }
+
+// ------------------------------------------------------------------------------------------
+// Context
+// ------------------------------------------------------------------------------------------
+
+struct AlbCtx {
+    int device = 0;
+    cudaStream_t st = 0;
+    SceneDev sc{};
+    std::vector<void*> tables;
+    Workspace ws;
+    // forward records
+    RecordStore rec[ALB_CHANNELS];
+    uint64_t rec_id_cap[ALB_CHANNELS] = {0};
+    uint64_t fwi_cap[ALB_CHANNELS] = {0}, sfi_cap[ALB_CHANNELS] = {0}, b_cap[ALB_CHANNELS] = {0};
+    unsigned long long* d_rec_count = nullptr;
+    uint64_t h_rec_count[ALB_CHANNELS] = {0};
+    double rec_rate[ALB_CHANNELS] = {2.0, 8.0, 1.05, 1.05};
+    MapIndex map[ALB_CHANNELS];
+    bool maps_built = false;
+    // backward queries
+    float4* qa[3] = {nullptr, nullptr, nullptr};
+    float4* qb[3] = {nullptr, nullptr, nullptr};
+    float4* qc[3] = {nullptr, nullptr, nullptr};
+    uint32_t* qid[3] = {nullptr, nullptr, nullptr};
+    uint32_t* qperm[3] = {nullptr, nullptr, nullptr};
+    double* qrk[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    uint64_t qcap[3] = {0, 0, 0}, qcap_b[3] = {0}, qcap_c[3] = {0}, qid_cap[3] = {0}, qperm_cap[3] = {0};
+    uint64_t qrk_cap[3][2] = {{0}};
+    unsigned long long* d_q_count = nullptr;
+    uint64_t h_q_count[3] = {0, 0, 0};
+    double q_rate[3] = {2.0, 8.0, 1.05};
+    // accumulators
+    unsigned long long* wf = nullptr;  // lo words then hi words, [2][channels][nbins]
+    unsigned long long* hm = nullptr;  // sampled heatmaps, [2 maps][2 words][bins*bins]
+    unsigned* hm_radius = nullptr;
+    // exit states
+    double* ex_pos = nullptr;
+    double* ex_dir = nullptr;
+    float* ex_f = nullptr;
+    uint64_t ex_cap = 0, ex_n = 0;
+    // misc
+    int* d_err = nullptr;
+    unsigned long long* d_stats = nullptr;
+    int keep_exit = 0, keep_ids = 0, precise = 1, sort_q = 1;
+    int64_t map_cap_hint = 0;
+    int launches = 0;
+    std::string err;
+    // phase timing (CUDA events on the context's stream)
+    double phase_ms[ALB_PHASES] = {0};
+    int64_t phase_calls[ALB_PHASES] = {0};
+    int64_t gathered[ALB_CHANNELS] = {0};
+    cudaEvent_t ev[2 * ALB_PHASES] = {};
+    bool ev_ready = false;
+};
+
+// Time one phase: record a start event, run `body`, record a stop event, and fold the
+// elapsed time into the accumulator once the stream has drained (the caller syncs).
+struct PhaseTimer {
+    AlbCtx* c;
+    int phase;
+    PhaseTimer(AlbCtx* ctx, int p) : c(ctx), phase(p) {
+        if (!c->ev_ready) {
+            for (auto& e : c->ev) cudaEventCreate(&e);
+            c->ev_ready = true;
+        }
+        cudaEventRecord(c->ev[2 * phase], c->st);
+    }
+    void stop() {
+        cudaEventRecord(c->ev[2 * phase + 1], c->st);
+        cudaEventSynchronize(c->ev[2 * phase + 1]);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev[2 * phase], c->ev[2 * phase + 1]) == cudaSuccess) c->phase_ms[phase] += ms;
+        c->phase_calls[phase] += 1;
+    }
+};
+
+static int fail(AlbCtx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(ctx, ALB_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+static int check_device(AlbCtx* ctx, const char* where) {
+    cudaError_t e = cudaStreamSynchronize(ctx->st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, ALB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    if (ctx->ws.failed()) {
+        ctx->ws.clear_failed();
+        return fail(ctx, ALB_ERR_CUDA, std::string(where) + ": device allocation failed");
+    }
+    int h = 0;
+    CK(cudaMemcpy(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h != 0) {
+        CK(cudaMemset(ctx->d_err, 0, sizeof(int)));
+        const char* what = h == ALB_ERR_ITER_CAP ? "a device loop hit its iteration cap"
+                           : h == ALB_ERR_REPLAY ? "a replay stream ran out of variates"
+                           : h == ALB_ERR_TOO_FEW ? "a photon map holds fewer records than k"
+                           : h == ALB_ERR_CAPACITY ? "a waveform bin index fell outside the waveform"
+                                                   : "device error";
+        return fail(ctx, h, std::string(where) + ": " + what);
+    }
+    return ALB_OK;
+}
+
+static thread_local std::string g_create_error;
+
+extern "C" const char* alb_last_error(const AlbCtx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
+    if (!p || !out) return ALB_ERR_INVALID;
+    *out = nullptr;
+    AlbCtx* ctx = new AlbCtx();
+    auto bad = [&](const std::string& m) {
+        g_create_error = m;
+        delete ctx;
+        return ALB_ERR_INVALID;
+    };
+    if (!(p->dt > 0) || p->steps <= 0 || p->sample_multiplier <= 0) return bad("bad time step");
+    if (p->k < 1 || p->k > 256) return bad("photon_mapping_k must be in [1, 256]");
+    if (p->n_layers < 1 || p->n_layers > ALB_MAX_LAYERS) return bad("1..8 water layers supported");
+    if (!(p->surface_y > p->floor_y)) return bad("seafloor must lie below the surface");
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) return bad("cudaSetDevice failed");
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    SceneDev& s = ctx->sc;
+    s.dt = p->dt;
+    s.total_steps = p->steps * (int64_t)p->sample_multiplier;
+    s.nbins = 2 * p->steps;
+    s.mult = p->sample_multiplier;
+    s.k = p->k;
+    s.ys = p->surface_y;
+    s.yf = p->floor_y;
+    s.v_air = p->speed_air;
+    s.n_water = p->n_water;
+    s.eta = 1.0 / p->n_water;
+    s.f0 = p->f0;
+    s.floor_albedo = p->seafloor_albedo;
+    s.floor_albedo32 = (float)p->seafloor_albedo;
+    s.surface_albedo = p->surface_albedo;
+    s.roughness = p->roughness;
+    double ga = p->roughness * p->roughness;
+    s.ggx_a2 = (float)(ga * ga);
+    for (int i = 0; i < 9; ++i) s.rot_d[i] = (double)p->laser_rot[i];
+    s.div = p->divergence;
+    s.fov = p->fov;
+    s.cos_fov = std::cos(p->fov);
+    s.aperture = p->aperture_radius;
+    s.pulse_sigma32 = p->pulse_sigma;
+    s.eff_rate32 = (double)(float)p->effective_rate;
+    s.rayleigh_sigma = p->divergence / 3.0;
+    s.rayleigh_mass = -std::expm1(-(p->divergence * p->divergence) / (2.0 * s.rayleigh_sigma * s.rayleigh_sigma));
+    s.n_layers = p->n_layers;
+    s.heatmap = p->heatmap_enabled;
+    s.hm_bins = p->heatmap_bins;
+    s.hm_wext = p->heatmap_water_extent;
+    s.hm_fext = p->heatmap_floor_extent;
+    s.hm_wbin = 2.0 * p->heatmap_water_extent / p->heatmap_bins;
+    s.hm_fbin = 2.0 * p->heatmap_floor_extent / p->heatmap_bins;
+    for (int i = 0; i < 3; ++i) {
+        s.wc[i] = p->water_center[i];
+        s.fc[i] = p->floor_center[i];
+    }
+    const int N = ALB_PHASE_DIVISIONS;
+    for (int l = 0; l < p->n_layers; ++l) {
+        const AlbLayer& L = p->layers[l];
+        if (!L.phase_theta || !L.phase_cdf || !L.phase_slope || !L.scatter_weight) return bad("missing layer table");
+        s.layer_bottom[l] = L.bottom_depth;
+        s.layer_speed[l] = L.speed;
+        s.layer_alpha[l] = L.alpha;
+        s.layer_ssa[l] = L.ssa;
+        s.layer_binw[l] = (float)L.bin_width;
+        double *th, *cdf, *sl;
+        float* w;
+        if (cudaMalloc(&th, N * sizeof(double)) != cudaSuccess || cudaMalloc(&cdf, N * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&sl, N * sizeof(double)) != cudaSuccess || cudaMalloc(&w, N * sizeof(float)) != cudaSuccess)
+            return bad("table allocation failed");
+        ctx->tables.insert(ctx->tables.end(), {th, cdf, sl, w});
+        std::vector<double> slope(N, 0.0);
+        std::memcpy(slope.data(), L.phase_slope, (N - 1) * sizeof(double));
+        std::vector<float> wf(N);
+        for (int i = 0; i < N; ++i) wf[i] = (float)L.scatter_weight[i];
+        cudaMemcpy(th, L.phase_theta, N * sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemcpy(cdf, L.phase_cdf, N * sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemcpy(sl, slope.data(), N * sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemcpy(w, wf.data(), N * sizeof(float), cudaMemcpyHostToDevice);
+        s.layer_theta[l] = th;
+        s.layer_cdf[l] = cdf;
+        s.layer_slope[l] = sl;
+        s.layer_weight[l] = w;
+    }
+    // accumulators
+    size_t wf_words = (size_t)2 * ALB_CHANNELS * s.nbins;
+    if (cudaMalloc(&ctx->wf, wf_words * 8) != cudaSuccess) return bad("waveform allocation failed");
+    cudaMemset(ctx->wf, 0, wf_words * 8);
+    if (s.heatmap) {
+        size_t hb = (size_t)s.hm_bins * s.hm_bins;
+        if (cudaMalloc(&ctx->hm, 4 * hb * 8) != cudaSuccess || cudaMalloc(&ctx->hm_radius, hb * 4) != cudaSuccess)
+            return bad("heatmap allocation failed");
+        cudaMemset(ctx->hm, 0, 4 * hb * 8);
+        cudaMemset(ctx->hm_radius, 0, hb * 4);
+    }
+    if (cudaMalloc(&ctx->d_rec_count, ALB_CHANNELS * 8) != cudaSuccess || cudaMalloc(&ctx->d_q_count, 3 * 8) != cudaSuccess ||
+        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, 16 * 8) != cudaSuccess)
+        return bad("counter allocation failed");
+    cudaMemset(ctx->d_rec_count, 0, ALB_CHANNELS * 8);
+    cudaMemset(ctx->d_q_count, 0, 3 * 8);
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    cudaMemset(ctx->d_stats, 0, 16 * 8);
+    if (cudaDeviceSynchronize() != cudaSuccess) return bad("device initialisation failed");
+    *out = ctx;
+    return ALB_OK;
+}
+
+extern "C" void alb_destroy(AlbCtx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (void* p : ctx->tables) cudaFree(p);
+    for (int c = 0; c < ALB_CHANNELS; ++c) {
+        cudaFree(ctx->rec[c].a); cudaFree(ctx->rec[c].b); cudaFree(ctx->rec[c].fwi); cudaFree(ctx->rec[c].sfi);
+        cudaFree(ctx->rec[c].id);
+        MapIndex& m = ctx->map[c];
+        cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id); cudaFree(m.box_lo); cudaFree(m.box_hi);
+    }
+    for (int k = 0; k < 3; ++k) {
+        cudaFree(ctx->qa[k]); cudaFree(ctx->qb[k]); cudaFree(ctx->qc[k]); cudaFree(ctx->qid[k]); cudaFree(ctx->qperm[k]);
+        cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]);
+    }
+    cudaFree(ctx->wf); cudaFree(ctx->hm); cudaFree(ctx->hm_radius);
+    cudaFree(ctx->ex_pos); cudaFree(ctx->ex_dir); cudaFree(ctx->ex_f);
+    cudaFree(ctx->d_rec_count); cudaFree(ctx->d_q_count); cudaFree(ctx->d_err); cudaFree(ctx->d_stats);
+    if (ctx->ev_ready)
+        for (auto& e : ctx->ev) cudaEventDestroy(e);
+    delete ctx;
+}
+
+extern "C" int alb_set_option(AlbCtx* ctx, int key, int64_t v) {
+    if (!ctx) return ALB_ERR_INVALID;
+    switch (key) {
+        case ALB_OPT_KEEP_EXIT_STATES: ctx->keep_exit = (int)v; break;
+        case ALB_OPT_KEEP_RECORD_IDS: ctx->keep_ids = (int)v; break;
+        case ALB_OPT_PRECISE: ctx->precise = (int)v; break;
+        case ALB_OPT_MAP_CAPACITY: ctx->map_cap_hint = v; break;
+        case ALB_OPT_SORT_QUERIES: ctx->sort_q = (int)v; break;
+        case ALB_OPT_STREAM:
+            ctx->st = (cudaStream_t)(intptr_t)v;
+            ctx->ws.set_stream(ctx->st);
+            break;
+        default: return fail(ctx, ALB_ERR_INVALID, "unknown option");
+    }
+    return ALB_OK;
+}
+
+// grow a record store to hold `need` records, preserving the first `keep`
+static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
+    RecordStore& r = ctx->rec[c];
+    bool want_hm = ctx->sc.heatmap != 0;
+    bool want_id = ctx->keep_ids != 0;
+    if (r.cap >= need && (!want_id || r.id) && (!want_hm || r.fwi)) return ALB_OK;
+    uint64_t cap = std::max<uint64_t>(need + need / 4, 1024);
+    float4 *a, *b, *fwi = nullptr, *sfi = nullptr;
+    uint32_t* id = nullptr;
+    CK(cudaMalloc(&a, cap * 16));
+    CK(cudaMalloc(&b, cap * 16));
+    if (want_hm) {
+        CK(cudaMalloc(&fwi, cap * 16));
+        CK(cudaMalloc(&sfi, cap * 16));
+    }
+    if (want_id) CK(cudaMalloc(&id, cap * 4));
+    if (keep) {
+        CK(cudaMemcpyAsync(a, r.a, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        CK(cudaMemcpyAsync(b, r.b, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        if (want_hm && r.fwi) {
+            CK(cudaMemcpyAsync(fwi, r.fwi, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
+            CK(cudaMemcpyAsync(sfi, r.sfi, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        }
+        if (want_id && r.id) CK(cudaMemcpyAsync(id, r.id, keep * 4, cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id);
+    r.a = a; r.b = b; r.fwi = fwi; r.sfi = sfi; r.id = id; r.cap = cap;
+    return ALB_OK;
+}
+
+static int ensure_queries(AlbCtx* ctx, int k, uint64_t need) {
+    if (ctx->qcap[k] >= need && (!ctx->keep_ids || ctx->qid[k])) return ALB_OK;
+    uint64_t cap = std::max<uint64_t>(need + need / 4, 1024);
+    cudaFree(ctx->qa[k]); cudaFree(ctx->qb[k]); cudaFree(ctx->qc[k]); cudaFree(ctx->qid[k]); cudaFree(ctx->qperm[k]);
+    cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]);
+    ctx->qid[k] = nullptr; ctx->qrk[k][0] = ctx->qrk[k][1] = nullptr;
+    CK(cudaMalloc(&ctx->qa[k], cap * 16));
+    CK(cudaMalloc(&ctx->qb[k], cap * 16));
+    CK(cudaMalloc(&ctx->qc[k], cap * 16));
+    CK(cudaMalloc(&ctx->qperm[k], cap * 4));
+    if (ctx->keep_ids) {
+        CK(cudaMalloc(&ctx->qid[k], cap * 4));
+        CK(cudaMalloc(&ctx->qrk[k][0], cap * 8));
+        CK(cudaMalloc(&ctx->qrk[k][1], cap * 8));
+    }
+    ctx->qcap[k] = cap;
+    return ALB_OK;
+}
+
+static TraceOut make_out(AlbCtx* ctx) {
+    TraceOut o{};
+    for (int c = 0; c < ALB_CHANNELS; ++c) {
+        o.rec_a[c] = ctx->rec[c].a;
+        o.rec_b[c] = ctx->rec[c].b;
+        o.rec_fwi[c] = ctx->rec[c].fwi;
+        o.rec_sfi[c] = ctx->rec[c].sfi;
+        o.rec_id[c] = ctx->rec[c].id;
+        o.rec_cap[c] = ctx->rec[c].cap;
+    }
+    o.rec_count = ctx->d_rec_count;
+    for (int k = 0; k < 3; ++k) {
+        o.q_a[k] = ctx->qa[k];
+        o.q_b[k] = ctx->qb[k];
+        o.q_c[k] = ctx->qc[k];
+        o.q_id[k] = ctx->qid[k];
+        o.q_cap[k] = ctx->qcap[k];
+    }
+    o.q_count = ctx->d_q_count;
+    o.ex_pos = ctx->keep_exit ? ctx->ex_pos : nullptr;
+    o.ex_dir = ctx->ex_dir;
+    o.ex_f = ctx->ex_f;
+    o.hm_radius = ctx->hm_radius;
+    o.err = ctx->d_err;
+    o.stats = ctx->d_stats;
+    return o;
+}
+
+// Q9 of the reference: a gather on a map with fewer than k records raises IndexError.
+static int check_map_sizes(AlbCtx* ctx) {
+    static const int need[3][2] = {{ALB_BOTTOM_REFLECTION, -1}, {ALB_SCATTER, -1},
+                                   {ALB_SURFACE_REFLECTION, ALB_SURFACE_TRANSMISSION_UP}};
+    static const char* names[4] = {"BOTTOM_REFLECTION", "SCATTER", "SURFACE_REFLECTION", "SURFACE_TRANSMISSION_UP"};
+    for (int k = 0; k < 3; ++k) {
+        if (ctx->h_q_count[k] == 0) continue;
+        for (int j = 0; j < 2; ++j) {
+            int c = need[k][j];
+            if (c < 0) continue;
+            if (ctx->map[c].n < (uint64_t)ctx->sc.k) {
+                char buf[256];
+                snprintf(buf, sizeof buf, "photon map %s holds %llu records, fewer than k=%d", names[c],
+                         (unsigned long long)ctx->map[c].n, ctx->sc.k);
+                return fail(ctx, ALB_ERR_TOO_FEW, buf);
+            }
+        }
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint64_t first, const AlbReplay* rp) {
+    if (!ctx) return ALB_ERR_INVALID;
+    if (pass != ALB_FORWARD && pass != ALB_BACKWARD) return fail(ctx, ALB_ERR_INVALID, "pass must be 0 or 1");
+    if (pass == ALB_BACKWARD && !ctx->maps_built) return fail(ctx, ALB_ERR_STATE, "backward trace before alb_build_maps");
+    if (first + n > (1ull << 32)) return fail(ctx, ALB_ERR_INVALID, "photon ids are 32-bit per pass");
+    CK(cudaSetDevice(ctx->device));
+    ctx->err.clear();
+    // replay streams to the device
+    AlbReplay drp{};
+    size_t mark = ctx->ws.mark();
+    if (rp) {
+        if (!rp->offsets || !rp->values || !rp->tau) return fail(ctx, ALB_ERR_INVALID, "incomplete replay");
+        int64_t* o = (int64_t*)ctx->ws.take_bytes((n + 1) * 8);
+        double* v = (double*)ctx->ws.take_bytes(rp->n_values * 8 + 8);
+        float* t = (float*)ctx->ws.take_bytes(rp->n_values * 4 + 4);
+        if (!o || !v || !t) return fail(ctx, ALB_ERR_CUDA, "replay upload allocation failed");
+        CK(cudaMemcpyAsync(o, rp->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(v, rp->values, rp->n_values * 8, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(t, rp->tau, rp->n_values * 4, cudaMemcpyHostToDevice, ctx->st));
+        drp.offsets = o;
+        drp.values = v;
+        drp.tau = t;
+        drp.n_values = rp->n_values;
+    }
+    if (ctx->keep_exit) {
+        if (ctx->ex_cap < n) {
+            cudaFree(ctx->ex_pos); cudaFree(ctx->ex_dir); cudaFree(ctx->ex_f);
+            CK(cudaMalloc(&ctx->ex_pos, n * 24));
+            CK(cudaMalloc(&ctx->ex_dir, n * 24));
+            CK(cudaMalloc(&ctx->ex_f, n * 40));
+            ctx->ex_cap = n;
+        }
+        ctx->ex_n = n;
+    }
+    CK(cudaMemsetAsync(ctx->d_stats, 0, 16 * 8, ctx->st));
+    if (pass == ALB_FORWARD) {
+        ctx->maps_built = false;
+        uint64_t before[ALB_CHANNELS];
+        std::memcpy(before, ctx->h_rec_count, sizeof before);
+        std::vector<unsigned> radius_backup;
+        size_t hb = ctx->sc.heatmap ? (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins : 0;
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            for (int c = 0; c < ALB_CHANNELS; ++c) {
+                uint64_t est = (uint64_t)(ctx->rec_rate[c] * (double)n * 1.2) + 4096;
+                if (ctx->map_cap_hint > 0) est = std::max<uint64_t>(est, (uint64_t)ctx->map_cap_hint);
+                int rc = ensure_records(ctx, c, before[c] + est, before[c]);
+                if (rc) return rc;
+            }
+            if (hb && attempt == 0) {
+                radius_backup.resize(hb);
+                CK(cudaMemcpy(radius_backup.data(), ctx->hm_radius, hb * 4, cudaMemcpyDeviceToHost));
+            }
+            TraceOut o = make_out(ctx);
+            PhaseTimer pt(ctx, 0);
+            launch_trace(ctx->sc, o, ALB_FORWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st);
+            pt.stop();
+            int rc = check_device(ctx, "forward trace");
+            if (rc) return rc;
+            unsigned long long cnt[ALB_CHANNELS];
+            CK(cudaMemcpy(cnt, ctx->d_rec_count, sizeof cnt, cudaMemcpyDeviceToHost));
+            bool overflow = false;
+            for (int c = 0; c < ALB_CHANNELS; ++c) {
+                uint64_t added = cnt[c] - before[c];
+                if (n > 0) ctx->rec_rate[c] = std::max(ctx->rec_rate[c] * 0.5, (double)added / (double)n);
+                if (cnt[c] > ctx->rec[c].cap) overflow = true;
+            }
+            if (!overflow) {
+                for (int c = 0; c < ALB_CHANNELS; ++c) ctx->h_rec_count[c] = cnt[c];
+                ctx->ws.release(mark);
+                return ALB_OK;
+            }
+            // undo and retry with the measured sizes
+            CK(cudaMemcpy(ctx->d_rec_count, before, sizeof before, cudaMemcpyHostToDevice));
+            if (hb) CK(cudaMemcpy(ctx->hm_radius, radius_backup.data(), hb * 4, cudaMemcpyHostToDevice));
+            for (int c = 0; c < ALB_CHANNELS; ++c) ctx->rec_rate[c] = (double)(cnt[c] - before[c]) / (double)n;
+        }
+        return fail(ctx, ALB_ERR_CAPACITY, "photon-map capacity could not be established");
+    }
+    // backward: trace -> queries -> gathers
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        for (int k = 0; k < 3; ++k) {
+            uint64_t est = (uint64_t)(ctx->q_rate[k] * (double)n * 1.2) + 4096;
+            int rc = ensure_queries(ctx, k, est);
+            if (rc) return rc;
+        }
+        CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
+        TraceOut o = make_out(ctx);
+        PhaseTimer pt(ctx, 2);
+        launch_trace(ctx->sc, o, ALB_BACKWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st);
+        pt.stop();
+        int rc = check_device(ctx, "backward trace");
+        if (rc) return rc;
+        unsigned long long cnt[3];
+        CK(cudaMemcpy(cnt, ctx->d_q_count, sizeof cnt, cudaMemcpyDeviceToHost));
+        bool overflow = false;
+        for (int k = 0; k < 3; ++k) {
+            if (n > 0) ctx->q_rate[k] = std::max(ctx->q_rate[k] * 0.5, (double)cnt[k] / (double)n);
+            if (cnt[k] > ctx->qcap[k]) overflow = true;
+            ctx->h_q_count[k] = cnt[k];
+        }
+        if (!overflow) break;
+        for (int k = 0; k < 3; ++k) ctx->q_rate[k] = (double)cnt[k] / (double)n;
+        if (attempt == 2) return fail(ctx, ALB_ERR_CAPACITY, "query capacity could not be established");
+    }
+    int rc = check_map_sizes(ctx);
+    if (rc) return rc;
+    Accum acc{};
+    acc.wf_lo = ctx->wf;
+    acc.wf_hi = ctx->wf + (size_t)ALB_CHANNELS * ctx->sc.nbins;
+    acc.nbins = ctx->sc.nbins;
+    if (ctx->sc.heatmap) {
+        size_t hb = (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins;
+        acc.hw_lo = ctx->hm;
+        acc.hw_hi = ctx->hm + hb;
+        acc.hf_lo = ctx->hm + 2 * hb;
+        acc.hf_hi = ctx->hm + 3 * hb;
+    }
+    static const int kinds[4] = {kQueryBottom, kQueryScatter, kQuerySurface, kQuerySurface};
+    static const int chans[4] = {ALB_BOTTOM_REFLECTION, ALB_SCATTER, ALB_SURFACE_REFLECTION, ALB_SURFACE_TRANSMISSION_UP};
+    for (int g = 0; g < 4; ++g) {
+        int k = kinds[g], c = chans[g];
+        uint64_t nq = ctx->h_q_count[k];
+        if (nq == 0) continue;
+        QueryDev q{};
+        q.a = ctx->qa[k];
+        q.b = ctx->qb[k];
+        q.c = ctx->qc[k];
+        q.n = nq;
+        q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
+        if (ctx->sort_q) {
+            PhaseTimer ps(ctx, 3);
+            sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
+            ps.stop();
+            q.perm = ctx->qperm[k];
+        }
+        PhaseTimer pg(ctx, 4 + c);
+        launch_gather(ctx->sc, map_dev(ctx->map[c]), q, c, acc, ctx->d_err, &ctx->launches, ctx->st);
+        pg.stop();
+        ctx->gathered[c] += (int64_t)nq;
+    }
+    rc = check_device(ctx, "gather");
+    ctx->ws.release(mark);
+    return rc;
+}
+
+extern "C" int alb_build_maps(AlbCtx* ctx) {
+    if (!ctx) return ALB_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    PhaseTimer pt(ctx, 1);
+    for (int c = 0; c < ALB_CHANNELS; ++c) {
+        build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st);
+    }
+    pt.stop();
+    int rc = check_device(ctx, "map build");
+    if (rc) return rc;
+    ctx->maps_built = true;
+    return ALB_OK;
+}
+
+extern "C" int alb_map_size(AlbCtx* ctx, int c, uint64_t* out) {
+    if (!ctx || !out || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    *out = ctx->h_rec_count[c];
+    return ALB_OK;
+}
+
+extern "C" int alb_export_map(AlbCtx* ctx, int c, float* pos, float* dir, float* energy, float* time,
+                              float* fwi, float* sfi, int64_t* pid, size_t n) {
+    if (!ctx || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    uint64_t m = ctx->h_rec_count[c];
+    if (n < m) return fail(ctx, ALB_ERR_INVALID, "export buffer smaller than the map");
+    if (m == 0) return ALB_OK;
+    const float4 *a, *b, *fw, *sf;
+    const uint32_t* id;
+    if (ctx->maps_built) {
+        a = ctx->map[c].a; b = ctx->map[c].b; id = ctx->map[c].id; fw = ctx->map[c].fwi; sf = ctx->map[c].sfi;
+    } else {
+        a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
+    }
+    std::vector<float4> ha(m), hb(m), hf, hs;
+    CK(cudaMemcpy(ha.data(), a, m * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hb.data(), b, m * 16, cudaMemcpyDeviceToHost));
+    if (fw && (fwi || sfi)) {
+        hf.resize(m);
+        hs.resize(m);
+        CK(cudaMemcpy(hf.data(), fw, m * 16, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(hs.data(), sf, m * 16, cudaMemcpyDeviceToHost));
+    }
+    std::vector<uint32_t> hid;
+    if (pid && id) {
+        hid.resize(m);
+        CK(cudaMemcpy(hid.data(), id, m * 4, cudaMemcpyDeviceToHost));
+    }
+    const float qnan = std::nanf("");
+    for (uint64_t i = 0; i < m; ++i) {
+        if (pos) { pos[3 * i] = ha[i].x; pos[3 * i + 1] = ha[i].y; pos[3 * i + 2] = ha[i].z; }
+        if (energy) energy[i] = ha[i].w;
+        if (dir) { dir[3 * i] = hb[i].x; dir[3 * i + 1] = hb[i].y; dir[3 * i + 2] = hb[i].z; }
+        if (time) time[i] = hb[i].w;
+        if (fwi) {
+            fwi[3 * i] = hf.empty() ? qnan : hf[i].x;
+            fwi[3 * i + 1] = hf.empty() ? qnan : hf[i].y;
+            fwi[3 * i + 2] = hf.empty() ? qnan : hf[i].z;
+        }
+        if (sfi) {
+            sfi[3 * i] = hs.empty() ? qnan : hs[i].x;
+            sfi[3 * i + 1] = hs.empty() ? qnan : hs[i].y;
+            sfi[3 * i + 2] = hs.empty() ? qnan : hs[i].z;
+        }
+        if (pid) pid[i] = hid.empty() ? -1 : (int64_t)hid[i];
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_get_heatmaps(AlbCtx* ctx, double* water, double* seafloor, float* radius, size_t bins2) {
+    if (!ctx) return ALB_ERR_INVALID;
+    if (!ctx->sc.heatmap) return fail(ctx, ALB_ERR_STATE, "heatmaps are disabled in this scene");
+    size_t hb = (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins;
+    if (bins2 < hb) return fail(ctx, ALB_ERR_INVALID, "heatmap buffer too small");
+    std::vector<unsigned long long> h(4 * hb);
+    CK(cudaMemcpy(h.data(), ctx->hm, 4 * hb * 8, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < hb; ++i) {
+        if (water) water[i] = fix_to_double(h[i], (long long)h[hb + i]);
+        if (seafloor) seafloor[i] = fix_to_double(h[2 * hb + i], (long long)h[3 * hb + i]);
+    }
+    if (radius) {
+        std::vector<unsigned> r(hb);
+        CK(cudaMemcpy(r.data(), ctx->hm_radius, hb * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < hb; ++i) radius[i] = (float)r[i];
+    }
+    return ALB_OK;
+}
+
+static int read_wf(AlbCtx* ctx, int c, std::vector<double>& out) {
+    int64_t nb = ctx->sc.nbins;
+    std::vector<unsigned long long> lo(nb), hi(nb);
+    CK(cudaMemcpy(lo.data(), ctx->wf + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hi.data(), ctx->wf + (size_t)ALB_CHANNELS * nb + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost));
+    out.resize(nb);
+    for (int64_t i = 0; i < nb; ++i) out[i] = fix_to_double(lo[i], (long long)hi[i]);
+    return ALB_OK;
+}
+
+extern "C" int alb_get_waveform(AlbCtx* ctx, int c, float* out, size_t nbins) {
+    if (!ctx || !out || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    if (nbins < (size_t)ctx->sc.nbins) return fail(ctx, ALB_ERR_INVALID, "waveform buffer too small");
+    std::vector<double> w;
+    int rc = read_wf(ctx, c, w);
+    if (rc) return rc;
+    for (size_t i = 0; i < w.size(); ++i) out[i] = (float)w[i];
+    return ALB_OK;
+}
+
+extern "C" int alb_get_waveform_f64(AlbCtx* ctx, int c, double* out, size_t nbins) {
+    if (!ctx || !out || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    if (nbins < (size_t)ctx->sc.nbins) return fail(ctx, ALB_ERR_INVALID, "waveform buffer too small");
+    std::vector<double> w;
+    int rc = read_wf(ctx, c, w);
+    if (rc) return rc;
+    std::memcpy(out, w.data(), w.size() * 8);
+    return ALB_OK;
+}
+
+extern "C" int alb_reset_waveform(AlbCtx* ctx) {
+    if (!ctx) return ALB_ERR_INVALID;
+    CK(cudaMemsetAsync(ctx->wf, 0, (size_t)2 * ALB_CHANNELS * ctx->sc.nbins * 8, ctx->st));
+    if (ctx->hm) CK(cudaMemsetAsync(ctx->hm, 0, (size_t)4 * ctx->sc.hm_bins * ctx->sc.hm_bins * 8, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return ALB_OK;
+}
+
+extern "C" int alb_reset(AlbCtx* ctx) {
+    if (!ctx) return ALB_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemsetAsync(ctx->d_rec_count, 0, ALB_CHANNELS * 8, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
+    if (ctx->hm_radius)
+        CK(cudaMemsetAsync(ctx->hm_radius, 0, (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins * 4, ctx->st));
+    for (int c = 0; c < ALB_CHANNELS; ++c) {
+        ctx->h_rec_count[c] = 0;
+        ctx->map[c].n = 0;
+    }
+    for (int k = 0; k < 3; ++k) ctx->h_q_count[k] = 0;
+    ctx->maps_built = false;
+    ctx->ex_n = 0;
+    return alb_reset_waveform(ctx);
+}
+
+extern "C" int alb_export_exit_states(AlbCtx* ctx, double* pos, double* dir, float* energy, float* tau,
+                                      float* tau_target, float* time, float* fwi, float* sfi, size_t n) {
+    if (!ctx) return ALB_ERR_INVALID;
+    if (!ctx->keep_exit || ctx->ex_n == 0) return fail(ctx, ALB_ERR_STATE, "no exit states kept");
+    if (n < ctx->ex_n) return fail(ctx, ALB_ERR_INVALID, "exit-state buffer too small");
+    uint64_t m = ctx->ex_n;
+    std::vector<float> f(10 * m);
+    if (pos) CK(cudaMemcpy(pos, ctx->ex_pos, m * 24, cudaMemcpyDeviceToHost));
+    if (dir) CK(cudaMemcpy(dir, ctx->ex_dir, m * 24, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(f.data(), ctx->ex_f, m * 40, cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < m; ++i) {
+        const float* r = f.data() + 10 * i;
+        if (energy) energy[i] = r[0];
+        if (tau) tau[i] = r[1];
+        if (tau_target) tau_target[i] = r[2];
+        if (time) time[i] = r[3];
+        for (int j = 0; j < 3; ++j) {
+            if (fwi) fwi[3 * i + j] = r[4 + j];
+            if (sfi) sfi[3 * i + j] = r[7 + j];
+        }
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_query_count(AlbCtx* ctx, int kind, uint64_t* out) {
+    if (!ctx || !out || kind < 0 || kind > 2) return ALB_ERR_INVALID;
+    *out = ctx->h_q_count[kind];
+    return ALB_OK;
+}
+
+extern "C" int alb_export_queries(AlbCtx* ctx, int kind, double* pos, float* dir, float* energy, float* time,
+                                  int64_t* pid, double* rk, double* rk2, size_t n) {
+    if (!ctx || kind < 0 || kind > 2) return ALB_ERR_INVALID;
+    uint64_t m = ctx->h_q_count[kind];
+    if (n < m) return fail(ctx, ALB_ERR_INVALID, "query buffer too small");
+    if (m == 0) return ALB_OK;
+    std::vector<float4> a(m), b(m), c(m);
+    CK(cudaMemcpy(a.data(), ctx->qa[kind], m * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b.data(), ctx->qb[kind], m * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(c.data(), ctx->qc[kind], m * 16, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> id;
+    if (ctx->qid[kind]) {
+        id.resize(m);
+        CK(cudaMemcpy(id.data(), ctx->qid[kind], m * 4, cudaMemcpyDeviceToHost));
+    }
+    if (rk && ctx->qrk[kind][0]) CK(cudaMemcpy(rk, ctx->qrk[kind][0], m * 8, cudaMemcpyDeviceToHost));
+    if (rk2 && ctx->qrk[kind][1]) CK(cudaMemcpy(rk2, ctx->qrk[kind][1], m * 8, cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < m; ++i) {
+        if (pos) {
+            pos[3 * i] = (double)a[i].x + (double)c[i].x;
+            pos[3 * i + 1] = (double)a[i].y + (double)c[i].y;
+            pos[3 * i + 2] = (double)a[i].z + (double)c[i].z;
+        }
+        if (dir) { dir[3 * i] = b[i].x; dir[3 * i + 1] = b[i].y; dir[3 * i + 2] = b[i].z; }
+        if (energy) energy[i] = a[i].w;
+        if (time) time[i] = b[i].w;
+        if (pid) pid[i] = id.empty() ? -1 : (int64_t)id[i];
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* qs, uint64_t nq, int k,
+                       int32_t* idx, double* dist) {
+    if (!ctx || !pts || !qs || !idx || !dist || k < 1 || k > 256) return ALB_ERR_INVALID;
+    if (m < (uint64_t)k) return fail(ctx, ALB_ERR_TOO_FEW, "fewer points than k");
+    CK(cudaSetDevice(ctx->device));
+    // the record's w lane carries its original index (bit pattern) through the sort
+    std::vector<float4> ha(m);
+    for (uint64_t i = 0; i < m; ++i) {
+        uint32_t tag = (uint32_t)i;
+        float w;
+        std::memcpy(&w, &tag, 4);
+        ha[i] = make_float4(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], w);
+    }
+    RecordStore r{};
+    size_t mark = ctx->ws.mark();
+    r.a = (float4*)ctx->ws.take_bytes(m * 16);
+    r.b = (float4*)ctx->ws.take_bytes(m * 16);
+    double* dq = (double*)ctx->ws.take_bytes(nq * 24);
+    int32_t* di = (int32_t*)ctx->ws.take_bytes(nq * k * 4);
+    double* dd = (double*)ctx->ws.take_bytes(nq * k * 8);
+    if (!r.a || !r.b || !dq || !di || !dd) return fail(ctx, ALB_ERR_CUDA, "knn allocation failed");
+    CK(cudaMemcpyAsync(r.a, ha.data(), m * 16, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(r.b, 0, m * 16, ctx->st));
+    CK(cudaMemcpyAsync(dq, qs, nq * 24, cudaMemcpyHostToDevice, ctx->st));
+    MapIndex mi;
+    build_map_index(ctx->ws, r, m, mi, ctx->st);
+    // indices returned by the search refer to the sorted order: map them back
+    launch_knn(map_dev(mi), dq, nq, k, di, dd, ctx->d_err, ctx->st);
+    std::vector<int32_t> sorted_idx(nq * k);
+    int rc = check_device(ctx, "knn");
+    if (rc) return rc;
+    CK(cudaMemcpy(sorted_idx.data(), di, nq * k * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dist, dd, nq * k * 8, cudaMemcpyDeviceToHost));
+    std::vector<float4> sa(m);
+    CK(cudaMemcpy(sa.data(), mi.a, m * 16, cudaMemcpyDeviceToHost));
+    cudaFree(mi.a); cudaFree(mi.b); cudaFree(mi.box_lo); cudaFree(mi.box_hi);
+    ctx->ws.release(mark);
+    for (uint64_t i = 0; i < nq * (uint64_t)k; ++i) {
+        uint32_t tag;
+        std::memcpy(&tag, &sa[sorted_idx[i]].w, 4);
+        idx[i] = (int32_t)tag;
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_stats(AlbCtx* ctx, int64_t* out, int n) {
+    if (!ctx || !out) return ALB_ERR_INVALID;
+    unsigned long long s[16];
+    CK(cudaMemcpy(s, ctx->d_stats, sizeof s, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n && i < 16; ++i) out[i] = (int64_t)s[i];
+    if (n > 2) out[2] = launches_total();
+    return ALB_OK;
+}
+
+extern "C" int alb_phase_times(AlbCtx* ctx, double* ms, int64_t* calls, int64_t* gathers, int reset) {
+    if (!ctx) return ALB_ERR_INVALID;
+    for (int i = 0; i < ALB_PHASES; ++i) {
+        if (ms) ms[i] = ctx->phase_ms[i];
+        if (calls) calls[i] = ctx->phase_calls[i];
+    }
+    if (gathers)
+        for (int c = 0; c < ALB_CHANNELS; ++c) gathers[c] = ctx->gathered[c];
+    if (reset) {
+        for (int i = 0; i < ALB_PHASES; ++i) {
+            ctx->phase_ms[i] = 0.0;
+            ctx->phase_calls[i] = 0;
+        }
+        for (int c = 0; c < ALB_CHANNELS; ++c) ctx->gathered[c] = 0;
+    }
+    return ALB_OK;
+}

@@ -1,0 +1,518 @@
+// Photon-map gather: exact k-nearest-neighbour density estimation at every backward event
+// and time-binned waveform accumulation. GPU form of Simulation.sample_photons
+// (alb_sim/core/simulation.py:132-214) with scipy KDTree.query(x, k) as the neighbour
+// search (alb_sim/photon_mapping/photon_map_index.py:17).
+//
+// One warp per query. The warp walks the 32-ary box tree depth first, nearest child
+// first (children sorted by box distance with a warp bitonic sort), keeps candidates in a
+// shared-memory buffer and shrinks it to the k best with a warp radix select whenever it
+// fills. Distances are float32 for the search; the threshold carries a relative margin
+// of 2^-18 so that every point whose float64 distance could rank at the k-th place
+// survives, and the boundary band is resolved with float64 distances exactly as the
+// reference's KDTree (float64 on float32-cast map positions) orders them.
+#include <cfloat>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace alb {
+
+constexpr int kGatherWarps = 4;
+constexpr int kStack = 32 * kMaxLevels;
+constexpr int kCap = 288;        // candidate buffer; shrunk when more than kCap-32 are held
+constexpr float kRelMargin = 3.814697265625e-06f;  // 2^-18
+
+struct WarpSmem {
+    uint32_t stk[kStack];
+    float stk_d[kStack];
+    float cd[kCap];
+    uint32_t ci[kCap];
+    uint32_t hist[256];
+    double bd[64];      // boundary band: float64 distances
+    uint32_t bi[64];
+};
+
+// Lower bound of the squared distance from the float64 query (qx + lx, ...) to a box:
+// the float32 per-axis gap is shrunk by its rounding bound and by the dropped low part,
+// so that pruning never discards a box the float64 search would have to open.
+ALB_DEVICE float box_gap(float lo, float hi, float q, float ql) {
+    float g = fmaxf(fmaxf(lo - q, q - hi), 0.f);
+    return fmaxf(g * (1.f - 2.384185791015625e-07f) - fabsf(ql), 0.f);
+}
+ALB_DEVICE float box_dist2(float qx, float qy, float qz, float lx, float ly, float lz, float4 lo, float4 hi) {
+    float dx = box_gap(lo.x, hi.x, qx, lx);
+    float dy = box_gap(lo.y, hi.y, qy, ly);
+    float dz = box_gap(lo.z, hi.z, qz, lz);
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz)) * (1.f - 4.76837158203125e-07f);
+}
+
+// float32 distance of a map point to the query (hi + lo split of the float64 position)
+ALB_DEVICE float point_dist2(float qx, float qy, float qz, float lx, float ly, float lz, float4 p) {
+    float dx = (p.x - qx) - lx;
+    float dy = (p.y - qy) - ly;
+    float dz = (p.z - qz) - lz;
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+ALB_DEVICE double point_dist2_f64(double qx, double qy, double qz, float4 p) {
+    double dx = (double)p.x - qx, dy = (double)p.y - qy, dz = (double)p.z - qz;
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// Warp bitonic sort of 32 (key, value) pairs, ascending by key.
+ALB_DEVICE void warp_sort32(float& key, uint32_t& val) {
+    const int l = lane_id();
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            float ok = __shfl_xor_sync(0xffffffffu, key, j);
+            uint32_t ov = __shfl_xor_sync(0xffffffffu, val, j);
+            bool up = ((l & k) == 0);
+            bool lower = ((l & j) == 0);
+            bool take_other = lower ? (up ? ok < key : ok > key) : (up ? ok > key : ok < key);
+            if (take_other) {
+                key = ok;
+                val = ov;
+            }
+        }
+    }
+}
+
+// k-th smallest (1-based) of cnt float distances in cd[] (all >= 0): warp radix select.
+ALB_DEVICE float warp_kth(WarpSmem& s, int cnt, int k) {
+    const int l = lane_id();
+    uint32_t prefix = 0u, pmask = 0u;
+    int need = k;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int i = l; i < 256; i += 32) s.hist[i] = 0u;
+        __syncwarp();
+        for (int i = l; i < cnt; i += 32) {
+            uint32_t u = __float_as_uint(s.cd[i]);
+            if ((u & pmask) == prefix) atomicAdd(&s.hist[(u >> shift) & 255u], 1u);
+        }
+        __syncwarp();
+        // inclusive scan over 256 bins, 8 per lane
+        uint32_t h[8], run = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            h[j] = s.hist[l * 8 + j];
+            run += h[j];
+        }
+        uint32_t incl = run;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (l >= o) incl += t;
+        }
+        uint32_t before = incl - run;
+        int digit = -1;
+        uint32_t below = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (digit < 0 && before + h[j] >= (uint32_t)need) {
+                digit = l * 8 + j;
+                below = before;
+            }
+            before += h[j];
+        }
+        unsigned who = __ballot_sync(0xffffffffu, digit >= 0);
+        int src = __ffs(who) - 1;
+        digit = __shfl_sync(0xffffffffu, digit, src);
+        below = __shfl_sync(0xffffffffu, below, src);
+        prefix |= ((uint32_t)digit) << shift;
+        pmask |= 255u << shift;
+        need -= (int)below;
+        __syncwarp();
+    }
+    return __uint_as_float(prefix);
+}
+
+// Keep the candidates with distance <= thr (order not preserved).
+ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
+    const int l = lane_id();
+    int out = 0;
+    for (int base = 0; base < cnt; base += 32) {
+        int i = base + l;
+        float d = i < cnt ? s.cd[i] : FLT_MAX;
+        uint32_t id = i < cnt ? s.ci[i] : 0u;
+        bool keep = i < cnt && d <= thr;
+        unsigned b = __ballot_sync(0xffffffffu, keep);
+        __syncwarp();
+        if (keep) {
+            int pos = out + __popc(b & lanemask_lt());
+            s.cd[pos] = d;
+            s.ci[pos] = id;
+        }
+        out += __popc(b);
+        __syncwarp();
+    }
+    return out;
+}
+
+struct KnnResult {
+    int n_in;          // candidates in cd/ci that are definitely among the k nearest
+    int n_band_take;   // band entries bi[0..n_band_take) also taken
+    double rk;         // float64 distance of the k-th neighbour
+};
+
+// Full k-NN search for one query. Returns false when the map has fewer than k records.
+ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz,
+                         KnnResult& res) {
+    const int l = lane_id();
+    const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+    const float lx = (float)(qx - (double)fx), ly = (float)(qy - (double)fy), lz = (float)(qz - (double)fz);
+    if (m.n < (uint64_t)k) return false;
+    float thr = FLT_MAX;  // admission threshold (float32 squared distance, with margin)
+    int cnt = 0;
+    int sp = 0;
+    // roots
+    {
+        int top = m.nlevels - 1;
+        uint64_t ntop = m.lvl_cnt[top];
+        float d = FLT_MAX;
+        uint32_t c = (uint32_t)l;
+        if ((uint64_t)l < ntop) d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[top] + l], m.box_hi[m.lvl_off[top] + l]);
+        warp_sort32(d, c);
+        unsigned b = __ballot_sync(0xffffffffu, d < FLT_MAX);
+        int nv = __popc(b);
+        if (l < nv) {
+            s.stk[sp + nv - 1 - l] = ((uint32_t)top << 29) | c;
+            s.stk_d[sp + nv - 1 - l] = d;
+        }
+        sp += nv;
+        __syncwarp();
+    }
+    int guard = 0;
+    while (sp > 0) {
+        if (++guard > (1 << 22)) break;
+        --sp;
+        uint32_t e = s.stk[sp];
+        float ed = s.stk_d[sp];
+        __syncwarp();
+        if (ed > thr) continue;
+        int lev = (int)(e >> 29);
+        uint32_t node = e & 0x1fffffffu;
+        if (lev == 0) {
+            uint64_t i = (uint64_t)node * 32 + l;
+            float d = FLT_MAX;
+            if (i < m.n) d = point_dist2(fx, fy, fz, lx, ly, lz, m.a[i]);
+            bool take = d <= thr;
+            unsigned b = __ballot_sync(0xffffffffu, take);
+            if (take) {
+                int pos = cnt + __popc(b & lanemask_lt());
+                s.cd[pos] = d;
+                s.ci[pos] = (uint32_t)i;
+            }
+            cnt += __popc(b);
+            __syncwarp();
+            if (cnt >= k && (thr == FLT_MAX || cnt > kCap - 32)) {
+                float kth = warp_kth(s, cnt, k);
+                thr = kth * (1.0f + 2.0f * kRelMargin);
+                cnt = warp_compact(s, cnt, thr);
+                if (cnt > kCap - 32) {  // pathological ties: fall back to the bare threshold
+                    thr = kth;
+                    cnt = warp_compact(s, cnt, thr);
+                }
+            }
+        } else {
+            uint64_t c = (uint64_t)node * 32 + l;
+            float d = FLT_MAX;
+            int cl = lev - 1;
+            if (c < m.lvl_cnt[cl]) {
+                d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[cl] + c], m.box_hi[m.lvl_off[cl] + c]);
+                if (d > thr) d = FLT_MAX;
+            }
+            uint32_t cc = (uint32_t)c;
+            warp_sort32(d, cc);
+            unsigned b = __ballot_sync(0xffffffffu, d < FLT_MAX);
+            int nv = __popc(b);
+            if (l < nv) {
+                s.stk[sp + nv - 1 - l] = ((uint32_t)cl << 29) | cc;
+                s.stk_d[sp + nv - 1 - l] = d;
+            }
+            sp += nv;
+            __syncwarp();
+        }
+    }
+    // final: exact k with the float64 boundary band
+    float kth = warp_kth(s, cnt, k);
+    float band_lo = kth * (1.0f - 2.0f * kRelMargin);
+    float band_hi = kth * (1.0f + 2.0f * kRelMargin);
+    // partition: definitely-in to the front, band to bd/bi
+    int n_in = 0, n_band = 0;
+    for (int base = 0; base < cnt; base += 32) {
+        int i = base + l;
+        float d = i < cnt ? s.cd[i] : FLT_MAX;
+        uint32_t id = i < cnt ? s.ci[i] : 0u;
+        bool in = i < cnt && d < band_lo;
+        bool band = i < cnt && d >= band_lo && d <= band_hi;
+        unsigned bin = __ballot_sync(0xffffffffu, in);
+        unsigned bb = __ballot_sync(0xffffffffu, band);
+        __syncwarp();
+        if (in) {
+            int pos = n_in + __popc(bin & lanemask_lt());
+            s.cd[pos] = d;
+            s.ci[pos] = id;
+        }
+        if (band) {
+            int pos = n_band + __popc(bb & lanemask_lt());
+            if (pos < 64) {
+                s.bi[pos] = id;
+                s.bd[pos] = point_dist2_f64(qx, qy, qz, m.a[id]);
+            }
+        }
+        n_in += __popc(bin);
+        n_band += __popc(bb);
+        __syncwarp();
+    }
+    if (n_band > 64) n_band = 64;
+    int take = k - n_in;
+    // rank band entries by (float64 distance, index); keep the `take` smallest, in rank order
+    double rk2 = 0.0;
+    for (int base = 0; base < n_band; base += 32) {
+        int i = base + l;
+        int rank = 0;
+        double di = 0.0;
+        uint32_t ii = 0;
+        if (i < n_band) {
+            di = s.bd[i];
+            ii = s.bi[i];
+            for (int j = 0; j < n_band; ++j) {
+                double dj = s.bd[j];
+                uint32_t ij = s.bi[j];
+                rank += (dj < di || (dj == di && ij < ii)) ? 1 : 0;
+            }
+        }
+        __syncwarp();
+        if (i < n_band && rank < take) {
+            s.hist[rank] = ii;  // reuse as the taken list, ordered by rank
+            if (rank == take - 1) rk2 = di;
+        }
+        __syncwarp();
+    }
+    // broadcast the k-th distance (lane holding rank take-1)
+    double rk2_all = rk2;
+    for (int o = 16; o > 0; o >>= 1) rk2_all = fmax(rk2_all, __shfl_xor_sync(0xffffffffu, rk2_all, o));
+    res.n_in = n_in;
+    res.n_band_take = take;
+    res.rk = sqrt(rk2_all);
+    __syncwarp();
+    return true;
+}
+
+ALB_DEVICE uint32_t knn_index(const WarpSmem& s, const KnnResult& r, int j) {
+    return j < r.n_in ? s.ci[j] : s.hist[j - r.n_in];
+}
+
+// ----------------------------------------------------------------------------------------
+// per-neighbour weights (float32 restatement of the reference's energy multipliers)
+// ----------------------------------------------------------------------------------------
+
+// GGX Cook-Torrance, alb_sim/physics/reflection/microfacet_brdf.py:96-147, with
+// wi = normalize(-d_map), wo = normalize(-d_query), n = +y.
+ALB_DEVICE float ggx_weight(float a2, float f0, float wix, float wiy, float wiz, float wox, float woy, float woz) {
+    float ni = rsqrtf(fmaf(wix, wix, fmaf(wiy, wiy, wiz * wiz)));
+    wix *= ni; wiy *= ni; wiz *= ni;
+    float hx = wix + wox, hy = wiy + woy, hz = wiz + woz;
+    float hn = sqrtf(fmaf(hx, hx, fmaf(hy, hy, hz * hz)));
+    if (hn > 0.f) { hx /= hn; hy /= hn; hz /= hn; }
+    float n_wi = fminf(fmaxf(wiy, 0.f), 1.f);
+    float n_wo = fminf(fmaxf(woy, 0.f), 1.f);
+    if (!(n_wi > 0.f && n_wo > 0.f)) return 0.f;
+    float wi_h = fminf(fmaxf(fmaf(wix, hx, fmaf(wiy, hy, wiz * hz)), 0.f), 1.f);
+    float n_h = fminf(fmaxf(hy, 0.f), 1.f);
+    float den = fmaf(a2 - 1.f, n_h * n_h, 1.f);
+    float D = a2 / (3.14159265358979f * den * den + kEps32);
+    float g1i = 2.f * n_wi / (n_wi + sqrtf(fmaf(1.f - a2, n_wi * n_wi, a2)));
+    float g1o = 2.f * n_wo / (n_wo + sqrtf(fmaf(1.f - a2, n_wo * n_wo, a2)));
+    float x = 1.f - wi_h;
+    float x2 = x * x;
+    float F = f0 + (1.f - f0) * (x2 * x2 * x);
+    return (D * g1i * g1o * F) / (4.f * n_wi * n_wo + kEps32);
+}
+
+// Scatter weight: CDF mass of the angular bin of theta = acos(d_map . view),
+// alb_sim/physics/scatter/energy.py:8-52 (view = normalize(-d_query)).
+ALB_DEVICE float scatter_weight(const SceneDev& sc, int layer, float dx, float dy, float dz, float vx, float vy, float vz) {
+    float n = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    float c = fmaf(dx, vx, fmaf(dy, vy, dz * vz)) * n;
+    c = fminf(fmaxf(c, -1.f), 1.f);
+    float th = acosf(c);
+    int i = (int)((th - kEps32) / sc.layer_binw[layer]);
+    i = min(max(i, 0), ALB_PHASE_DIVISIONS - 1);
+    return __ldg(sc.layer_weight[layer] + i);
+}
+
+// float32 -> 128-bit fixed point (64 fractional bits), integer ops only.
+ALB_DEVICE Fix128 f32_to_fix(float v) {
+    Fix128 r{0ull, 0ll};
+    uint32_t b = __float_as_uint(v);
+    uint32_t ex = (b >> 23) & 0xffu;
+    if (ex == 0u || ex == 255u) return r;  // zero / subnormal / inf / nan contribute nothing
+    uint64_t mant = (uint64_t)((b & 0x7fffffu) | 0x800000u);
+    int sh = (int)ex - 150 + 64;  // value * 2^64 = mant * 2^sh
+    uint64_t lo = 0ull, hi = 0ull;
+    if (sh > 86) {
+        lo = ~0ull;
+        hi = 0x7fffffffffffffffull;
+    } else if (sh >= 64) {
+        hi = mant << (sh - 64);
+    } else if (sh > 40) {
+        lo = mant << sh;
+        hi = mant >> (64 - sh);
+    } else if (sh >= 0) {
+        lo = mant << sh;
+    } else if (sh > -24) {
+        lo = mant >> (-sh);
+    }
+    if (b & 0x80000000u) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    r.lo = lo;
+    r.hi = (long long)hi;
+    return r;
+}
+
+template <int CHANNEL>
+__global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
+                                                              int* err) {
+    __shared__ WarpSmem smem[kGatherWarps];
+    const int w = threadIdx.x >> 5, l = lane_id();
+    WarpSmem& s = smem[w];
+    const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
+    for (uint64_t qi = (uint64_t)blockIdx.x * kGatherWarps + w; qi < q.n; qi += warps) {
+        uint64_t src = q.perm ? q.perm[qi] : qi;
+        float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
+        double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
+        KnnResult r;
+        if (!warp_knn(m, s, k, qx, qy, qz, r)) {
+            if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
+            return;
+        }
+        if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
+        const float Es = qa.w, ts = qb.w;
+        const float rk = (float)r.rk;
+        float norm;
+        if (CHANNEL == ALB_SCATTER) norm = 1.0f / ((4.0f / 3.0f) * 3.14159265358979f * rk * rk * rk);
+        else norm = 1.0f / (3.14159265358979f * rk * rk);
+        // query-constant pieces
+        float vinv = rsqrtf(fmaf(qb.x, qb.x, fmaf(qb.y, qb.y, qb.z * qb.z)));
+        float vx = -qb.x * vinv, vy = -qb.y * vinv, vz = -qb.z * vinv;  // normalize(-d_query)
+        float wconst = 0.f;
+        if (CHANNEL == ALB_BOTTOM_REFLECTION) wconst = (float)(sc.floor_albedo / kPi) * fmaxf(0.f, -qb.y);
+        if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
+        // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
+        const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
+        for (int j = l; j < k; j += 32) {
+            uint32_t idx = knn_index(s, r, j);
+            float4 pa = m.a[idx], pb = m.b[idx];
+            float w;
+            if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+            else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+            else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+            float c = ((Es * pa.w) * norm) * w;
+            int bin = (int)((ts + pb.w) / (float)sc.mult);
+            if (bin >= 0 && bin < acc.nbins) {
+                Fix128 f = f32_to_fix(c);
+                uint64_t o = (uint64_t)CHANNEL * acc.nbins + bin;
+                fix_atomic_add(acc.wf_lo + o, acc.wf_hi + o, f);
+            } else {
+                atomicCAS(err, 0, ALB_ERR_CAPACITY);
+            }
+            if (acc.hw_lo && m.fwi) {
+                // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61
+                float4 fw = m.fwi[idx], sf = m.sfi[idx];
+                Fix128 f = f32_to_fix(c);
+                if (fw.x == fw.x) {
+                    long long xi = (long long)(((double)fw.x - sc.wc[0] + sc.hm_wext) / sc.hm_wbin);
+                    long long zi = (long long)(((double)fw.z - sc.wc[2] + sc.hm_wext) / sc.hm_wbin);
+                    if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+                        fix_atomic_add(acc.hw_lo + xi * sc.hm_bins + zi, acc.hw_hi + xi * sc.hm_bins + zi, f);
+                }
+                if (sf.x == sf.x) {
+                    long long xi = (long long)(((double)sf.x - sc.fc[0] + sc.hm_fext) / sc.hm_fbin);
+                    long long zi = (long long)(((double)sf.z - sc.fc[2] + sc.hm_fext) / sc.hm_fbin);
+                    if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+                        fix_atomic_add(acc.hf_lo + xi * sc.hm_bins + zi, acc.hf_hi + xi * sc.hm_bins + zi, f);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Standalone KDTree.query(x, k): sorted indices and float64 distances.
+__global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const double* __restrict__ qs, uint64_t nq,
+                                                           int k, int32_t* out_idx, double* out_dist, int* err) {
+    __shared__ WarpSmem smem[kGatherWarps];
+    const int w = threadIdx.x >> 5, l = lane_id();
+    WarpSmem& s = smem[w];
+    const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
+    for (uint64_t qi = (uint64_t)blockIdx.x * kGatherWarps + w; qi < nq; qi += warps) {
+        double qx = qs[3 * qi], qy = qs[3 * qi + 1], qz = qs[3 * qi + 2];
+        KnnResult r;
+        if (!warp_knn(m, s, k, qx, qy, qz, r)) {
+            if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
+            return;
+        }
+        // float64 distances of the k neighbours, then rank-sort them (k <= kMaxK)
+        for (int j = l; j < k; j += 32) {
+            uint32_t idx = knn_index(s, r, j);
+            double d = point_dist2_f64(qx, qy, qz, m.a[idx]);
+            int rank = 0;
+            for (int t = 0; t < k; ++t) {
+                uint32_t it = knn_index(s, r, t);
+                double dt = point_dist2_f64(qx, qy, qz, m.a[it]);
+                rank += (dt < d || (dt == d && it < idx)) ? 1 : 0;
+            }
+            out_idx[qi * k + rank] = (int32_t)idx;
+            out_dist[qi * k + rank] = sqrt(d);
+        }
+        __syncwarp();
+    }
+}
+
+static unsigned gather_blocks(uint64_t nq) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t want = (nq + kGatherWarps - 1) / kGatherWarps;
+    uint64_t cap = (uint64_t)sms * 16;
+    return (unsigned)(want < cap ? (want ? want : 1) : cap);
+}
+
+void launch_gather(const SceneDev& sc, const MapDev& map, const QueryDev& q, int channel, const Accum& acc,
+                   int* err, int* launches, cudaStream_t st) {
+    if (q.n == 0) return;
+    unsigned blocks = gather_blocks(q.n);
+    int k = sc.k;
+    switch (channel) {
+        case ALB_BOTTOM_REFLECTION:
+            k_gather<ALB_BOTTOM_REFLECTION><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            note_launch();
+            break;
+        case ALB_SCATTER:
+            k_gather<ALB_SCATTER><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            note_launch();
+            break;
+        case ALB_SURFACE_REFLECTION:
+            k_gather<ALB_SURFACE_REFLECTION><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            note_launch();
+            break;
+        default:
+            k_gather<ALB_SURFACE_TRANSMISSION_UP><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            note_launch();
+            break;
+    }
+    if (launches) ++*launches;
+}
+
+void launch_knn(const MapDev& map, const double* queries, uint64_t nq, int k, int32_t* out_idx, double* out_dist,
+                int* err, cudaStream_t st) {
+    if (nq == 0) return;
+    k_knn<<<gather_blocks(nq), kGatherWarps * 32, 0, st>>>(map, queries, nq, k, out_idx, out_dist, err);
+    note_launch();
+}
+
+}  // namespace alb

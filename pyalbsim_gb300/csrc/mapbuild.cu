@@ -1,0 +1,512 @@
+// Photon-map index build: the GPU replacement of build_photon_map_data + PhotonMapIndex
+// (alb_sim/photon_mapping/build_photon_map_data.py:8-62, photon_map_index.py:6-17).
+//
+// Records are ordered along a Morton curve of a uniform grid over the map's bounding box
+// (cell key = interleaved cell coordinates, 32 bits) by an LSD radix sort, permuted into
+// that order as two float4 streams, and cut into buckets of 32 consecutive records. A
+// bucket's bounding box is a leaf; 32 consecutive boxes form the next level up, until 32
+// or fewer boxes remain. The gather walks this implicit 32-ary box tree warp-wide.
+#include <algorithm>
+#include <cstdio>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace alb {
+
+// ------------------------------------------------------------------------------------------
+// bounding box
+// ------------------------------------------------------------------------------------------
+
+ALB_DEVICE unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+ALB_HOST_DEVICE float ord2f(unsigned u) {
+    unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+// box[0..2] = ordered-min of x,y,z, box[3..5] = ordered-max; initialised to (~0, 0).
+__global__ void k_bbox(const float4* __restrict__ a, const float4* __restrict__ c, uint64_t n,
+                       unsigned* box) {
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float4 p = a[i];
+        float x = p.x, y = p.y, z = p.z;
+        if (c) {  // query streams carry a low part; the box only needs the float part
+            (void)c;
+        }
+        lo[0] = fminf(lo[0], x); hi[0] = fmaxf(hi[0], x);
+        lo[1] = fminf(lo[1], y); hi[1] = fmaxf(hi[1], y);
+        lo[2] = fminf(lo[2], z); hi[2] = fmaxf(hi[2], z);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(box + k, f2ord(lo[k]));
+            atomicMax(box + 3 + k, f2ord(hi[k]));
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Morton keys
+// ------------------------------------------------------------------------------------------
+
+ALB_DEVICE uint32_t part1by1(uint32_t x) {  // 16 bits -> even bits
+    x &= 0x0000ffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+ALB_DEVICE uint32_t part1by2(uint32_t x) {  // 10 bits -> every third bit
+    x &= 0x000003ffu;
+    x = (x | (x << 16)) & 0xff0000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+ALB_DEVICE uint32_t morton_key(const KeyGrid& g, float x, float y, float z) {
+    float v[3] = {x, y, z};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float t = (v[k] - g.lo[k]) * g.scale[k];
+        t = fminf(fmaxf(t, 0.0f), (float)g.maxq[k]);
+        q[k] = (uint32_t)t;
+    }
+    if (g.naxes == 3) return part1by2(q[0]) | (part1by2(q[1]) << 1) | (part1by2(q[2]) << 2);
+    if (g.naxes == 2) return part1by1(q[g.ax[0]]) | (part1by1(q[g.ax[1]]) << 1);
+    if (g.naxes == 1) return q[g.ax[0]];
+    return 0u;
+}
+
+__global__ void k_keys(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n,
+                       KeyGrid g, uint32_t* keys, uint32_t* vals, unsigned* or_and) {
+    unsigned o = 0u, an = 0xffffffffu;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float4 p = a[i];
+        uint32_t key = morton_key(g, p.x, p.y, p.z);
+        keys[i] = key;
+        vals[i] = (uint32_t)i;
+        o |= key;
+        an &= key;
+    }
+    (void)perm;
+    for (int s = 16; s > 0; s >>= 1) {
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+        an &= __shfl_xor_sync(0xffffffffu, an, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicOr(or_and, o);
+        atomicAnd(or_and + 1, an);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// LSD radix sort of (u32 key, u32 value), 8-bit digits, stable.
+// Tile = 8 warps x 16 rounds x 32 lanes; key t of warp w, round j, lane l is
+// tile_base + w*512 + j*32 + l, so ranking warps in order, rounds in order and lanes in
+// order preserves the input order of equal digits.
+// ------------------------------------------------------------------------------------------
+constexpr int kRsWarps = 8, kRsItems = 16, kRsThreads = kRsWarps * 32;
+constexpr int kRsTile = kRsThreads * kRsItems;
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restrict__ keys, uint64_t n,
+                                                         int shift, uint32_t* hist, uint32_t ntiles) {
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * kRsTile;
+    for (int j = threadIdx.x; j < kRsTile; j += kRsThreads) {
+        uint64_t i = base + j;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += kRsThreads) hist[(uint64_t)d * ntiles + blockIdx.x] = h[d];
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __restrict__ kin,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ kout,
+                                                            uint32_t* __restrict__ vout, uint64_t n,
+                                                            int shift, const uint32_t* __restrict__ offs,
+                                                            uint32_t ntiles) {
+    __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t goff[256];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
+    for (int d = threadIdx.x; d < 256; d += kRsThreads) goff[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * kRsTile + (uint64_t)w * (kRsItems * 32);
+    uint32_t key[kRsItems], val[kRsItems], rank[kRsItems];
+    const unsigned lt = lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < kRsItems; ++j) {
+        uint64_t i = base + (uint64_t)j * 32 + l;
+        bool valid = i < n;
+        key[j] = valid ? kin[i] : 0u;
+        val[j] = valid ? vin[i] : 0u;
+        unsigned act = __ballot_sync(0xffffffffu, valid);
+        rank[j] = 0;
+        if (valid) {
+            uint32_t d = (key[j] >> shift) & 255u;
+            unsigned peers = __match_any_sync(act, d);
+            uint32_t cur = wcnt[w][d];
+            __syncwarp(act);
+            rank[j] = cur + __popc(peers & lt);
+            if (l == __ffs(peers) - 1) wcnt[w][d] = cur + __popc(peers);
+            __syncwarp(act);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int ww = 0; ww < kRsWarps; ++ww) {
+            uint32_t c = wcnt[ww][threadIdx.x];
+            wcnt[ww][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRsItems; ++j) {
+        uint64_t i = base + (uint64_t)j * 32 + l;
+        if (i < n) {
+            uint32_t d = (key[j] >> shift) & 255u;
+            uint32_t dst = goff[d] + wcnt[w][d] + rank[j];
+            kout[dst] = key[j];
+            vout[dst] = val[j];
+        }
+    }
+}
+
+// Exclusive scan of u32 (device-wide, recursive over block sums).
+constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile(uint32_t* data, uint64_t n, uint32_t* sums) {
+    __shared__ uint32_t warp_tot[kScanThreads / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t acc = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        uint64_t i = base + j;
+        v[j] = i < n ? data[i] : 0u;
+        acc += v[j];
+    }
+    // exclusive scan of per-thread totals across the block
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = acc;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (l >= o) incl += t;
+    }
+    if (l == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = l < kScanThreads / 32 ? warp_tot[l] : 0u;
+        uint32_t ti = t;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (l >= o) ti += u;
+        }
+        if (l < kScanThreads / 32) warp_tot[l] = ti - t;
+        if (l == kScanThreads / 32 - 1 && sums) sums[blockIdx.x] = ti;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[w] + incl - acc;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        uint64_t i = base + j;
+        if (i < n) data[i] = run;
+        run += v[j];
+    }
+}
+
+__global__ void k_scan_add(uint32_t* data, uint64_t n, const uint32_t* sums) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) data[i] += sums[i / kScanTile];
+}
+
+static void exclusive_scan(Workspace& ws, uint32_t* data, uint64_t n, cudaStream_t st) {
+    uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles <= 1) {
+        k_scan_tile<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
+        note_launch();
+        return;
+    }
+    uint32_t* sums = ws.take_u32(tiles);
+    k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, st>>>(data, n, sums);
+    note_launch();
+    exclusive_scan(ws, sums, tiles, st);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(data, n, sums);
+    note_launch();
+}
+
+int radix_sort_pairs(Workspace& ws, uint32_t*& keys, uint32_t*& vals, uint32_t*& keys_alt,
+                     uint32_t*& vals_alt, uint64_t n, uint32_t varying_bits, cudaStream_t st) {
+    if (n <= 1) return 0;
+    const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
+    size_t mark = ws.mark();
+    uint32_t* hist = ws.take_u32((uint64_t)ntiles * 256);
+    int passes = 0;
+    for (int shift = 0; shift < 32; shift += 8) {
+        if (((varying_bits >> shift) & 255u) == 0u) continue;  // digit constant over all keys
+        k_rs_hist<<<ntiles, kRsThreads, 0, st>>>(keys, n, shift, hist, ntiles);
+        note_launch();
+        exclusive_scan(ws, hist, (uint64_t)ntiles * 256, st);
+        k_rs_scatter<<<ntiles, kRsThreads, 0, st>>>(keys, vals, keys_alt, vals_alt, n, shift, hist, ntiles);
+        note_launch();
+        std::swap(keys, keys_alt);
+        std::swap(vals, vals_alt);
+        ++passes;
+    }
+    ws.release(mark);
+    return passes;
+}
+
+// ------------------------------------------------------------------------------------------
+// permutation and box tree
+// ------------------------------------------------------------------------------------------
+
+__global__ void k_permute4(const float4* __restrict__ src, const uint32_t* __restrict__ perm,
+                           float4* __restrict__ dst, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+__global__ void k_permute_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ perm,
+                              uint32_t* __restrict__ dst, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+// One warp per leaf: box of 32 consecutive sorted records.
+__global__ void k_leaf_boxes(const float4* __restrict__ a, uint64_t n, float4* lo, float4* hi, uint64_t nleaf) {
+    uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    int l = threadIdx.x & 31;
+    if (warp >= nleaf) return;
+    uint64_t i = warp * 32 + l;
+    float x0 = 3.4e38f, y0 = 3.4e38f, z0 = 3.4e38f, x1 = -3.4e38f, y1 = -3.4e38f, z1 = -3.4e38f;
+    if (i < n) {
+        float4 p = a[i];
+        x0 = x1 = p.x; y0 = y1 = p.y; z0 = z1 = p.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        z0 = fminf(z0, __shfl_xor_sync(0xffffffffu, z0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        z1 = fmaxf(z1, __shfl_xor_sync(0xffffffffu, z1, o));
+    }
+    if (l == 0) {
+        lo[warp] = make_float4(x0, y0, z0, 0.f);
+        hi[warp] = make_float4(x1, y1, z1, 0.f);
+    }
+}
+
+// One warp per parent: union of up to 32 child boxes.
+__global__ void k_parent_boxes(const float4* __restrict__ clo, const float4* __restrict__ chi, uint64_t nchild,
+                               float4* plo, float4* phi, uint64_t nparent) {
+    uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    int l = threadIdx.x & 31;
+    if (warp >= nparent) return;
+    uint64_t i = warp * 32 + l;
+    float x0 = 3.4e38f, y0 = 3.4e38f, z0 = 3.4e38f, x1 = -3.4e38f, y1 = -3.4e38f, z1 = -3.4e38f;
+    if (i < nchild) {
+        float4 a = clo[i], b = chi[i];
+        x0 = a.x; y0 = a.y; z0 = a.z; x1 = b.x; y1 = b.y; z1 = b.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        z0 = fminf(z0, __shfl_xor_sync(0xffffffffu, z0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        z1 = fmaxf(z1, __shfl_xor_sync(0xffffffffu, z1, o));
+    }
+    if (l == 0) {
+        plo[warp] = make_float4(x0, y0, z0, 0.f);
+        phi[warp] = make_float4(x1, y1, z1, 0.f);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host drivers
+// ------------------------------------------------------------------------------------------
+
+KeyGrid make_key_grid(const float lo[3], const float hi[3]) {
+    KeyGrid g{};
+    float ext[3], emax = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        ext[k] = hi[k] - lo[k];
+        emax = std::max(emax, ext[k]);
+    }
+    int na = 0;
+    for (int k = 0; k < 3; ++k) {
+        g.lo[k] = lo[k];
+        // an axis with (almost) no extent carries no key bits (planar surface/floor maps)
+        if (ext[k] > 1e-6f * std::max(emax, 1e-30f) && ext[k] > 0.f) g.ax[na++] = k;
+    }
+    g.naxes = na;
+    int bits = na == 3 ? 10 : (na == 2 ? 16 : 32);
+    for (int k = 0; k < 3; ++k) {
+        bool active = false;
+        for (int j = 0; j < na; ++j) active |= (g.ax[j] == k);
+        if (!active) {
+            g.scale[k] = 0.f;
+            g.maxq[k] = 0u;
+            continue;
+        }
+        double maxq = bits >= 32 ? 4294967040.0 : (double)((1u << bits) - 1u);
+        g.maxq[k] = (uint32_t)maxq;
+        g.scale[k] = (float)(maxq / (double)ext[k]);
+    }
+    return g;
+}
+
+int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st) {
+    uint64_t n = m.n;
+    uint64_t cnt = (n + 31) / 32;
+    int lev = 0;
+    uint64_t off = 0;
+    while (true) {
+        m.lvl_off[lev] = off;
+        m.lvl_cnt[lev] = cnt;
+        off += cnt;
+        ++lev;
+        if (cnt <= 32 || lev >= kMaxLevels) break;
+        cnt = (cnt + 31) / 32;
+    }
+    m.nlevels = lev;
+    m.nboxes = off;
+    m.box_lo = (float4*)ws.alloc_persistent(m.box_lo, m.box_cap, off);
+    m.box_hi = (float4*)ws.alloc_persistent(m.box_hi, m.box_cap_hi, off);
+    uint64_t nl = m.lvl_cnt[0];
+    k_leaf_boxes<<<(unsigned)((nl * 32 + 255) / 256), 256, 0, st>>>(m.a, n, m.box_lo, m.box_hi, nl);
+    note_launch();
+    for (int l = 1; l < m.nlevels; ++l) {
+        uint64_t np = m.lvl_cnt[l];
+        k_parent_boxes<<<(unsigned)((np * 32 + 255) / 256), 256, 0, st>>>(
+            m.box_lo + m.lvl_off[l - 1], m.box_hi + m.lvl_off[l - 1], m.lvl_cnt[l - 1],
+            m.box_lo + m.lvl_off[l], m.box_hi + m.lvl_off[l], np);
+        note_launch();
+    }
+    return 0;
+}
+
+int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st) {
+    unsigned* box = ws.scratch_box();
+    unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 4096);
+    if (blocks == 0) blocks = 1;
+    k_bbox<<<blocks, 256, 0, st>>>(a, nullptr, n, box);
+    note_launch();
+    unsigned h[6];
+    cudaMemcpyAsync(h, box, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = ord2f(h[k]);
+        hi[k] = ord2f(h[3 + k]);
+    }
+    return 0;
+}
+
+// Sort the records of one channel into Morton order and build the box tree.
+int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st) {
+    m.n = n;
+    if (n == 0) {
+        m.nlevels = 0;
+        return 0;
+    }
+    float lo[3], hi[3];
+    compute_bbox(ws, rec.a, n, lo, hi, st);
+    m.grid = make_key_grid(lo, hi);
+    size_t mark = ws.mark();
+    uint32_t* keys = ws.take_u32(n);
+    uint32_t* vals = ws.take_u32(n);
+    uint32_t* keys2 = ws.take_u32(n);
+    uint32_t* vals2 = ws.take_u32(n);
+    unsigned* oa = ws.scratch_box();
+    unsigned init[2] = {0u, 0xffffffffu};
+    cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
+    k_keys<<<blocks, 256, 0, st>>>(rec.a, nullptr, n, m.grid, keys, vals, oa);
+    note_launch();
+    unsigned h[2];
+    cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    radix_sort_pairs(ws, keys, vals, keys2, vals2, n, h[0] ^ h[1], st);
+    m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
+    m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, n);
+    k_permute4<<<blocks, 256, 0, st>>>(rec.a, vals, m.a, n);
+    note_launch();
+    k_permute4<<<blocks, 256, 0, st>>>(rec.b, vals, m.b, n);
+    note_launch();
+    if (rec.fwi) {
+        m.fwi = (float4*)ws.alloc_persistent(m.fwi, m.fwi_cap, n);
+        m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, n);
+        k_permute4<<<blocks, 256, 0, st>>>(rec.fwi, vals, m.fwi, n);
+        note_launch();
+        k_permute4<<<blocks, 256, 0, st>>>(rec.sfi, vals, m.sfi, n);
+        note_launch();
+    }
+    if (rec.id) {
+        m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, n);
+        k_permute_u32<<<blocks, 256, 0, st>>>(rec.id, vals, m.id, n);
+        note_launch();
+    }
+    build_box_tree(ws, m, st);
+    ws.release(mark);
+    return 0;
+}
+
+// Spatial order of gather queries under a map's key grid (for cache locality).
+int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, uint32_t* perm,
+                 cudaStream_t st) {
+    if (n == 0) return 0;
+    size_t mark = ws.mark();
+    uint32_t* keys = ws.take_u32(n);
+    uint32_t* vals = perm;
+    uint32_t* keys2 = ws.take_u32(n);
+    uint32_t* vals2 = ws.take_u32(n);
+    unsigned* oa = ws.scratch_box();
+    unsigned init[2] = {0u, 0xffffffffu};
+    cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
+    k_keys<<<blocks, 256, 0, st>>>(qa, nullptr, n, g, keys, vals, oa);
+    note_launch();
+    unsigned h[2];
+    cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    uint32_t* k0 = keys;
+    uint32_t* v0 = vals;
+    radix_sort_pairs(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st);
+    if (v0 != perm) cudaMemcpyAsync(perm, v0, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    ws.release(mark);
+    return 0;
+}
+
+}  // namespace alb

@@ -1,0 +1,313 @@
+"""Host-side scene model: every constant and table the device kernels consume.
+
+This restates, in float64 NumPy, the parts of the reference model that are evaluated once
+per configuration:
+
+* time step and step count (``alb_sim/physics/models/simulation.py:35-49``);
+* laser axis from DEGREES (``alb_sim/physics/models/laser.py:22-33``) and the float32
+  Rodrigues matrix that rotates +z onto it (``alb_sim/math/rotation_matrix.py:39-102``);
+* Fournier-Forand phase table and CDF on 18000 angles and the backscatter fraction
+  (``alb_sim/physics/scatter/fournier_forand_phase_function.py:9-48, 89-111``);
+* Churnside lidar attenuation alpha and single-scattering albedo (alpha - a) / alpha
+  (``alb_sim/physics/models/water.py:117-184, 237-245``);
+* Schlick base reflectance from the top layer's refractive index
+  (``alb_sim/physics/models/sea_surface.py:30-33``);
+* the per-angular-bin scatter weight table used by the gather
+  (``alb_sim/physics/scatter/energy.py:8-52``).
+
+Any object exposing the reference's config attribute names is accepted, so the
+reference's own ``SimulationConfig`` instances work unchanged.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+LIGHT_SPEED_AIR = 2.998e8
+FLOAT32_EPS = float(np.finfo(np.float32).eps)
+SCATTER_DIVISIONS = 18000
+
+CH_BOTTOM, CH_SCATTER, CH_SURFACE_REFLECTION, CH_SURFACE_TRANSMISSION_UP = 0, 1, 2, 3
+MAX_LAYERS = 8
+
+
+def fournier_forand_table(junge_slope: float, n_ratio: float):
+    """FF phase function p(theta) on 18000 angles in [1e-6, pi] and its normalised CDF.
+
+    The CDF is the running sum of p(theta) * sin(theta) divided by its last element.
+    """
+    theta = np.linspace(1e-6, np.pi, SCATTER_DIVISIONS, dtype=np.float64)
+    nu = (3.0 - junge_slope) / 2.0
+    k = 4.0 / (3.0 * (n_ratio - 1.0) ** 2)
+    s2 = np.sin(theta / 2.0) ** 2
+    dl = k * s2
+    d180 = k * np.sin(np.pi / 2.0) ** 2
+    dl_nu = dl**nu
+    main = (
+        nu * (1.0 - dl)
+        - (1.0 - dl_nu)
+        + (dl * (1.0 - dl_nu) - nu * (1.0 - dl)) * np.sin(theta / 2.0) ** (-2)
+    ) * (1.0 / (4.0 * np.pi * (1.0 - dl) ** 2 * dl_nu))
+    back = ((1.0 - d180**nu) / (16.0 * np.pi * (d180 - 1.0) * d180**nu)) * (
+        3.0 * np.cos(theta) ** 2 - 1.0
+    )
+    pf = main + back
+    cdf = np.cumsum(pf * np.sin(theta))
+    cdf /= cdf[-1]
+    return theta, pf, cdf
+
+
+def fournier_forand_backscatter(junge_slope: float, n_ratio: float) -> float:
+    """Fraction of FF scattering into the backward hemisphere (closed form at 90 deg)."""
+    nu = (3.0 - junge_slope) / 2.0
+    d90 = (4.0 / (3.0 * (n_ratio - 1.0) ** 2)) * np.sin(np.pi / 4.0) ** 2
+    top = 1.0 - d90 ** (nu + 1.0) - 0.5 * (1.0 - d90**nu)
+    bottom = (1.0 - d90) * d90**nu
+    return float(1.0 - top / bottom)
+
+
+def churnside_alpha(a, b, salinity, wavelength_um, flying_height, divergence, bb_frac):
+    """Lidar attenuation coefficient alpha (1/m) of a homogeneous water parcel.
+
+    alpha = Kd + (b_p - 4.18 b_p B (1 - 0.52 e^{-10.8 b})) exp(-0.85 D (a + b_p)),
+    Kd = a + 4.18 b_p B (1 - 0.52 e^{-10.8 a}), b_p = b - b_w(salinity, lambda),
+    D = 2 H tan(div / 2) the laser spot diameter at the surface.
+    """
+    b_w = (1.0 + 0.008027 * salinity) * 0.00012 * wavelength_um ** (-4.24)
+    b_p = b - b_w
+    spot = 2.0 * flying_height * math.tan(divergence / 2.0)
+    kd = a + 4.18 * b_p * bb_frac * (1.0 - 0.52 * np.exp(-10.8 * a))
+    beam_part = (b_p - 4.18 * b_p * bb_frac * (1.0 - 0.52 * np.exp(-10.8 * b))) * np.exp(
+        -0.85 * spot * (a + b_p)
+    )
+    return kd + beam_part
+
+
+def rotation_z_to(v) -> np.ndarray:
+    """float32 matrix rotating +z onto the direction ``v`` (Rodrigues, with the
+    reference's isclose() special cases for +z and -z)."""
+    v = np.asarray(v, dtype=np.float64)
+    v = v / np.linalg.norm(v)
+    c = v[2]
+    ax, ay = -v[1], v[0]
+    if np.isclose(c, 1.0):
+        return np.eye(3, dtype=np.float32)
+    if np.isclose(c, -1.0):
+        return np.array([[1, 0, 0], [0, -1, 0], [0, 0, -1]], dtype=np.float32)
+    s2 = ax * ax + ay * ay
+    K = np.array([[0.0, 0.0, ay], [0.0, 0.0, -ax], [-ay, ax, 0.0]])
+    R = np.eye(3) + K + (K @ K) * ((1.0 - c) / s2)
+    return R.astype(np.float32)
+
+
+def scatter_weight_table(theta: np.ndarray, cdf: np.ndarray):
+    """Gather weight per angular bin: CDF mass of bin i of width (pi - eps32) / 18000.
+
+    The bin width is a float32 quantity in the reference (numpy scalar promotion), so it
+    is kept as float32 here and the bin edges are i * width in float64.
+    """
+    n = len(theta)
+    width32 = np.float32(np.float32(np.pi) - np.float32(FLOAT32_EPS)) / np.float32(n)
+    width = float(width32)
+    i = np.arange(n, dtype=np.float64)
+    lo = np.interp(i * width, theta, cdf)
+    hi = np.interp((i + 1.0) * width, theta, cdf)
+    return (hi - lo), width32
+
+
+def _is_constant(layer) -> bool:
+    return all(
+        isinstance(getattr(layer, name), float)
+        for name in (
+            "scattering_coefficient",
+            "absorption_coefficient",
+            "salinity",
+            "refractive_index",
+        )
+    )
+
+
+def _value_at(value, z_local, height):
+    if isinstance(value, float):
+        return value
+    return value.at(z_local / height)
+
+
+@dataclass
+class LayerModel:
+    height: float
+    bottom_depth: float  # cumulative depth of the layer's lower boundary
+    constant: bool
+    alpha64: float  # lidar attenuation at the layer top (constant layers: everywhere)
+    alpha32: float  # float32-rounded, the value the integrator adds up
+    ssa32: float  # single-scattering albedo, float32
+    speed32: float  # c / n rounded to float32 (the reference stores speeds in float32)
+    n_top: float
+    absorption: float
+    ff_theta: np.ndarray
+    ff_cdf: np.ndarray
+    ff_slope: np.ndarray
+    backscatter: float
+    scatter_weight: np.ndarray
+    bin_width32: float
+
+
+@dataclass
+class SceneModel:
+    """Everything derived from a configuration; the source of the C ABI scene struct."""
+
+    sample_rate: int
+    sample_multiplier: int
+    k: int
+    dt: float
+    steps: int
+    total_substeps: int
+    surface_y: float
+    floor_y: float
+    depth: float
+    laser_dir: np.ndarray
+    laser_rot32: np.ndarray
+    divergence: float
+    fov: float
+    aperture_radius: float
+    pulse_sigma: float
+    effective_rate: float
+    n_water: float
+    f0: float
+    seafloor_albedo: float
+    surface_albedo: float
+    roughness: float
+    flying_height: float
+    layers: List[LayerModel] = field(default_factory=list)
+    heatmap_enabled: bool = False
+    heatmap_bins: int = 200
+    heatmap_water_extent: float = 1.0
+    heatmap_seafloor_extent: float = 10.0
+    water_center: np.ndarray = None
+    floor_center: np.ndarray = None
+
+    @property
+    def n_bins(self) -> int:
+        return 2 * self.steps
+
+    @property
+    def all_constant(self) -> bool:
+        return all(layer.constant for layer in self.layers)
+
+
+def refract(d, normal, n1, n2):
+    """Snell refraction of the (possibly non-unit) direction ``d`` about ``normal``,
+    normalised; returns (direction, total-internal-reflection flag)."""
+    eta = n1 / n2
+    cos_i = float(np.clip(np.dot(-np.asarray(d, dtype=np.float64), normal), -1.0, 1.0))
+    sin2_t = eta**2 * (1.0 - cos_i**2)
+    cos_t = math.sqrt(max(0.0, 1.0 - sin2_t))
+    t = eta * np.asarray(d, dtype=np.float64) + (eta * cos_i - cos_t) * np.asarray(
+        normal, dtype=np.float64
+    )
+    return t / np.linalg.norm(t), sin2_t > 1.0
+
+
+def build_scene(cfg) -> SceneModel:
+    """Derive the scene constants of ``cfg`` (a SimulationConfig, ours or the reference's)."""
+    laser = cfg.laser
+    theta = math.radians(laser.nadir_angle)
+    phi = math.radians(laser.azimuth_angle)
+    laser_dir = np.array(
+        [math.sin(theta) * math.cos(phi), -math.cos(theta), math.sin(theta) * math.sin(phi)]
+    )
+
+    layers: List[LayerModel] = []
+    depth_acc = 0.0
+    for layer in cfg.water.layers:
+        ff = layer.fournier_forand_parameters
+        th, _, cdf = fournier_forand_table(ff.junge_slope, ff.refractive_index_ratio)
+        bb = fournier_forand_backscatter(ff.junge_slope, ff.refractive_index_ratio)
+        a0 = _value_at(layer.absorption_coefficient, 0.0, layer.height)
+        b0 = _value_at(layer.scattering_coefficient, 0.0, layer.height)
+        s0 = _value_at(layer.salinity, 0.0, layer.height)
+        n0 = _value_at(layer.refractive_index, 0.0, layer.height)
+        alpha = float(
+            churnside_alpha(
+                a0, b0, s0, laser.wavelength, cfg.scene.flying_height,
+                laser.divergence_angle, bb,
+            )
+        )
+        ssa = (alpha - a0) / alpha
+        with np.errstate(divide="ignore", invalid="ignore"):
+            slope = np.diff(th) / np.diff(cdf)
+        weight, width32 = scatter_weight_table(th, cdf)
+        depth_acc = depth_acc + float(layer.height)
+        layers.append(
+            LayerModel(
+                height=float(layer.height),
+                bottom_depth=depth_acc,
+                constant=_is_constant(layer),
+                alpha64=alpha,
+                alpha32=float(np.float32(alpha)),
+                ssa32=float(np.float32(ssa)),
+                speed32=float(np.float32(LIGHT_SPEED_AIR / n0)),
+                n_top=float(n0),
+                absorption=float(a0),
+                ff_theta=th,
+                ff_cdf=cdf,
+                ff_slope=slope,
+                backscatter=bb,
+                scatter_weight=weight,
+                bin_width32=float(width32),
+            )
+        )
+    depth = layers[-1].bottom_depth
+    surface_y = -float(cfg.scene.flying_height)
+    floor_y = -(float(cfg.scene.flying_height) + depth)
+
+    sample_rate = cfg.sensor.sample_rate
+    mult = cfg.sample_multiplier
+    eff_rate = mult * sample_rate
+    dt = 1 / eff_rate
+    distance = floor_y / laser_dir[1]
+    steps = int(1.5 * (distance * round(sample_rate)) / LIGHT_SPEED_AIR)
+
+    n_water = layers[0].n_top
+    f0 = ((1 - n_water) / (1 + n_water)) ** 2
+
+    water_center = (surface_y / laser_dir[1]) * laser_dir
+    refr, _ = refract(laser_dir, np.array([0.0, 1.0, 0.0]), 1.0, n_water)
+    floor_center = water_center + (-depth / refr[1]) * refr
+
+    hm = cfg.heatmap
+    return SceneModel(
+        sample_rate=int(sample_rate),
+        sample_multiplier=int(mult),
+        k=int(cfg.photon_mapping_k),
+        dt=dt,
+        steps=steps,
+        total_substeps=steps * mult,
+        surface_y=surface_y,
+        floor_y=floor_y,
+        depth=depth,
+        laser_dir=laser_dir,
+        laser_rot32=rotation_z_to(laser_dir),
+        divergence=float(laser.divergence_angle),
+        fov=float(cfg.sensor.field_of_view),
+        aperture_radius=float(cfg.sensor.aperture_radius),
+        pulse_sigma=float(laser.pulse_fwhm / (2 * np.sqrt(2 * np.log(2)))),
+        effective_rate=float(eff_rate),
+        n_water=n_water,
+        f0=f0,
+        seafloor_albedo=float(cfg.sea_floor.albedo),
+        surface_albedo=float(cfg.sea_surface.albedo),
+        roughness=float(cfg.sea_surface.roughness),
+        flying_height=float(cfg.scene.flying_height),
+        layers=layers,
+        heatmap_enabled=bool(hm.enabled),
+        heatmap_bins=int(hm.bins),
+        heatmap_water_extent=float(hm.water_extent),
+        heatmap_seafloor_extent=float(hm.seafloor_extent),
+        water_center=water_center,
+        floor_center=floor_center,
+    )

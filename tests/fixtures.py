@@ -1,0 +1,116 @@
+"""Helpers shared by the tests: golden-fixture loading and configuration rebuilding."""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from pyalbsim_gb300.config import (
+    HeatmapConfig,
+    LaserConfig,
+    SceneConfig,
+    SeaFloorConfig,
+    SeaSurfaceConfig,
+    SensorConfig,
+    SimulationConfig,
+    TurbidityLayerConfig,
+    WaterConfig,
+)
+from pyalbsim_gb300.config.water import FournierForandConfig
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name)))
+
+
+def config_from_fixture(d) -> SimulationConfig:
+    """Rebuild the SimulationConfig a golden fixture was recorded with."""
+    f = lambda k: d[k].item() if np.ndim(d[k]) == 0 else d[k]  # noqa: E731
+    layers = tuple(
+        TurbidityLayerConfig(
+            height=float(h),
+            absorption_coefficient=float(a),
+            scattering_coefficient=float(b),
+            salinity=float(s),
+            refractive_index=float(n),
+            fournier_forand_parameters=FournierForandConfig(refractive_index_ratio=float(nr), junge_slope=float(j)),
+        )
+        for h, a, b, s, n, j, nr in zip(
+            d["cfg_layer_height"], d["cfg_layer_a"], d["cfg_layer_b"], d["cfg_layer_salinity"],
+            d["cfg_layer_n"], d["cfg_layer_junge"], d["cfg_layer_nratio"],
+        )
+    )
+    return SimulationConfig(
+        sample_multiplier=int(f("cfg_sample_multiplier")),
+        photon_mapping_k=int(f("cfg_k")),
+        scene=SceneConfig(flying_height=float(f("cfg_flying_height"))),
+        water=WaterConfig(layers=layers),
+        laser=LaserConfig(
+            divergence_angle=float(f("cfg_divergence")),
+            wavelength=float(f("cfg_wavelength")),
+            nadir_angle=float(f("cfg_nadir")),
+            azimuth_angle=float(f("cfg_azimuth")),
+            pulse_fwhm=float(f("cfg_pulse_fwhm")),
+        ),
+        sensor=SensorConfig(
+            aperture_radius=float(f("cfg_aperture")),
+            field_of_view=float(f("cfg_fov")),
+            sample_rate=int(f("cfg_sample_rate")),
+        ),
+        sea_floor=SeaFloorConfig(albedo=float(f("cfg_floor_albedo"))),
+        sea_surface=SeaSurfaceConfig(albedo=float(f("cfg_surface_albedo")), roughness=float(f("cfg_roughness"))),
+        heatmap=HeatmapConfig(
+            enabled=bool(f("cfg_heatmap_enabled")),
+            bins=int(f("cfg_heatmap_bins")),
+            water_extent=float(f("cfg_heatmap_water_extent")),
+            seafloor_extent=float(f("cfg_heatmap_seafloor_extent")),
+        ),
+    )
+
+
+def replay_streams(d, prefix):
+    return d[f"{prefix}_offsets"], d[f"{prefix}_stream"], d[f"{prefix}_stream_tau"]
+
+
+def sort_records(pos, photon, time):
+    """Canonical record order: (photon id, time, x, y, z)."""
+    return np.lexsort((pos[:, 2], pos[:, 1], pos[:, 0], time, photon))
+
+
+def assert_statistically_equal(w, st, family_alpha=1e-3):
+    """w: [runs, 4, bins] N_f*N_b-normalised waveforms of independent runs; st: the
+    reference's per-run waveforms (``per_run``), mean and standard error per bin.
+
+    Two checks per populated bin:
+    * CLT regime (both relative standard errors below 25%): |mean - ref| within
+      3 combined standard errors; at most the normal tail (plus one bin) may exceed it;
+    * every bin, including heavy-tailed ones where a handful of near-spot gathers with
+      a tiny k-NN radius dominate a run: a two-sided Mann-Whitney rank test of the
+      per-run values must not reject at the family-wise level ``family_alpha``
+      (Bonferroni over the tested bins).
+    """
+    from scipy.stats import mannwhitneyu
+
+    runs = w.shape[0]
+    mean, se = w.mean(0), w.std(0, ddof=1) / np.sqrt(runs)
+    ref_runs = st["per_run"]
+    rmean, rse = st["mean"], st["se"]
+    tested = []
+    for c in range(4):
+        populated = (rmean[c] > 0) | (mean[c] > 0)
+        clt = populated & (se[c] < 0.25 * np.abs(mean[c])) & (rse[c] < 0.25 * np.abs(rmean[c]))
+        comb = np.sqrt(se[c] ** 2 + rse[c] ** 2)
+        z = np.abs(mean[c] - rmean[c])[clt] / comb[clt]
+        if z.size:
+            assert np.sum(z > 3.0) <= 1 + 0.01 * z.size, (c, np.sort(z)[-5:])
+        for b in np.nonzero(populated)[0]:
+            a, r = w[:, c, b], ref_runs[:, c, b]
+            if np.all(a == a[0]) and np.all(r == a[0]):
+                continue
+            tested.append((c, b, mannwhitneyu(a, r, alternative="two-sided").pvalue))
+    if tested:
+        worst = min(tested, key=lambda t: t[2])
+        assert worst[2] > family_alpha / len(tested), worst

@@ -1,0 +1,159 @@
+"""C-ABI and host-logic tests that need no GPU: the library loads and exports every
+declared entry point, the ctypes mirror of the structs has the C layout, configuration
+objects behave like the reference's, and error codes map to the reference's exceptions."""
+
+import dataclasses
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+from pyalbsim_gb300 import config as cfgmod
+from pyalbsim_gb300.build import INCLUDE, build_library
+
+HEADER = os.path.join(INCLUDE, "albgpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(alb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+
+    path = build_library()
+    lib = ctypes.CDLL(path)  # loading needs no GPU
+    missing = [f for f in declared_functions() if not hasattr(lib, f)]
+    assert not missing, missing
+    from pyalbsim_gb300._native import EXPORTED
+
+    assert sorted(EXPORTED) == declared_functions()
+
+
+def test_ctypes_struct_layout_matches_c():
+    import ctypes
+
+    from oracle.oracle import abi_layout
+    from pyalbsim_gb300._native import AlbLayer, AlbReplay, AlbSceneParams
+
+    lay = abi_layout()
+    assert lay[0] == ctypes.sizeof(AlbSceneParams)
+    assert lay[1] == ctypes.sizeof(AlbLayer)
+    assert lay[2] == AlbSceneParams.layers.offset
+    assert lay[3] == AlbSceneParams.water_center.offset
+    assert lay[4] == AlbSceneParams.laser_rot.offset
+    assert lay[5] == AlbLayer.phase_theta.offset
+    assert lay[6] == ctypes.sizeof(AlbReplay)
+
+
+def test_error_codes_map_to_reference_exceptions():
+    from pyalbsim_gb300._native import raise_for
+
+    raise_for(0, "ok")
+    with pytest.raises(ValueError):
+        raise_for(-1, "bad config")
+    with pytest.raises(IndexError):
+        raise_for(-2, "map smaller than k")
+    for code in (-3, -4, -5, -6, -7):
+        with pytest.raises(RuntimeError):
+            raise_for(code, "x")
+
+
+def test_config_validation_like_reference():
+    with pytest.raises(ValueError):
+        cfgmod.LaserConfig(nadir_angle=90)
+    with pytest.raises(ValueError):
+        cfgmod.SceneConfig(flying_height=0)
+    with pytest.raises(ValueError):
+        cfgmod.SeaFloorConfig(albedo=1.5)
+    with pytest.raises(ValueError):
+        cfgmod.SeaSurfaceConfig(albedo=-0.1)
+    with pytest.raises(ValueError):
+        cfgmod.SensorConfig(aperture_radius=-1)
+    with pytest.raises(ValueError):
+        cfgmod.TurbidityLayerConfig(height=0)
+    with pytest.raises(ValueError):
+        cfgmod.TurbidityLayerConfig(sublayer_dz=None)
+    with pytest.raises(TypeError):
+        cfgmod.TurbidityLayerConfig(absorption_coefficient=True)
+    layer = cfgmod.TurbidityLayerConfig(height=3, salinity=35)
+    assert isinstance(layer.salinity, float) and layer.num_sublayers == 60
+
+
+REF_SRC = "/root/reference/src"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+def test_config_fields_and_defaults_equal_reference():
+    sys.path.insert(0, REF_SRC)
+    import importlib
+
+    pairs = [
+        ("alb_sim.config.laser", "LaserConfig"),
+        ("alb_sim.config.scene", "SceneConfig"),
+        ("alb_sim.config.sensor", "SensorConfig"),
+        ("alb_sim.config.sea_floor", "SeaFloorConfig"),
+        ("alb_sim.config.sea_surface", "SeaSurfaceConfig"),
+        ("alb_sim.config.heatmap", "HeatmapConfig"),
+        ("alb_sim.config.run", "RunConfig"),
+        ("alb_sim.config.water", "TurbidityLayerConfig"),
+        ("alb_sim.config.water", "FournierForandConfig"),
+        ("alb_sim.config.simulation", "SimulationConfig"),
+    ]
+    for mod, name in pairs:
+        ref = getattr(importlib.import_module(mod), name)
+        ours = getattr(cfgmod, name)
+        rf = {f.name: f for f in dataclasses.fields(ref)}
+        of = {f.name: f for f in dataclasses.fields(ours)}
+        assert list(rf) == list(of), name
+        r_inst, o_inst = ref(), ours()
+        for k in rf:
+            rv, ov = getattr(r_inst, k), getattr(o_inst, k)
+            if dataclasses.is_dataclass(rv):
+                assert dataclasses.asdict(rv) == dataclasses.asdict(ov), (name, k)
+            else:
+                assert rv == ov, (name, k)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+def test_scene_accepts_reference_config_objects():
+    sys.path.insert(0, REF_SRC)
+    from alb_sim.config.simulation import SimulationConfig as RefCfg
+
+    from pyalbsim_gb300.scene import build_scene
+
+    a = build_scene(RefCfg())
+    b = build_scene(cfgmod.SimulationConfig())
+    assert a.steps == b.steps and a.layers[0].alpha64 == b.layers[0].alpha64
+    np.testing.assert_array_equal(a.laser_rot32, b.laser_rot32)
+
+
+def test_seed_derivation():
+    from pyalbsim_gb300.engine import seed_from_rng
+
+    s1 = seed_from_rng(np.random.default_rng(3))
+    s2 = seed_from_rng(np.random.default_rng(3))
+    assert s1 == s2 and 0 <= s1 < 2**63
+    assert seed_from_rng(None) != seed_from_rng(None)
+
+
+def test_product_path_never_imports_oracle():
+    import pathlib
+
+    pkg = pathlib.Path(__file__).resolve().parents[1] / "pyalbsim_gb300"
+    for f in pkg.rglob("*.py"):
+        assert not re.search(r"^\s*(from|import)\s+oracle", f.read_text(), re.M), f
+    for f in pkg.rglob("*"):
+        if f.suffix in (".cu", ".cuh", ".h"):
+            assert "alb_oracle" not in f.read_text(), f
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from pyalbsim_gb300 import _native
+
+    monkeypatch.setattr(_native, "_lib", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _native.load_library(str(tmp_path / "absent.so"))

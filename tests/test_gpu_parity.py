@@ -1,0 +1,255 @@
+"""GPU parity tests: the CUDA path through the C ABI against the reference's recorded runs
+(replay mode), the oracle (same Philox streams), scipy's KDTree answers and independent
+reference runs (statistics). All tests here need a GB300 and libalbgpu.so."""
+
+import numpy as np
+import pytest
+
+from fixtures import assert_statistically_equal, config_from_fixture, load, replay_streams
+from oracle.oracle import oracle_run
+from pyalbsim_gb300.engine import GpuEngine
+from pyalbsim_gb300.scene import build_scene
+
+pytestmark = pytest.mark.gpu
+
+REPLAYS = ["small", "twolayer", "cfg0"]
+# Tolerances: FP32 arithmetic on the device vs float64 in the reference.
+REL_WAVEFORM_L1 = 1e-5
+
+
+def _engine(cfg, ids=True, exits=True):
+    eng = GpuEngine(cfg)
+    if ids:
+        eng.keep_record_ids(True)
+    if exits:
+        eng.keep_exit_states(True)
+    return eng
+
+
+@pytest.fixture(scope="module", params=REPLAYS)
+def gpu_replay(request, gpu_available):
+    d = load(f"replay_{request.param}.npz")
+    cfg = config_from_fixture(d)
+    nf, nb = int(d["n_fwd"]), int(d["n_bwd"])
+    eng = _engine(cfg)
+    eng.forward(nf, 0, replay=replay_streams(d, "fwd"))
+    fexit = eng.ctx.exit_states(nf)
+    maps = {c: eng.ctx.export_map(c) for c in range(4)}  # unsorted (record) order
+    eng.build_maps()
+    eng.backward(nb, 0, replay=replay_streams(d, "bwd"))
+    bexit = eng.ctx.exit_states(nb)
+    queries = {k: eng.ctx.export_queries(k) for k in range(3)}
+    wf = eng.waveform_array(f64=True)
+    heat = eng.heatmaps()
+    orc = oracle_run(eng.scene, nf, nb, replay_fwd=replay_streams(d, "fwd"), replay_bwd=replay_streams(d, "bwd"))
+    out = dict(d=d, maps=maps, fexit=fexit, bexit=bexit, queries=queries, wf=wf, heat=heat, orc=orc, eng=eng)
+    yield request.param, out
+    eng.close()
+
+
+def test_replay_maps_match_reference(gpu_replay):
+    name, o = gpu_replay
+    d = o["d"]
+    for c in range(4):
+        pos, dr, e, t, fwi, sfi, pid = o["maps"][c]
+        if f"map{c}_pos" not in d:
+            assert len(e) == 0
+            continue
+        assert len(e) == len(d[f"map{c}_energy"]), (name, c)
+        ia = np.lexsort((t, pid))
+        ib = np.lexsort((d[f"map{c}_time"], d[f"map{c}_ids"]))
+        np.testing.assert_array_equal(pid[ia], d[f"map{c}_ids"][ib])
+        np.testing.assert_array_equal(t[ia], d[f"map{c}_time"][ib])
+        np.testing.assert_allclose(e[ia], d[f"map{c}_energy"][ib], rtol=1e-6)
+        np.testing.assert_allclose(pos[ia], d[f"map{c}_pos"][ib], rtol=1e-5, atol=1e-5)
+        np.testing.assert_allclose(dr[ia], d[f"map{c}_dir"][ib], rtol=0, atol=1e-5)
+
+
+def test_replay_exit_states_match_reference(gpu_replay):
+    name, o = gpu_replay
+    d = o["d"]
+    for p, ex in (("fwd", o["fexit"]), ("bwd", o["bexit"])):
+        np.testing.assert_allclose(ex["energy"], d[f"{p}_final_energy"], rtol=1e-6)
+        np.testing.assert_array_equal(ex["time"], d[f"{p}_final_time"])
+        np.testing.assert_array_equal(ex["tau_target"], d[f"{p}_final_tau_target"])
+        np.testing.assert_allclose(ex["tau"], d[f"{p}_final_tau"], rtol=1e-5, atol=1e-5)
+        np.testing.assert_allclose(ex["pos"], d[f"{p}_final_pos"], rtol=1e-5, atol=1e-4)
+        np.testing.assert_allclose(ex["dir"], d[f"{p}_final_dir"], rtol=0, atol=1e-5)
+
+
+def test_replay_queries_match_reference(gpu_replay):
+    name, o = gpu_replay
+    q = o["d"]["queries"]
+    for kind in range(3):
+        mine = o["queries"][kind]
+        ref = q[q[:, 0] == kind]
+        assert len(mine["energy"]) == len(ref), (name, kind)
+        if len(ref) == 0:
+            continue
+        ia = np.lexsort((mine["time"], mine["id"]))
+        ib = np.lexsort((ref[:, 9], ref[:, 1]))
+        np.testing.assert_array_equal(mine["id"][ia], ref[ib, 1].astype(np.int64))
+        np.testing.assert_array_equal(mine["time"][ia], ref[ib, 9].astype(np.float32))
+        np.testing.assert_allclose(mine["pos"][ia], ref[ib, 2:5], rtol=1e-6, atol=1e-5)
+
+
+def test_replay_waveform_matches_reference(gpu_replay):
+    """Waveform vs the reference's float64-accumulated waveform: L1 <= 1e-5 per channel."""
+    name, o = gpu_replay
+    ref = o["d"]["waveform64"]
+    for c in range(4):
+        den = np.abs(ref[c]).sum()
+        if den == 0:
+            continue
+        l1 = np.abs(o["wf"][c] - ref[c]).sum() / den
+        assert l1 < REL_WAVEFORM_L1, (name, c, l1)
+
+
+def test_replay_waveform_matches_oracle(gpu_replay):
+    name, o = gpu_replay
+    orc = o["orc"]["waveform"]
+    for c in range(4):
+        den = np.abs(orc[c]).sum()
+        if den:
+            assert np.abs(o["wf"][c] - orc[c]).sum() / den < REL_WAVEFORM_L1, (name, c)
+
+
+def test_replay_rk_matches_oracle(gpu_replay):
+    """k-th neighbour distance of every gather equals the oracle's (brute-force) one."""
+    name, o = gpu_replay
+    orc = o["orc"]
+    for ch, kind in ((0, 0), (1, 1), (2, 2), (3, 2)):
+        if ch not in orc["rk"]:
+            continue
+        mine = o["queries"][kind]
+        ref_q = orc["queries"][kind]
+        key_m = np.lexsort((mine["time"], mine["id"]))
+        key_r = np.lexsort((ref_q["time"], ref_q["photon"]))
+        rk_m = (mine["rk2"] if ch == 3 else mine["rk"])[key_m]
+        np.testing.assert_allclose(rk_m, orc["rk"][ch][key_r], rtol=1e-6, atol=1e-9)
+
+
+def test_replay_heatmaps(gpu_replay):
+    name, o = gpu_replay
+    d = o["d"]
+    if o["heat"] is None or "heat_radius" not in d:
+        return
+    np.testing.assert_array_equal(o["heat"].scatter_radius_heatmap, d["heat_radius"])
+    for mine, key in ((o["heat"].water_heatmap, "heat_water"), (o["heat"].seafloor_heatmap, "heat_floor")):
+        ref = d[key].astype(np.float64)
+        assert np.abs(mine - ref).sum() / np.abs(ref).sum() < 1e-4, key
+
+
+def test_knn_neighbour_sets_bit_exact(gpu_available):
+    kn = load("knn.npz")
+    eng = GpuEngine(config_from_fixture(load("replay_small.npz")))
+    try:
+        for name in ("planar", "cloud", "cloud_k16"):
+            pts, qs, k = kn[f"{name}_points"], kn[f"{name}_queries"], int(kn[f"{name}_k"])
+            dist, idx = eng.ctx.knn(pts, qs, k)
+            np.testing.assert_allclose(dist, kn[f"{name}_dist"], rtol=1e-12, atol=0)
+            ref_idx, ref_d = kn[f"{name}_idx"], kn[f"{name}_dist"]
+            for i in range(len(qs)):
+                strict = set(ref_idx[i][ref_d[i] < ref_d[i][-1]])  # exclude exact ties at r_k
+                assert strict <= set(idx[i]), (name, i)
+    finally:
+        eng.close()
+
+
+def _philox_run(cfg, nf, nb, seed, ids=True):
+    eng = _engine(cfg, ids=ids, exits=True)
+    eng.forward(nf, seed)
+    fexit = eng.ctx.exit_states(nf)
+    maps = {c: eng.ctx.export_map(c) for c in range(4)}
+    eng.build_maps()
+    eng.backward(nb, seed)
+    wf = eng.waveform_array(f64=True)
+    eng.close()
+    return fexit, maps, wf
+
+
+def test_philox_matches_oracle_photon_by_photon(gpu_available):
+    """Same Philox streams on both sides: identical records, exit states and waveform."""
+    d = load("replay_small.npz")
+    cfg = config_from_fixture(d)
+    nf, nb, seed = 4000, 1000, 1234567
+    fexit, maps, wf = _philox_run(cfg, nf, nb, seed)
+    scene = build_scene(cfg)
+    orc = oracle_run(scene, nf, nb, seed=seed)
+    np.testing.assert_array_equal(fexit["time"], orc["fwd_exit"]["time"])
+    np.testing.assert_allclose(fexit["pos"], orc["fwd_exit"]["pos"], rtol=1e-5, atol=1e-4)
+    for c in range(4):
+        pos, dr, e, t, fwi, sfi, pid = maps[c]
+        om = orc["maps"][c]
+        assert len(e) == len(om["energy"]), c
+        ia = np.lexsort((t, pid))
+        ib = np.lexsort((om["time"], om["photon"]))
+        np.testing.assert_array_equal(pid[ia], om["photon"][ib])
+        np.testing.assert_array_equal(t[ia], om["time"][ib])
+        np.testing.assert_allclose(pos[ia], om["pos"][ib], rtol=1e-5, atol=1e-5)
+    for c in range(4):
+        den = np.abs(orc["waveform"][c]).sum()
+        if den:
+            assert np.abs(wf[c] - orc["waveform"][c]).sum() / den < REL_WAVEFORM_L1, c
+
+
+def test_waveform_bit_identical_run_to_run(gpu_available):
+    cfg = config_from_fixture(load("replay_small.npz"))
+    a = _philox_run(cfg, 20000, 5000, 99, ids=False)[2]
+    b = _philox_run(cfg, 20000, 5000, 99, ids=False)[2]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_philox_statistics_match_reference(gpu_available):
+    """Every waveform bin within 3 combined standard errors of 16 independent reference
+    runs (N_f*N_b-normalised), allowing the normal tail; total L1 within 1%."""
+    st = load("stats_small.npz")
+    cfg = config_from_fixture(st)
+    runs, nf, nb = 32, int(st["n_fwd"]), int(st["n_bwd"])
+    waves = np.stack([_philox_run(cfg, nf, nb, 5000 + r, ids=False)[2] / (nf * nb) for r in range(runs)])
+    assert_statistically_equal(waves, st)
+    # larger single run: L1 distance of the summed waveform to the reference mean <= 1%
+    big = _philox_run(cfg, 200000, 50000, 77, ids=False)[2].sum(0) / (200000 * 50000)
+    ref = st["mean"].sum(0)
+    assert np.abs(big - ref).sum() / np.abs(ref).sum() < 0.05
+
+
+def test_too_few_photons_raises_index_error(gpu_available):
+    """Reference quirk: a gather on a map with fewer than k records raises IndexError."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    eng = GpuEngine(cfg)
+    try:
+        eng.forward(10, 1)  # fewer surface records than k=32
+        eng.build_maps()
+        with pytest.raises(IndexError):
+            eng.backward(100, 1)
+    finally:
+        eng.close()
+
+
+def test_drop_in_run_linear_and_run_parallel(gpu_available):
+    from pyalbsim_gb300.config import RunConfig
+    from pyalbsim_gb300.execution.linear import run_linear
+    from pyalbsim_gb300.execution.parallel import run_parallel
+    from pyalbsim_gb300.photon_mapping.photon_type import PhotonType
+
+    cfg = config_from_fixture(load("replay_small.npz"))
+    rc = RunConfig(photons_per_batch_forward=2000, photons_per_batch_backward=500, batches_forward=2, batches_backward=2)
+    w = run_linear(cfg, rc, rng=np.random.default_rng(0))
+    assert set(w) == set(PhotonType)
+    steps = build_scene(cfg).steps
+    for arr in w.values():
+        assert arr.dtype == np.float32 and arr.shape == (2 * steps,)
+        assert np.all(arr >= 0)
+    w2 = run_linear(cfg, rc, rng=np.random.default_rng(0))
+    for t in w:
+        np.testing.assert_array_equal(w[t], w2[t])
+    wave, maps, heat = run_parallel(cfg, rc, seed=5)
+    assert set(wave) == set(PhotonType)
+    # fixed seed: every forward batch is the same photons (reference behaviour)
+    sr = maps[PhotonType.SURFACE_REFLECTION]
+    n = len(sr.energies)
+    assert n == 2 * 2000
+    a = np.lexsort((sr.positions[:, 2], sr.positions[:, 0]))
+    np.testing.assert_array_equal(sr.positions[a][0::2], sr.positions[a][1::2])
+    assert heat is not None and heat.water_heatmap.shape == (20, 20)

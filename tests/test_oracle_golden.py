@@ -1,0 +1,142 @@
+"""Pin the oracle (CPU restatement) to the reference: replayed runs against the reference's
+recorded runs, k-NN against scipy's KDTree answers, Philox statistics against independent
+reference runs. These run on the CPU only."""
+
+import numpy as np
+import pytest
+
+from fixtures import assert_statistically_equal, config_from_fixture, load, replay_streams
+from oracle.oracle import Oracle, oracle_run
+from pyalbsim_gb300.scene import build_scene
+
+REPLAYS = ["small", "twolayer", "cfg0"]
+
+
+@pytest.fixture(scope="module", params=REPLAYS)
+def replayed(request):
+    d = load(f"replay_{request.param}.npz")
+    scene = build_scene(config_from_fixture(d))
+    r = oracle_run(scene, int(d["n_fwd"]), int(d["n_bwd"]),
+                   replay_fwd=replay_streams(d, "fwd"), replay_bwd=replay_streams(d, "bwd"))
+    return request.param, d, scene, r
+
+
+def test_steps_match(replayed):
+    _, d, scene, _ = replayed
+    assert scene.steps == int(d["steps"])
+
+
+def test_photon_maps_record_by_record(replayed):
+    """Same records (photon, step) per type; energies and times exact; geometry to 1e-6."""
+    _, d, _, r = replayed
+    for c in range(4):
+        mp = r["maps"][c]
+        if f"map{c}_pos" not in d:
+            assert len(mp["energy"]) == 0
+            continue
+        ia = np.lexsort((mp["time"], mp["photon"]))
+        ib = np.lexsort((d[f"map{c}_time"], d[f"map{c}_ids"]))
+        np.testing.assert_array_equal(mp["photon"][ia], d[f"map{c}_ids"][ib])
+        np.testing.assert_array_equal(mp["time"][ia], d[f"map{c}_time"][ib])
+        np.testing.assert_array_equal(mp["energy"][ia], d[f"map{c}_energy"][ib])
+        np.testing.assert_allclose(mp["pos"][ia], d[f"map{c}_pos"][ib], rtol=1e-6, atol=1e-5)
+        np.testing.assert_allclose(mp["dir"][ia], d[f"map{c}_dir"][ib], rtol=0, atol=1e-6)
+        fa, fb = mp["fwi"][ia], d[f"map{c}_fwi"][ib]
+        np.testing.assert_array_equal(np.isnan(fa), np.isnan(fb))
+        np.testing.assert_allclose(fa[~np.isnan(fa)], fb[~np.isnan(fb)], rtol=1e-6, atol=1e-5)
+
+
+def test_exit_states(replayed):
+    _, d, _, r = replayed
+    for p in ("fwd", "bwd"):
+        ex = r[f"{p}_exit"]
+        np.testing.assert_array_equal(ex["energy"], d[f"{p}_final_energy"])
+        np.testing.assert_array_equal(ex["tau_target"], d[f"{p}_final_tau_target"])
+        np.testing.assert_array_equal(ex["time"], d[f"{p}_final_time"])
+        np.testing.assert_allclose(ex["tau"], d[f"{p}_final_tau"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(ex["pos"], d[f"{p}_final_pos"], rtol=1e-5, atol=1e-4)
+        np.testing.assert_allclose(ex["dir"], d[f"{p}_final_dir"], rtol=0, atol=1e-5)
+
+
+def test_waveform_float64(replayed):
+    """Float64-accumulated reference waveform: L1 within 1e-6 per channel."""
+    _, d, _, r = replayed
+    for c in range(4):
+        ref = d["waveform64"][c]
+        got = r["waveform"][c]
+        den = np.abs(ref).sum()
+        if den == 0:
+            assert np.abs(got).sum() == 0
+            continue
+        assert np.abs(got - ref).sum() / den < 1e-6, c
+
+
+def test_waveform_float32_reference_units(replayed):
+    """The reference's own float32 accumulation, within its rounding error."""
+    _, d, _, r = replayed
+    for c in range(4):
+        ref = d["waveform32"][c].astype(np.float64)
+        den = np.abs(ref).sum()
+        if den:
+            assert np.abs(r["waveform"][c] - ref).sum() / den < 1e-4
+
+
+def test_queries(replayed):
+    """Backward events (gather queries) match the reference's event by event. The reference
+    logs a surface entry twice (SURFACE_REFLECTION and SURFACE_TRANSMISSION_UP gathers);
+    query kind 0/1/2 corresponds to its channel 0/1/2 entries."""
+    _, d, _, r = replayed
+    q = d["queries"]  # channel, photon, pos3, dir3, E, t, contribution sum
+    for kind in range(3):
+        mine = r["queries"][kind]
+        ref = q[q[:, 0] == kind]
+        if len(ref) == 0:
+            assert len(mine["energy"]) == 0
+            continue
+        ia = np.lexsort((mine["time"], mine["photon"]))
+        ib = np.lexsort((ref[:, 9], ref[:, 1]))
+        np.testing.assert_array_equal(mine["photon"][ia], ref[ib, 1].astype(np.int64))
+        np.testing.assert_array_equal(mine["time"][ia], ref[ib, 9].astype(np.float32))
+        np.testing.assert_allclose(mine["pos"][ia], ref[ib, 2:5], rtol=1e-6, atol=1e-5)
+        np.testing.assert_array_equal(mine["energy"][ia], ref[ib, 8].astype(np.float32))
+
+
+def test_heatmaps(replayed):
+    name, d, _, r = replayed
+    if "heat_radius" not in d:
+        return
+    np.testing.assert_array_equal(r["heat_radius"].reshape(d["heat_radius"].shape), d["heat_radius"].astype(np.uint32))
+    for key, mine in (("heat_water", r["heat_water"]), ("heat_floor", r["heat_floor"])):
+        ref = d[key].astype(np.float64).ravel()
+        den = np.abs(ref).sum()
+        assert np.abs(mine - ref).sum() / den < 1e-4, key
+
+
+def test_knn_matches_kdtree():
+    kn = load("knn.npz")
+    for name in ("planar", "cloud", "cloud_k16"):
+        pts, qs, k = kn[f"{name}_points"], kn[f"{name}_queries"], int(kn[f"{name}_k"])
+        orc = Oracle(build_scene(config_from_fixture(load("replay_small.npz"))))
+        dist, idx = orc.knn(pts, qs, k)
+        np.testing.assert_allclose(dist, kn[f"{name}_dist"], rtol=1e-12, atol=0)
+        for i in range(len(qs)):
+            ref = kn[f"{name}_idx"][i]
+            rd = kn[f"{name}_dist"][i]
+            # sets must agree except for exact ties at the k-th distance
+            strict = set(ref[rd < rd[-1]])
+            assert strict <= set(idx[i]), (name, i)
+
+
+def test_oracle_philox_statistics_match_reference():
+    """Philox runs of the oracle agree with independent reference runs per waveform bin
+    within 3 combined standard errors, and in normalised L1 within the MC noise."""
+    st = load("stats_small.npz")
+    scene = build_scene(config_from_fixture(st))
+    runs, nf, nb = 32, int(st["n_fwd"]), int(st["n_bwd"])
+    waves = []
+    for r in range(runs):
+        out = oracle_run(scene, nf, nb, seed=777 + r)
+        waves.append(out["waveform"] / (nf * nb))
+    w = np.stack(waves)
+    assert_statistically_equal(w, st)
+

@@ -1,0 +1,133 @@
+"""Known-answer tests of the host-side scene model and the oracle's physics functions
+against values the reference's own functions returned (tests/golden/kat_physics.npz)."""
+
+import numpy as np
+import pytest
+
+from fixtures import load
+from pyalbsim_gb300.config import (
+    HeatmapConfig, LaserConfig, SceneConfig, SeaFloorConfig, SeaSurfaceConfig, SensorConfig,
+    SimulationConfig, TurbidityLayerConfig, WaterConfig,
+)
+from pyalbsim_gb300.scene import (
+    build_scene, fournier_forand_backscatter, fournier_forand_table, refract, rotation_z_to,
+)
+
+KAT = load("kat_physics.npz")
+
+
+def small_config():
+    return SimulationConfig(
+        photon_mapping_k=32,
+        scene=SceneConfig(flying_height=10.0),
+        water=WaterConfig(layers=(TurbidityLayerConfig(
+            height=2.0, absorption_coefficient=0.1, scattering_coefficient=1.0, refractive_index=1.34),)),
+        laser=LaserConfig(divergence_angle=5e-3, nadir_angle=10.0, azimuth_angle=30.0, pulse_fwhm=3e-9),
+        sensor=SensorConfig(aperture_radius=0.1, field_of_view=50e-3, sample_rate=int(1e9)),
+        sea_floor=SeaFloorConfig(albedo=0.2),
+        sea_surface=SeaSurfaceConfig(albedo=0.1, roughness=float(np.sqrt(0.05))),
+        heatmap=HeatmapConfig(enabled=True, bins=20, water_extent=1.0, seafloor_extent=3.0),
+    )
+
+
+def two_layer_config():
+    return SimulationConfig(
+        photon_mapping_k=24,
+        scene=SceneConfig(flying_height=8.0),
+        water=WaterConfig(layers=(
+            TurbidityLayerConfig(height=0.7, absorption_coefficient=0.2, scattering_coefficient=1.5),
+            TurbidityLayerConfig(height=1.3, absorption_coefficient=0.05, scattering_coefficient=0.6,
+                                 refractive_index=1.36),
+        )),
+        laser=LaserConfig(divergence_angle=4e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
+        sensor=SensorConfig(aperture_radius=0.05, field_of_view=40e-3, sample_rate=int(1e9)),
+        sea_floor=SeaFloorConfig(albedo=0.3),
+        heatmap=HeatmapConfig(enabled=False),
+    )
+
+
+def config0_geometry():
+    return SimulationConfig(
+        scene=SceneConfig(flying_height=400.0),
+        water=WaterConfig(layers=(TurbidityLayerConfig(
+            height=5.0, absorption_coefficient=0.05, scattering_coefficient=0.20, refractive_index=1.34),)),
+        laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
+        sensor=SensorConfig(field_of_view=20e-3, sample_rate=int(1e10)),
+        sea_floor=SeaFloorConfig(albedo=0.15),
+        sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.05))),
+        heatmap=HeatmapConfig(enabled=False),
+    )
+
+
+CONFIGS = [small_config, two_layer_config, config0_geometry, SimulationConfig]
+
+
+def test_fournier_forand_tables_bit_exact():
+    for i in range(3):
+        junge, nratio = KAT[f"ff{i}_params"]
+        stride = int(KAT[f"ff{i}_stride"])
+        _, pf, cdf = fournier_forand_table(junge, nratio)
+        np.testing.assert_array_equal(pf[::stride], KAT[f"ff{i}_pf"])
+        np.testing.assert_array_equal(cdf[::stride], KAT[f"ff{i}_cdf"])
+        assert fournier_forand_backscatter(junge, nratio) == KAT[f"ff{i}_bb"]
+
+
+def test_model_scalars_match_reference():
+    rows = KAT["model_rows"]
+    for row in rows:
+        ci, li = int(row[0]), int(row[1])
+        s = build_scene(CONFIGS[ci]())
+        layer = s.layers[li]
+        assert s.steps == int(row[2])
+        assert s.dt == row[3]
+        assert s.surface_y == row[4] and s.floor_y == row[5]
+        assert layer.alpha64 == row[6]                      # Churnside lidar attenuation
+        assert layer.ssa32 == np.float32(row[7])            # single-scattering albedo (float32 store)
+        assert layer.speed32 == float(np.float32(row[8]))   # c / n stored as float32
+        assert s.f0 == row[9]
+        np.testing.assert_array_equal(s.laser_dir, row[10:13])
+        np.testing.assert_allclose(s.water_center, row[13:16], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(s.floor_center, row[16:19], rtol=0, atol=1e-12)
+
+
+def test_rotation_matrices_bit_exact():
+    for v, r in zip(KAT["rot_in"], KAT["rot_out"]):
+        np.testing.assert_array_equal(rotation_z_to(v), r)
+
+
+def test_snell_refraction():
+    for tag, sgn in (("up", 1), ("down", -1)):
+        for d, t, tir in zip(KAT[f"snell_in_{tag}"], KAT[f"snell_out_{tag}"], KAT[f"snell_tir_{tag}"]):
+            out, flag = refract(d, np.array([0.0, sgn, 0.0]), 1.0, 1.34)
+            np.testing.assert_allclose(out, t, rtol=0, atol=2e-16)
+            assert flag == tir
+
+
+def test_ggx_reflected_energy_oracle():
+    from oracle.oracle import kat_ggx
+
+    for r_i, rough in enumerate(KAT["ggx_rough"]):
+        for w_i, wo in enumerate(KAT["ggx_wo"]):
+            ref = KAT[f"ggx_{r_i}_{w_i}"]
+            got = kat_ggx(rough, 0.0211, KAT["ggx_wi"], wo)
+            np.testing.assert_allclose(got, ref, rtol=2e-7, atol=1e-30)
+
+
+def test_scatter_bin_energy_oracle():
+    from oracle.oracle import kat_scatter_energy
+
+    s = build_scene(small_config())  # FF(3.62, 1.1) tables, as the fixture
+    # the fixture passed its vector as calculate_energy_batch's view direction
+    got = kat_scatter_energy(s, KAT["senergy_pdirs"], KAT["senergy_sdir"])
+    np.testing.assert_allclose(got, KAT["senergy_val"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("mk", CONFIGS)
+def test_scene_struct_packs(mk):
+    from pyalbsim_gb300._native import scene_struct
+
+    s = build_scene(mk())
+    p, keep = scene_struct(s)
+    assert p.n_layers == len(s.layers)
+    assert p.steps == s.steps and p.k == s.k
+    assert abs(p.layers[p.n_layers - 1].bottom_depth - s.depth) < 1e-12
