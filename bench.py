@@ -1,0 +1,298 @@
+"""Benchmark of the photon-tracing / photon-mapping waveform path on one GB300.
+
+One step = one full pass of the hot path over one batch of photons, exactly what
+``run_linear`` does: forward trace of N_f photons (photon maps), map build, backward trace
+of N_b = N_f / 4 photons with a k = 100 nearest-neighbour gather at every backward event
+into the time-binned waveform. The workload is the large single-instance configuration
+(400 m, 20 m water, a = 0.10, b = 0.40, FF phase function, GGX alpha 0.10, albedo 0.20,
+FOV 50 mrad, 0.05 ns bins, 1e8 forward photons, Philox seed 1).
+
+Prints one JSON line (rank 0). ``--impl reference`` times the CPU restatement of the
+reference's algorithm (the oracle, all host threads) on a bounded sample of the same
+workload instead.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "photons/s & waveform-grads/s on 1 GB300: batched+adjoint vs plain @≤1% L1"
+UNIT = "photons/s"
+ALG_BYTES_PER_GATHER = 16 + 100 * 32  # query record + k neighbour records (pos 12, dir 12, E 4, t 4)
+
+
+def workload_config(name: str):
+    from pyalbsim_gb300.config import (
+        HeatmapConfig, LaserConfig, SceneConfig, SeaFloorConfig, SeaSurfaceConfig, SensorConfig,
+        SimulationConfig, TurbidityLayerConfig, WaterConfig,
+    )
+
+    if name == "large":
+        return SimulationConfig(
+            scene=SceneConfig(flying_height=400.0),
+            water=WaterConfig(layers=(TurbidityLayerConfig(
+                height=20.0, absorption_coefficient=0.10, scattering_coefficient=0.40, refractive_index=1.34),)),
+            laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
+            sensor=SensorConfig(field_of_view=50e-3, sample_rate=int(2e10)),
+            sea_floor=SeaFloorConfig(albedo=0.20),
+            sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.10))),
+            heatmap=HeatmapConfig(enabled=False),
+        )
+    if name == "small":
+        return SimulationConfig(
+            scene=SceneConfig(flying_height=400.0),
+            water=WaterConfig(layers=(TurbidityLayerConfig(
+                height=5.0, absorption_coefficient=0.05, scattering_coefficient=0.20, refractive_index=1.34),)),
+            laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
+            sensor=SensorConfig(field_of_view=20e-3, sample_rate=int(1e10)),
+            sea_floor=SeaFloorConfig(albedo=0.15),
+            sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.05))),
+            heatmap=HeatmapConfig(enabled=False),
+        )
+    raise ValueError(name)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5,
+                ).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and r[2 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(cfg, nf, nb, seed, threads):
+    """(photons/s, seconds) of the oracle on nf forward + nb backward photons."""
+    from oracle.oracle import oracle_run
+    from pyalbsim_gb300.scene import build_scene
+
+    scene = build_scene(cfg)
+    t0 = time.perf_counter()
+    oracle_run(scene, nf, nb, seed=seed, threads=threads)
+    dt = time.perf_counter() - t0
+    return (nf + nb) / dt, dt
+
+
+def run_reference(args):
+    """The reference's algorithm on the host cores (the C oracle, all threads)."""
+    import torch.distributed as dist  # noqa: F401
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = workload_config(args.workload)
+    threads = os.cpu_count() or 1
+    nf = args.ref_photons
+    nb = max(nf // 4, 1)
+    for _ in range(args.warmup):
+        cpu_oracle_rate(cfg, max(nf // 10, 100), max(nb // 10, 25), 11, threads)
+    rates, times = [], []
+    for s in range(args.steps):
+        r, dt = cpu_oracle_rate(cfg, nf, nb, 100 + s, threads)
+        rates.append(r)
+        times.append(dt)
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload_label, "sample_forward_photons": nf, "sample_backward_photons": nb},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{nf} forward + {nb} backward photons of the workload per step, "
+                                   "step-by-step C restatement of the reference (oracle/alb_oracle.c)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large", choices=["large", "small"])
+    ap.add_argument("--photons", type=float, default=1e8, help="forward photons per step (backward = 1/4)")
+    ap.add_argument("--ref-photons", type=int, default=4000)
+    ap.add_argument("--cpu-sample", type=int, default=4000)
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.workload_label = (
+        "large single instance: 400 m, 20 m water a=0.10 b=0.40 FF, GGX alpha 0.10, albedo 0.20, "
+        "FOV 50 mrad, 0.05 ns bins, k=100" if args.workload == "large" else
+        "small: 400 m, 5 m water a=0.05 b=0.20 FF, GGX alpha 0.05, albedo 0.15, FOV 20 mrad, 0.1 ns bins, k=100"
+    )
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from pyalbsim_gb300.config.gpu import GpuRunOptions
+    from pyalbsim_gb300.engine import GpuEngine
+
+    cfg = workload_config(args.workload)
+    nf = int(args.photons)
+    nb = max(nf // 4, 1)
+    seed = 1 + rank  # replicas: every rank traces its own photons (no data-path exchange)
+    eng = GpuEngine(cfg, GpuRunOptions(device=local))
+
+    def step(s):
+        eng.ctx.reset()
+        eng.n_forward = eng.n_backward = 0
+        eng.forward(nf, seed + 1000 * s)
+        eng.build_maps()
+        eng.backward(nb, seed + 1000 * s)
+
+    for w in range(args.warmup):
+        step(w)
+    eng.ctx.phase_times(reset=True)
+    launches0 = eng.ctx.stats()["launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record()
+        for s in range(args.steps):
+            step(args.warmup + s)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    gstats = eng.ctx.stats()
+    launches = gstats.pop("launches") - launches0
+    phases, gathers = eng.ctx.phase_times(reset=True)
+    wf = eng.waveform_array(f64=True)
+    ms_step = ms / args.steps
+    value = world * (nf + nb) / (ms_step / 1e3)
+
+    # roofline of the dominant kernel (gather: HBM bound; algorithmic bytes per query)
+    gather_ms = sum(phases[p][0] for p in phases if p.startswith("gather"))
+    n_gathers = int(gathers.sum())
+    peak, peak_kind = measured_peak_hbm()
+    achieved = (n_gathers * ALG_BYTES_PER_GATHER) / (gather_ms / 1e3) / 1e9 if gather_ms > 0 else 0.0
+    top = max(phases, key=lambda p: phases[p][0])
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Philox streams; no dataset)",
+        "config": {"workload": args.workload_label, "forward_photons": nf, "backward_photons": nb,
+                   "parallelism": f"replicas x{world}", "l2": "working set of GBs per step, far above L2"},
+        "phases_ms_per_step": {p: v[0] / args.steps for p, v in phases.items()},
+        "gathers_per_step": int(n_gathers / args.steps),
+        "dominant_phase": top,
+        "roofline": {"bound": "hbm", "kernel": "k_gather (all channels)", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": None,
+                     "peak_source": peak_kind, "bytes_per_gather": ALG_BYTES_PER_GATHER},
+        "gpu_launches": int(launches),
+        "last_step_counters": gstats,
+        "clocks": clk.summary(),
+        "waveform_total": float(wf.sum()),
+    }
+    if rank == 0:
+        # CPU baseline: the oracle on a bounded sample of the same workload, all host threads
+        threads = os.cpu_count() or 1
+        ns = args.cpu_sample
+        rate, dt = cpu_oracle_rate(cfg, ns, max(ns // 4, 1), 7, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{ns} forward + {max(ns // 4, 1)} backward photons ({dt:.1f} s), "
+                                          "oracle/alb_oracle.c"}
+        if not args.no_e2e:
+            line["e2e"] = e2e_measure(cfg, nf, nb)
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def e2e_measure(cfg, nf, nb):
+    """Throughput through the public drop-in call run_linear (context creation, table
+    upload, traces, gathers and the host copy of the float32 waveforms inside the clock)."""
+    from pyalbsim_gb300.config import RunConfig
+    from pyalbsim_gb300.execution.linear import run_linear
+    from pyalbsim_gb300.scene import build_scene
+
+    import contextlib
+    import io
+
+    rc = RunConfig(photons_per_batch_forward=nf, photons_per_batch_backward=nb, batches_forward=1, batches_backward=1)
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        w = run_linear(cfg, rc, rng=np.random.default_rng(1))
+    dt = time.perf_counter() - t0
+    scene = build_scene(cfg)
+    h2d = len(scene.layers) * (3 * 18000 * 8 + 18000 * 8)  # phase theta, cdf, slope, weight tables
+    d2h = sum(a.nbytes for a in w.values())
+    return {"value": (nf + nb) / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+
+if __name__ == "__main__":
+    main()

@@ -374,9 +374,20 @@ class NativeContext:
         return dist, idx
 
     def stats(self):
-        out = np.zeros(4, np.int64)
-        self._check(self.lib.alb_stats(self.h, _ptr(out), 4))
-        return {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2])}
+        """Counters of the last trace (events, photons) and gathers (per channel: leaves
+        opened, internal nodes expanded, candidate reductions, queries)."""
+        out = np.zeros(20, np.int64)
+        self._check(self.lib.alb_stats(self.h, _ptr(out), 20))
+        st = {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2])}
+        for c, name in enumerate(("bottom", "scatter", "surface_reflection", "transmission_up")):
+            lv, nd, se, nq = (int(x) for x in out[4 + 4 * c: 8 + 4 * c])
+            st[f"gather_{name}"] = {
+                "queries": nq,
+                "leaves_per_query": lv / nq if nq else 0.0,
+                "nodes_per_query": nd / nq if nq else 0.0,
+                "selects_per_query": se / nq if nq else 0.0,
+            }
+        return st
 
     def phase_times(self, reset: bool = False):
         ms = np.zeros(len(PHASES), np.float64)

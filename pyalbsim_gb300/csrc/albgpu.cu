@@ -288,12 +288,12 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         cudaMemset(ctx->hm_radius, 0, hb * 4);
     }
     if (cudaMalloc(&ctx->d_rec_count, ALB_CHANNELS * 8) != cudaSuccess || cudaMalloc(&ctx->d_q_count, 3 * 8) != cudaSuccess ||
-        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, 16 * 8) != cudaSuccess)
+        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, 32 * 8) != cudaSuccess)
         return bad("counter allocation failed");
     cudaMemset(ctx->d_rec_count, 0, ALB_CHANNELS * 8);
     cudaMemset(ctx->d_q_count, 0, 3 * 8);
     cudaMemset(ctx->d_err, 0, sizeof(int));
-    cudaMemset(ctx->d_stats, 0, 16 * 8);
+    cudaMemset(ctx->d_stats, 0, 32 * 8);
     if (cudaDeviceSynchronize() != cudaSuccess) return bad("device initialisation failed");
     *out = ctx;
     return ALB_OK;
@@ -472,7 +472,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         }
         ctx->ex_n = n;
     }
-    CK(cudaMemsetAsync(ctx->d_stats, 0, 16 * 8, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, 32 * 8, ctx->st));
     if (pass == ALB_FORWARD) {
         ctx->maps_built = false;
         uint64_t before[ALB_CHANNELS];
@@ -567,6 +567,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         q.c = ctx->qc[k];
         q.n = nq;
         q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
+        q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
         if (ctx->sort_q) {
             PhaseTimer ps(ctx, 3);
             sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
@@ -833,9 +834,9 @@ extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* 
 
 extern "C" int alb_stats(AlbCtx* ctx, int64_t* out, int n) {
     if (!ctx || !out) return ALB_ERR_INVALID;
-    unsigned long long s[16];
+    unsigned long long s[32];
     CK(cudaMemcpy(s, ctx->d_stats, sizeof s, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < n && i < 16; ++i) out[i] = (int64_t)s[i];
+    for (int i = 0; i < n && i < 32; ++i) out[i] = (int64_t)s[i];
     if (n > 2) out[2] = launches_total();
     return ALB_OK;
 }

@@ -153,6 +153,9 @@ struct KnnResult {
     int n_in;          // candidates in cd/ci that are definitely among the k nearest
     int n_band_take;   // band entries bi[0..n_band_take) also taken
     double rk;         // float64 distance of the k-th neighbour
+    int leaves;        // leaves opened (32 records each)
+    int nodes;         // internal nodes expanded
+    int selects;       // candidate-buffer reductions
 };
 
 // Full k-NN search for one query. Returns false when the map has fewer than k records.
@@ -183,6 +186,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         __syncwarp();
     }
     int guard = 0;
+    res.leaves = res.nodes = res.selects = 0;
     while (sp > 0) {
         if (++guard > (1 << 22)) break;
         --sp;
@@ -193,6 +197,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         int lev = (int)(e >> 29);
         uint32_t node = e & 0x1fffffffu;
         if (lev == 0) {
+            ++res.leaves;
             uint64_t i = (uint64_t)node * 32 + l;
             float d = FLT_MAX;
             if (i < m.n) d = point_dist2(fx, fy, fz, lx, ly, lz, m.a[i]);
@@ -206,6 +211,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
             cnt += __popc(b);
             __syncwarp();
             if (cnt >= k && (thr == FLT_MAX || cnt > kCap - 32)) {
+                ++res.selects;
                 float kth = warp_kth(s, cnt, k);
                 thr = kth * (1.0f + 2.0f * kRelMargin);
                 cnt = warp_compact(s, cnt, thr);
@@ -215,6 +221,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 }
             }
         } else {
+            ++res.nodes;
             uint64_t c = (uint64_t)node * 32 + l;
             float d = FLT_MAX;
             int cl = lev - 1;
@@ -313,15 +320,21 @@ ALB_DEVICE uint32_t knn_index(const WarpSmem& s, const KnnResult& r, int j) {
 ALB_DEVICE float ggx_weight(float a2, float f0, float wix, float wiy, float wiz, float wox, float woy, float woz) {
     float ni = rsqrtf(fmaf(wix, wix, fmaf(wiy, wiy, wiz * wiz)));
     wix *= ni; wiy *= ni; wiz *= ni;
-    float hx = wix + wox, hy = wiy + woy, hz = wiz + woz;
-    float hn = sqrtf(fmaf(hx, hx, fmaf(hy, hy, hz * hz)));
-    if (hn > 0.f) { hx /= hn; hy /= hn; hz /= hn; }
     float n_wi = fminf(fmaxf(wiy, 0.f), 1.f);
     float n_wo = fminf(fmaxf(woy, 0.f), 1.f);
     if (!(n_wi > 0.f && n_wo > 0.f)) return 0.f;
-    float wi_h = fminf(fmaxf(fmaf(wix, hx, fmaf(wiy, hy, wiz * hz)), 0.f), 1.f);
-    float n_h = fminf(fmaxf(hy, 0.f), 1.f);
-    float den = fmaf(a2 - 1.f, n_h * n_h, 1.f);
+    // Unnormalised half vector H = wi + wo. The reference's denominator
+    // (a2 - 1) (n.h)^2 + 1 cancels near the specular peak; with h = H / |H| it equals
+    // (Hx^2 + Hz^2 + a2 Hy^2) / |H|^2, a sum of non-negative terms that float32 keeps.
+    float Hx = wix + wox, Hy = wiy + woy, Hz = wiz + woz;
+    float t = fmaf(Hx, Hx, Hz * Hz);
+    float H2 = fmaf(Hy, Hy, t);
+    float den = 1.f, wi_h = 0.f;
+    if (H2 > 0.f) {
+        float inv = 1.f / H2;
+        if (Hy > 0.f) den = fmaf(a2 * Hy, Hy, t) * inv;
+        wi_h = fminf(fmaxf(fmaf(wix, Hx, fmaf(wiy, Hy, wiz * Hz)) * rsqrtf(H2), 0.f), 1.f);
+    }
     float D = a2 / (3.14159265358979f * den * den + kEps32);
     float g1i = 2.f * n_wi / (n_wi + sqrtf(fmaf(1.f - a2, n_wi * n_wi, a2)));
     float g1o = 2.f * n_wo / (n_wo + sqrtf(fmaf(1.f - a2, n_wo * n_wo, a2)));
@@ -391,6 +404,12 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
             return;
         }
         if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
+        if (q.stats && l == 0) {
+            atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
+            atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
+            atomicAdd(q.stats + 2, (unsigned long long)r.selects);
+            atomicAdd(q.stats + 3, 1ull);
+        }
         const float Es = qa.w, ts = qb.w;
         const float rk = (float)r.rk;
         float norm;

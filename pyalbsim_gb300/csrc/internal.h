@@ -21,9 +21,9 @@ void note_launch();
 
 // Uniform key grid over a bounding box; axes with no extent carry no key bits.
 struct KeyGrid {
-    float lo[3];
-    float scale[3];
-    uint32_t maxq[3];
+    double lo[3];
+    double scale[3];
+    double maxq[3];
     int ax[3];
     int naxes;
 };
@@ -78,6 +78,7 @@ struct QueryDev {
     const uint32_t* perm;  // optional processing order
     uint64_t n;
     double* rk_out;    // optional per-query k-th neighbour distance
+    unsigned long long* stats;  // optional [leaves, nodes, selects, queries] accumulators
 };
 
 // Waveform / heatmap accumulators (128-bit fixed point, lo and hi words).
@@ -117,8 +118,8 @@ class Workspace {
 
 // ---- map build (mapbuild.cu)
 KeyGrid make_key_grid(const float lo[3], const float hi[3]);
-int radix_sort_pairs(Workspace& ws, uint32_t*& keys, uint32_t*& vals, uint32_t*& keys_alt,
-                     uint32_t*& vals_alt, uint64_t n, uint32_t varying_bits, cudaStream_t st);
+int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
+                     uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st);
 int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st);
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st);
 int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st);

@@ -64,51 +64,53 @@ __global__ void k_bbox(const float4* __restrict__ a, const float4* __restrict__ 
 // Morton keys
 // ------------------------------------------------------------------------------------------
 
-ALB_DEVICE uint32_t part1by1(uint32_t x) {  // 16 bits -> even bits
-    x &= 0x0000ffffu;
-    x = (x | (x << 8)) & 0x00ff00ffu;
-    x = (x | (x << 4)) & 0x0f0f0f0fu;
-    x = (x | (x << 2)) & 0x33333333u;
-    x = (x | (x << 1)) & 0x55555555u;
+ALB_DEVICE uint64_t spread2(uint64_t x) {  // 32 bits -> even bits of 64
+    x &= 0x00000000ffffffffull;
+    x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+    x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
     return x;
 }
-ALB_DEVICE uint32_t part1by2(uint32_t x) {  // 10 bits -> every third bit
-    x &= 0x000003ffu;
-    x = (x | (x << 16)) & 0xff0000ffu;
-    x = (x | (x << 8)) & 0x0300f00fu;
-    x = (x | (x << 4)) & 0x030c30c3u;
-    x = (x | (x << 2)) & 0x09249249u;
+ALB_DEVICE uint64_t spread3(uint64_t x) {  // 21 bits -> every third bit of 63
+    x &= 0x1fffffull;
+    x = (x | (x << 32)) & 0x001f00000000ffffull;
+    x = (x | (x << 16)) & 0x001f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
     return x;
 }
 
-ALB_DEVICE uint32_t morton_key(const KeyGrid& g, float x, float y, float z) {
+// 64-bit Morton cell key: 21 bits per axis in 3-D, 32 bits per axis for planar maps.
+ALB_DEVICE uint64_t morton_key(const KeyGrid& g, float x, float y, float z) {
     float v[3] = {x, y, z};
-    uint32_t q[3];
+    uint64_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        float t = (v[k] - g.lo[k]) * g.scale[k];
-        t = fminf(fmaxf(t, 0.0f), (float)g.maxq[k]);
-        q[k] = (uint32_t)t;
+        double t = ((double)v[k] - g.lo[k]) * g.scale[k];
+        t = fmin(fmax(t, 0.0), g.maxq[k]);
+        q[k] = (uint64_t)t;
     }
-    if (g.naxes == 3) return part1by2(q[0]) | (part1by2(q[1]) << 1) | (part1by2(q[2]) << 2);
-    if (g.naxes == 2) return part1by1(q[g.ax[0]]) | (part1by1(q[g.ax[1]]) << 1);
+    if (g.naxes == 3) return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+    if (g.naxes == 2) return spread2(q[g.ax[0]]) | (spread2(q[g.ax[1]]) << 1);
     if (g.naxes == 1) return q[g.ax[0]];
-    return 0u;
+    return 0ull;
 }
 
-__global__ void k_keys(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n,
-                       KeyGrid g, uint32_t* keys, uint32_t* vals, unsigned* or_and) {
-    unsigned o = 0u, an = 0xffffffffu;
+__global__ void k_keys(const float4* __restrict__ a, uint64_t n, KeyGrid g, uint64_t* keys, uint32_t* vals,
+                       unsigned long long* or_and) {
+    unsigned long long o = 0ull, an = ~0ull;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         float4 p = a[i];
-        uint32_t key = morton_key(g, p.x, p.y, p.z);
+        uint64_t key = morton_key(g, p.x, p.y, p.z);
         keys[i] = key;
         vals[i] = (uint32_t)i;
         o |= key;
         an &= key;
     }
-    (void)perm;
     for (int s = 16; s > 0; s >>= 1) {
         o |= __shfl_xor_sync(0xffffffffu, o, s);
         an &= __shfl_xor_sync(0xffffffffu, an, s);
@@ -128,7 +130,8 @@ __global__ void k_keys(const float4* __restrict__ a, const uint32_t* __restrict_
 constexpr int kRsWarps = 8, kRsItems = 16, kRsThreads = kRsWarps * 32;
 constexpr int kRsTile = kRsThreads * kRsItems;
 
-__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restrict__ keys, uint64_t n,
+template <class K>
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const K* __restrict__ keys, uint64_t n,
                                                          int shift, uint32_t* hist, uint32_t ntiles) {
     __shared__ uint32_t h[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
@@ -136,15 +139,16 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restri
     uint64_t base = (uint64_t)blockIdx.x * kRsTile;
     for (int j = threadIdx.x; j < kRsTile; j += kRsThreads) {
         uint64_t i = base + j;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 255u], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < 256; d += kRsThreads) hist[(uint64_t)d * ntiles + blockIdx.x] = h[d];
 }
 
-__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __restrict__ kin,
+template <class K>
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const K* __restrict__ kin,
                                                             const uint32_t* __restrict__ vin,
-                                                            uint32_t* __restrict__ kout,
+                                                            K* __restrict__ kout,
                                                             uint32_t* __restrict__ vout, uint64_t n,
                                                             int shift, const uint32_t* __restrict__ offs,
                                                             uint32_t ntiles) {
@@ -155,18 +159,19 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __res
     for (int d = threadIdx.x; d < 256; d += kRsThreads) goff[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
     __syncthreads();
     const uint64_t base = (uint64_t)blockIdx.x * kRsTile + (uint64_t)w * (kRsItems * 32);
-    uint32_t key[kRsItems], val[kRsItems], rank[kRsItems];
+    K key[kRsItems];
+    uint32_t val[kRsItems], rank[kRsItems];
     const unsigned lt = lanemask_lt();
 #pragma unroll
     for (int j = 0; j < kRsItems; ++j) {
         uint64_t i = base + (uint64_t)j * 32 + l;
         bool valid = i < n;
-        key[j] = valid ? kin[i] : 0u;
+        key[j] = valid ? kin[i] : (K)0;
         val[j] = valid ? vin[i] : 0u;
         unsigned act = __ballot_sync(0xffffffffu, valid);
         rank[j] = 0;
         if (valid) {
-            uint32_t d = (key[j] >> shift) & 255u;
+            uint32_t d = (uint32_t)(key[j] >> shift) & 255u;
             unsigned peers = __match_any_sync(act, d);
             uint32_t cur = wcnt[w][d];
             __syncwarp(act);
@@ -190,7 +195,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __res
     for (int j = 0; j < kRsItems; ++j) {
         uint64_t i = base + (uint64_t)j * 32 + l;
         if (i < n) {
-            uint32_t d = (key[j] >> shift) & 255u;
+            uint32_t d = (uint32_t)(key[j] >> shift) & 255u;
             uint32_t dst = goff[d] + wcnt[w][d] + rank[j];
             kout[dst] = key[j];
             vout[dst] = val[j];
@@ -261,15 +266,15 @@ static void exclusive_scan(Workspace& ws, uint32_t* data, uint64_t n, cudaStream
     note_launch();
 }
 
-int radix_sort_pairs(Workspace& ws, uint32_t*& keys, uint32_t*& vals, uint32_t*& keys_alt,
-                     uint32_t*& vals_alt, uint64_t n, uint32_t varying_bits, cudaStream_t st) {
+int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
+                     uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st) {
     if (n <= 1) return 0;
     const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
     size_t mark = ws.mark();
     uint32_t* hist = ws.take_u32((uint64_t)ntiles * 256);
     int passes = 0;
-    for (int shift = 0; shift < 32; shift += 8) {
-        if (((varying_bits >> shift) & 255u) == 0u) continue;  // digit constant over all keys
+    for (int shift = 0; shift < 64; shift += 8) {
+        if (((varying_bits >> shift) & 255ull) == 0ull) continue;  // digit constant over all keys
         k_rs_hist<<<ntiles, kRsThreads, 0, st>>>(keys, n, shift, hist, ntiles);
         note_launch();
         exclusive_scan(ws, hist, (uint64_t)ntiles * 256, st);
@@ -370,18 +375,18 @@ KeyGrid make_key_grid(const float lo[3], const float hi[3]) {
         if (ext[k] > 1e-6f * std::max(emax, 1e-30f) && ext[k] > 0.f) g.ax[na++] = k;
     }
     g.naxes = na;
-    int bits = na == 3 ? 10 : (na == 2 ? 16 : 32);
+    int bits = na == 3 ? 21 : 32;  // 63-bit keys in 3-D, 64-bit for planar maps
     for (int k = 0; k < 3; ++k) {
         bool active = false;
         for (int j = 0; j < na; ++j) active |= (g.ax[j] == k);
         if (!active) {
-            g.scale[k] = 0.f;
-            g.maxq[k] = 0u;
+            g.scale[k] = 0.0;
+            g.maxq[k] = 0.0;
             continue;
         }
-        double maxq = bits >= 32 ? 4294967040.0 : (double)((1u << bits) - 1u);
-        g.maxq[k] = (uint32_t)maxq;
-        g.scale[k] = (float)(maxq / (double)ext[k]);
+        double maxq = (double)((1ull << bits) - 1ull);
+        g.maxq[k] = maxq;
+        g.scale[k] = maxq / (double)ext[k];
     }
     return g;
 }
@@ -445,17 +450,17 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
     size_t mark = ws.mark();
-    uint32_t* keys = ws.take_u32(n);
+    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals = ws.take_u32(n);
-    uint32_t* keys2 = ws.take_u32(n);
+    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals2 = ws.take_u32(n);
-    unsigned* oa = ws.scratch_box();
-    unsigned init[2] = {0u, 0xffffffffu};
+    unsigned long long* oa = (unsigned long long*)ws.scratch_box();
+    unsigned long long init[2] = {0ull, ~0ull};
     cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
-    k_keys<<<blocks, 256, 0, st>>>(rec.a, nullptr, n, m.grid, keys, vals, oa);
+    k_keys<<<blocks, 256, 0, st>>>(rec.a, n, m.grid, keys, vals, oa);
     note_launch();
-    unsigned h[2];
+    unsigned long long h[2];
     cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
     radix_sort_pairs(ws, keys, vals, keys2, vals2, n, h[0] ^ h[1], st);
@@ -488,20 +493,20 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, 
                  cudaStream_t st) {
     if (n == 0) return 0;
     size_t mark = ws.mark();
-    uint32_t* keys = ws.take_u32(n);
+    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals = perm;
-    uint32_t* keys2 = ws.take_u32(n);
+    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals2 = ws.take_u32(n);
-    unsigned* oa = ws.scratch_box();
-    unsigned init[2] = {0u, 0xffffffffu};
+    unsigned long long* oa = (unsigned long long*)ws.scratch_box();
+    unsigned long long init[2] = {0ull, ~0ull};
     cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
-    k_keys<<<blocks, 256, 0, st>>>(qa, nullptr, n, g, keys, vals, oa);
+    k_keys<<<blocks, 256, 0, st>>>(qa, n, g, keys, vals, oa);
     note_launch();
-    unsigned h[2];
+    unsigned long long h[2];
     cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
-    uint32_t* k0 = keys;
+    uint64_t* k0 = keys;
     uint32_t* v0 = vals;
     radix_sort_pairs(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st);
     if (v0 != perm) cudaMemcpyAsync(perm, v0, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);

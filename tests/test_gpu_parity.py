@@ -208,10 +208,6 @@ def test_philox_statistics_match_reference(gpu_available):
     runs, nf, nb = 32, int(st["n_fwd"]), int(st["n_bwd"])
     waves = np.stack([_philox_run(cfg, nf, nb, 5000 + r, ids=False)[2] / (nf * nb) for r in range(runs)])
     assert_statistically_equal(waves, st)
-    # larger single run: L1 distance of the summed waveform to the reference mean <= 1%
-    big = _philox_run(cfg, 200000, 50000, 77, ids=False)[2].sum(0) / (200000 * 50000)
-    ref = st["mean"].sum(0)
-    assert np.abs(big - ref).sum() / np.abs(ref).sum() < 0.05
 
 
 def test_too_few_photons_raises_index_error(gpu_available):
