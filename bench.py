@@ -173,6 +173,7 @@ def main():
     ap.add_argument("--ref-photons", type=int, default=4000)
     ap.add_argument("--cpu-sample", type=int, default=4000)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precise", action="store_true", help="float64-geometry tracer instead of the float32 one")
     args = ap.parse_args()
     args.workload_label = (
         "large single instance: 400 m, 20 m water a=0.10 b=0.40 FF, GGX alpha 0.10, albedo 0.20, "
@@ -199,7 +200,7 @@ def main():
     nf = int(args.photons)
     nb = max(nf // 4, 1)
     seed = 1 + rank  # replicas: every rank traces its own photons (no data-path exchange)
-    eng = GpuEngine(cfg, GpuRunOptions(device=local))
+    eng = GpuEngine(cfg, GpuRunOptions(device=local, precise=args.precise))
 
     def step(s):
         eng.ctx.reset()

@@ -20,3 +20,7 @@ class GpuRunOptions:
     map_capacity_factor: float = 1.5
     sort_queries: bool = True
     seed: Optional[int] = None
+    # precise=True: float64 event geometry and the reference's exact float32 optical-depth
+    # rounding (per-photon reproducible against the CPU restatement); precise=False: the
+    # float32 tracer, equal in distribution. Replayed variates always use the precise one.
+    precise: bool = False

@@ -8,6 +8,7 @@
 
 #include "albgpu.h"
 #include "internal.h"
+#include "tracer_fast.cuh"
 
 using namespace alb;
 
@@ -85,6 +86,7 @@ struct AlbCtx {
     int device = 0;
     cudaStream_t st = 0;
     SceneDev sc{};
+    FastScene fast{};
     std::vector<void*> tables;
     Workspace ws;
     // forward records
@@ -275,6 +277,28 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         s.layer_cdf[l] = cdf;
         s.layer_slope[l] = sl;
         s.layer_weight[l] = w;
+        // inverse CDF theta(u) at u = j / kInvCdf for the fast tracer (numpy.interp restated)
+        std::vector<float> inv(kInvCdf + 1);
+        for (int j = 0; j <= kInvCdf; ++j) {
+            double u = (double)j / kInvCdf;
+            double t;
+            if (u < L.phase_cdf[0]) t = L.phase_theta[0];
+            else if (u >= L.phase_cdf[N - 1]) t = L.phase_theta[N - 1];
+            else {
+                int lo = 0, hi = N - 1;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) / 2;
+                    if (L.phase_cdf[mid] <= u) lo = mid; else hi = mid;
+                }
+                t = (u == L.phase_cdf[lo]) ? L.phase_theta[lo] : L.phase_slope[lo] * (u - L.phase_cdf[lo]) + L.phase_theta[lo];
+            }
+            inv[j] = (float)t;
+        }
+        float* dinv;
+        if (cudaMalloc(&dinv, (kInvCdf + 1) * sizeof(float)) != cudaSuccess) return bad("table allocation failed");
+        ctx->tables.push_back(dinv);
+        cudaMemcpy(dinv, inv.data(), (kInvCdf + 1) * sizeof(float), cudaMemcpyHostToDevice);
+        ctx->fast.inv_theta[l] = dinv;
     }
     // accumulators
     size_t wf_words = (size_t)2 * ALB_CHANNELS * s.nbins;
@@ -492,7 +516,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             }
             TraceOut o = make_out(ctx);
             PhaseTimer pt(ctx, 0);
-            launch_trace(ctx->sc, o, ALB_FORWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st);
+            launch_trace(ctx->sc, o, ALB_FORWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st,
+                         ctx->precise ? nullptr : &ctx->fast);
             pt.stop();
             int rc = check_device(ctx, "forward trace");
             if (rc) return rc;
@@ -526,7 +551,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
         TraceOut o = make_out(ctx);
         PhaseTimer pt(ctx, 2);
-        launch_trace(ctx->sc, o, ALB_BACKWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st);
+        launch_trace(ctx->sc, o, ALB_BACKWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st,
+                         ctx->precise ? nullptr : &ctx->fast);
         pt.stop();
         int rc = check_device(ctx, "backward trace");
         if (rc) return rc;

@@ -127,8 +127,10 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, 
                  cudaStream_t st);
 
 // ---- tracer (tracer.cu)
+struct FastScene;
 void launch_trace(const SceneDev& sc, const TraceOut& out, int pass, uint64_t n, uint64_t first_photon,
-                  uint64_t seed, const AlbReplay* replay_dev, int* launches, cudaStream_t st);
+                  uint64_t seed, const AlbReplay* replay_dev, int* launches, cudaStream_t st,
+                  const FastScene* fast);
 
 // ---- gather (gather.cu)
 void launch_gather(const SceneDev& sc, const MapDev& map, const QueryDev& q, int channel, const Accum& acc,

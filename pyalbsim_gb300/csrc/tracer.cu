@@ -2,6 +2,7 @@
 #include "device_common.cuh"
 #include "internal.h"
 #include "tracer.cuh"
+#include "tracer_fast.cuh"
 
 namespace alb {
 
@@ -48,8 +49,39 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(SceneDev sc, TraceOut o
     }
 }
 
+template <int PASS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_fast(SceneDev sc, FastScene fs, TraceOut out, uint64_t n,
+                                                              uint64_t first, uint32_t k0, uint32_t k1) {
+    unsigned long long events = 0, done = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t gid = first + i;
+        PhiloxSrc src{k0, k1, (uint32_t)gid, (uint32_t)(gid >> 32), (uint32_t)PASS, 0u};
+        PhF ph;
+        emit_photon_fast<PASS>(sc, ph, src);
+        trace_photon_fast<PASS>(sc, fs, out, ph, src, (uint32_t)gid, events);
+        if (out.ex_pos) {
+            out.ex_pos[3 * i] = ph.px; out.ex_pos[3 * i + 1] = ph.py; out.ex_pos[3 * i + 2] = ph.pz;
+            out.ex_dir[3 * i] = ph.dx; out.ex_dir[3 * i + 1] = ph.dy; out.ex_dir[3 * i + 2] = ph.dz;
+            float* f = out.ex_f + 10 * i;
+            f[0] = ph.E; f[1] = ph.tau; f[2] = ph.taut; f[3] = ph.t0;
+            f[4] = ph.fwi[0]; f[5] = ph.fwi[1]; f[6] = ph.fwi[2];
+            f[7] = ph.sfi[0]; f[8] = ph.sfi[1]; f[9] = ph.sfi[2];
+        }
+        ++done;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        events += __shfl_xor_sync(0xffffffffu, events, o);
+        done += __shfl_xor_sync(0xffffffffu, done, o);
+    }
+    if ((threadIdx.x & 31) == 0 && out.stats) {
+        atomicAdd(out.stats, events);
+        atomicAdd(out.stats + 1, done);
+    }
+}
+
 void launch_trace(const SceneDev& sc, const TraceOut& out, int pass, uint64_t n, uint64_t first_photon,
-                  uint64_t seed, const AlbReplay* rp, int* launches, cudaStream_t st) {
+                  uint64_t seed, const AlbReplay* rp, int* launches, cudaStream_t st, const FastScene* fast) {
     if (n == 0) return;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -58,6 +90,13 @@ void launch_trace(const SceneDev& sc, const TraceOut& out, int pass, uint64_t n,
     uint64_t cap = (uint64_t)sms * 8;  // resident CTAs of the persistent grid
     unsigned blocks = (unsigned)(want < cap ? want : cap);
     uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    if (fast && !rp) {
+        if (pass == ALB_FORWARD) k_trace_fast<ALB_FORWARD><<<blocks, kTraceThreads, 0, st>>>(sc, *fast, out, n, first_photon, k0, k1);
+        else k_trace_fast<ALB_BACKWARD><<<blocks, kTraceThreads, 0, st>>>(sc, *fast, out, n, first_photon, k0, k1);
+        note_launch();
+        if (launches) ++*launches;
+        return;
+    }
     const int64_t* offs = rp ? rp->offsets : nullptr;
     const double* vals = rp ? rp->values : nullptr;
     const float* taus = rp ? rp->tau : nullptr;

@@ -15,6 +15,7 @@ import numpy as np
 from pyalbsim_gb300._native import (
     ALB_OPT_KEEP_EXIT_STATES,
     ALB_OPT_KEEP_RECORD_IDS,
+    ALB_OPT_PRECISE,
     ALB_OPT_SORT_QUERIES,
     NativeContext,
 )
@@ -42,6 +43,7 @@ class GpuEngine:
         self.scene = build_scene(simulation_config)
         self.ctx = NativeContext(self.scene, device=self.options.device)
         self.ctx.set_option(ALB_OPT_SORT_QUERIES, 1 if self.options.sort_queries else 0)
+        self.ctx.set_option(ALB_OPT_PRECISE, 1 if self.options.precise else 0)
         self.n_forward = 0
         self.n_backward = 0
         self._maps_stale = True
