@@ -289,6 +289,133 @@ int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*&
 }
 
 // ------------------------------------------------------------------------------------------
+// k-d order: a left-balanced median-split k-d tree over 32-record leaves. A node holding
+// c leaves gives its left child the largest power of two below c, so every aligned run of
+// 32^j leaves is one k-d subtree and the implicit 32-ary box tree inherits k-d cells
+// (tight, non-overlapping boxes) instead of Morton runs that straddle far-apart cells.
+// Built level by level: node boxes -> key (node, 16-bit coordinate on the node's widest
+// axis) -> stable radix sort of (key, permutation).
+// ------------------------------------------------------------------------------------------
+
+ALB_DEVICE void kd_node(uint64_t leaf, uint64_t L, int depth, uint64_t& a, uint64_t& c) {
+    a = 0;
+    c = L;
+    for (int i = 0; i < depth && c > 1; ++i) {
+        uint64_t left = 1ull << (63 - __clzll((long long)(c - 1)));
+        if (leaf - a < left) {
+            c = left;
+        } else {
+            a += left;
+            c -= left;
+        }
+    }
+}
+
+__global__ void k_iota(uint32_t* p, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = (uint32_t)i;
+}
+
+// node boxes of this level (ordered-int min/max), warp-aggregated when a warp is in one node
+__global__ void k_kd_bbox(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n, uint64_t L,
+                          int depth, unsigned* lo, unsigned* hi) {
+    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+         base += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = base + (threadIdx.x & 31);
+        bool valid = i < n;
+        uint64_t na = 0, nc = 0;
+        float x = 0.f, y = 0.f, z = 0.f;
+        if (valid) {
+            kd_node(i / 32, L, depth, na, nc);
+            float4 p = a[perm[i]];
+            x = p.x; y = p.y; z = p.z;
+        }
+        unsigned long long key = valid ? na : ~0ull;
+        unsigned peers = __match_any_sync(0xffffffffu, key);
+        unsigned ox0 = f2ord(x), oy0 = f2ord(y), oz0 = f2ord(z);
+        unsigned ox1 = ox0, oy1 = oy0, oz1 = oz0;
+        if (peers == 0xffffffffu) {
+            for (int o = 16; o > 0; o >>= 1) {
+                ox0 = min(ox0, __shfl_xor_sync(0xffffffffu, ox0, o)); ox1 = max(ox1, __shfl_xor_sync(0xffffffffu, ox1, o));
+                oy0 = min(oy0, __shfl_xor_sync(0xffffffffu, oy0, o)); oy1 = max(oy1, __shfl_xor_sync(0xffffffffu, oy1, o));
+                oz0 = min(oz0, __shfl_xor_sync(0xffffffffu, oz0, o)); oz1 = max(oz1, __shfl_xor_sync(0xffffffffu, oz1, o));
+            }
+            if ((threadIdx.x & 31) != 0) continue;
+        }
+        if (!valid || nc <= 1) continue;
+        atomicMin(lo + 3 * na, ox0); atomicMin(lo + 3 * na + 1, oy0); atomicMin(lo + 3 * na + 2, oz0);
+        atomicMax(hi + 3 * na, ox1); atomicMax(hi + 3 * na + 1, oy1); atomicMax(hi + 3 * na + 2, oz1);
+    }
+}
+
+__global__ void k_kd_keys(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n, uint64_t L,
+                          int depth, const unsigned* __restrict__ lo, const unsigned* __restrict__ hi, uint64_t* keys,
+                          unsigned long long* or_and) {
+    unsigned long long o = 0ull, an = ~0ull;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t na, nc;
+        kd_node(i / 32, L, depth, na, nc);
+        uint64_t q = 0;
+        if (nc > 1) {
+            float l0 = ord2f(lo[3 * na]), l1 = ord2f(lo[3 * na + 1]), l2 = ord2f(lo[3 * na + 2]);
+            float e0 = ord2f(hi[3 * na]) - l0, e1 = ord2f(hi[3 * na + 1]) - l1, e2 = ord2f(hi[3 * na + 2]) - l2;
+            float4 p = a[perm[i]];
+            float v, l, e;
+            if (e0 >= e1 && e0 >= e2) { v = p.x; l = l0; e = e0; }
+            else if (e1 >= e2) { v = p.y; l = l1; e = e1; }
+            else { v = p.z; l = l2; e = e2; }
+            if (e > 0.f) q = (uint64_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
+        }
+        uint64_t key = (na << 16) | q;
+        keys[i] = key;
+        o |= key;
+        an &= key;
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+        an &= __shfl_xor_sync(0xffffffffu, an, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicOr(or_and, o);
+        atomicAnd(or_and + 1, an);
+    }
+}
+
+// perm <- k-d order of the n records of `a`
+static void kd_order(Workspace& ws, const float4* a, uint64_t n, uint32_t*& perm, uint32_t*& perm_alt,
+                     cudaStream_t st) {
+    const uint64_t L = (n + 31) / 32;
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
+    k_iota<<<blocks, 256, 0, st>>>(perm, n);
+    note_launch();
+    if (L <= 1) return;
+    int depth_max = 64 - __builtin_clzll((unsigned long long)(L - 1));  // ceil(log2 L)
+    size_t mark = ws.mark();
+    unsigned* lo = (unsigned*)ws.take_bytes(L * 12);
+    unsigned* hi = (unsigned*)ws.take_bytes(L * 12);
+    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
+    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
+    unsigned long long* oa = (unsigned long long*)ws.scratch_box();
+    for (int d = 0; d < depth_max; ++d) {
+        cudaMemsetAsync(lo, 0xff, L * 12, st);
+        cudaMemsetAsync(hi, 0x00, L * 12, st);
+        k_kd_bbox<<<blocks, 256, 0, st>>>(a, perm, n, L, d, lo, hi);
+        note_launch();
+        unsigned long long init[2] = {0ull, ~0ull};
+        cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
+        k_kd_keys<<<blocks, 256, 0, st>>>(a, perm, n, L, d, lo, hi, keys, oa);
+        note_launch();
+        unsigned long long h[2];
+        cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        uint64_t* k0 = keys;
+        uint64_t* k1 = keys2;
+        radix_sort_pairs(ws, k0, perm, k1, perm_alt, n, h[0] ^ h[1], st);
+    }
+    ws.release(mark);
+}
+
+// ------------------------------------------------------------------------------------------
 // permutation and box tree
 // ------------------------------------------------------------------------------------------
 
@@ -450,20 +577,10 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
     size_t mark = ws.mark();
-    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals = ws.take_u32(n);
-    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals2 = ws.take_u32(n);
-    unsigned long long* oa = (unsigned long long*)ws.scratch_box();
-    unsigned long long init[2] = {0ull, ~0ull};
-    cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
-    k_keys<<<blocks, 256, 0, st>>>(rec.a, n, m.grid, keys, vals, oa);
-    note_launch();
-    unsigned long long h[2];
-    cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    radix_sort_pairs(ws, keys, vals, keys2, vals2, n, h[0] ^ h[1], st);
+    kd_order(ws, rec.a, n, vals, vals2, st);
     m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
     m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, n);
     k_permute4<<<blocks, 256, 0, st>>>(rec.a, vals, m.a, n);
