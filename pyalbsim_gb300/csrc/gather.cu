@@ -387,10 +387,43 @@ ALB_DEVICE Fix128 f32_to_fix(float v) {
     return r;
 }
 
+// Per-CTA shared-memory cache of waveform bins: direct-mapped on the bin index, a slot is
+// claimed once by CAS on its tag; hits are exact 128-bit integer adds in shared memory,
+// misses go to global memory. Flushed once when the CTA finishes. The sum is integer, so
+// the split between cache and global memory cannot change the result.
+constexpr int kBinCache = 1024;
+struct BinCache {
+    int tag[kBinCache];
+    unsigned long long lo[kBinCache];
+    unsigned long long hi[kBinCache];
+};
+
+ALB_DEVICE void bin_add(BinCache& bc, const Accum& acc, int channel, int bin, const Fix128& f) {
+    int slot = bin & (kBinCache - 1);
+    int t = bc.tag[slot];
+    if (t != bin && t == -1) {
+        int old = atomicCAS(&bc.tag[slot], -1, bin);
+        t = (old == -1) ? bin : old;
+    }
+    if (t == bin) {
+        fix_atomic_add(&bc.lo[slot], &bc.hi[slot], f);
+    } else {
+        uint64_t o = (uint64_t)channel * acc.nbins + bin;
+        fix_atomic_add(acc.wf_lo + o, acc.wf_hi + o, f);
+    }
+}
+
 template <int CHANNEL>
 __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
     __shared__ WarpSmem smem[kGatherWarps];
+    __shared__ BinCache bc;
+    for (int i = threadIdx.x; i < kBinCache; i += blockDim.x) {
+        bc.tag[i] = -1;
+        bc.lo[i] = 0ull;
+        bc.hi[i] = 0ull;
+    }
+    __syncthreads();
     const int w = threadIdx.x >> 5, l = lane_id();
     WarpSmem& s = smem[w];
     const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
@@ -401,7 +434,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
         KnnResult r;
         if (!warp_knn(m, s, k, qx, qy, qz, r)) {
             if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
-            return;
+            break;
         }
         if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
         if (q.stats && l == 0) {
@@ -433,9 +466,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
             float c = ((Es * pa.w) * norm) * w;
             int bin = (int)((ts + pb.w) / (float)sc.mult);
             if (bin >= 0 && bin < acc.nbins) {
-                Fix128 f = f32_to_fix(c);
-                uint64_t o = (uint64_t)CHANNEL * acc.nbins + bin;
-                fix_atomic_add(acc.wf_lo + o, acc.wf_hi + o, f);
+                bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
             } else {
                 atomicCAS(err, 0, ALB_ERR_CAPACITY);
             }
@@ -458,6 +489,15 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
             }
         }
         __syncwarp();
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBinCache; i += blockDim.x) {
+        int t = bc.tag[i];
+        if (t >= 0) {
+            uint64_t o = (uint64_t)CHANNEL * acc.nbins + t;
+            Fix128 f{bc.lo[i], (long long)bc.hi[i]};
+            fix_atomic_add(acc.wf_lo + o, acc.wf_hi + o, f);
+        }
     }
 }
 
