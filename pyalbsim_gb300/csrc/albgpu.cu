@@ -451,10 +451,10 @@ static int check_map_sizes(AlbCtx* ctx) {
         for (int j = 0; j < 2; ++j) {
             int c = need[k][j];
             if (c < 0) continue;
-            if (ctx->map[c].n < (uint64_t)ctx->sc.k) {
+            if (ctx->map[c].n_real < (uint64_t)ctx->sc.k) {
                 char buf[256];
                 snprintf(buf, sizeof buf, "photon map %s holds %llu records, fewer than k=%d", names[c],
-                         (unsigned long long)ctx->map[c].n, ctx->sc.k);
+                         (unsigned long long)ctx->map[c].n_real, ctx->sc.k);
                 return fail(ctx, ALB_ERR_TOO_FEW, buf);
             }
         }
@@ -615,7 +615,8 @@ extern "C" int alb_build_maps(AlbCtx* ctx) {
     CK(cudaSetDevice(ctx->device));
     PhaseTimer pt(ctx, 1);
     for (int c = 0; c < ALB_CHANNELS; ++c) {
-        build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st);
+        if (build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st) != 0)
+            return fail(ctx, ALB_ERR_CAPACITY, "photon-map index build failed (cell partition)");
     }
     pt.stop();
     int rc = check_device(ctx, "map build");
@@ -638,11 +639,8 @@ extern "C" int alb_export_map(AlbCtx* ctx, int c, float* pos, float* dir, float*
     if (m == 0) return ALB_OK;
     const float4 *a, *b, *fw, *sf;
     const uint32_t* id;
-    if (ctx->maps_built) {
-        a = ctx->map[c].a; b = ctx->map[c].b; id = ctx->map[c].id; fw = ctx->map[c].fwi; sf = ctx->map[c].sfi;
-    } else {
-        a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
-    }
+    // records in append order (the index holds them in k-d order with padding dummies)
+    a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
     std::vector<float4> ha(m), hb(m), hf, hs;
     CK(cudaMemcpy(ha.data(), a, m * 16, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hb.data(), b, m * 16, cudaMemcpyDeviceToHost));
@@ -745,6 +743,7 @@ extern "C" int alb_reset(AlbCtx* ctx) {
     for (int c = 0; c < ALB_CHANNELS; ++c) {
         ctx->h_rec_count[c] = 0;
         ctx->map[c].n = 0;
+        ctx->map[c].n_real = 0;
     }
     for (int k = 0; k < 3; ++k) ctx->h_q_count[k] = 0;
     ctx->maps_built = false;
@@ -838,7 +837,7 @@ extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* 
     CK(cudaMemsetAsync(r.b, 0, m * 16, ctx->st));
     CK(cudaMemcpyAsync(dq, qs, nq * 24, cudaMemcpyHostToDevice, ctx->st));
     MapIndex mi;
-    build_map_index(ctx->ws, r, m, mi, ctx->st);
+    if (build_map_index(ctx->ws, r, m, mi, ctx->st) != 0) return fail(ctx, ALB_ERR_CAPACITY, "knn index build failed");
     // indices returned by the search refer to the sorted order: map them back
     launch_knn(map_dev(mi), dq, nq, k, di, dd, ctx->d_err, ctx->st);
     std::vector<int32_t> sorted_idx(nq * k);

@@ -164,7 +164,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
     const int l = lane_id();
     const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
     const float lx = (float)(qx - (double)fx), ly = (float)(qy - (double)fy), lz = (float)(qz - (double)fz);
-    if (m.n < (uint64_t)k) return false;
+    if (m.n_real < (uint64_t)k) return false;
     float thr = FLT_MAX;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
     int sp = 0;

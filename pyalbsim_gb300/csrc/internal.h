@@ -40,7 +40,8 @@ struct RecordStore {
 
 // Sorted records + implicit 32-ary box tree of one channel.
 struct MapIndex {
-    uint64_t n = 0;
+    uint64_t n = 0;       // records in the index, including padding dummies
+    uint64_t n_real = 0;  // records of the photon map
     float4* a = nullptr;
     float4* b = nullptr;
     float4* fwi = nullptr;
@@ -65,6 +66,7 @@ struct MapDev {
     const float4* box_lo;
     const float4* box_hi;
     uint64_t n;
+    uint64_t n_real;
     int nlevels;
     uint64_t lvl_off[kMaxLevels];
     uint64_t lvl_cnt[kMaxLevels];
@@ -147,6 +149,7 @@ inline MapDev map_dev(const MapIndex& m) {
     d.box_lo = m.box_lo;
     d.box_hi = m.box_hi;
     d.n = m.n;
+    d.n_real = m.n_real;
     d.nlevels = m.nlevels;
     for (int i = 0; i < kMaxLevels; ++i) {
         d.lvl_off[i] = m.lvl_off[i];

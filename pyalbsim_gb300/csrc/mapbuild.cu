@@ -416,6 +416,326 @@ static void kd_order(Workspace& ws, const float4* a, uint64_t n, uint32_t*& perm
 }
 
 // ------------------------------------------------------------------------------------------
+// Sample-partitioned k-d order (the build used for photon maps):
+//  1. a median-split k-d tree of T levels is built on a strided sample of the records
+//     (kd_order above, on the sample only);
+//  2. every record descends the T split planes to one of 2^T cells (one pass);
+//  3. one radix sort groups the records by cell;
+//  4. one CTA per cell finishes an exact left-balanced k-d order of the cell's records in
+//     shared memory and pads the cell to whole 32-record leaves with dummy records (NaN
+//     position: never admitted by the gather, ignored by the box reductions).
+// Leaves therefore never straddle cells and are exact k-d leaves inside them.
+// ------------------------------------------------------------------------------------------
+__global__ void k_permute4(const float4* __restrict__ src, const uint32_t* __restrict__ perm,
+                           float4* __restrict__ dst, uint64_t n);
+
+constexpr int kCellMax = 4096;     // records per cell handled by one CTA
+constexpr int kCellThreads = 512;
+constexpr uint32_t kDummy = 0xffffffffu;
+
+__global__ void k_take_sample(const float4* __restrict__ a, uint64_t n, uint64_t stride, uint64_t S, float4* out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < S; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t j = i * stride;
+        out[i] = a[j < n ? j : n - 1];
+    }
+}
+
+// split planes of the top tree (heap order, node 1 = root) from the k-d ordered sample:
+// node j of level d covers sample positions [j*seg, (j+1)*seg), seg = S >> d; its plane is
+// the widest axis of the node's sample box at the coordinate of the element seg/2.
+// one CTA (256 threads) per node h = blockIdx.x + 1
+__global__ void __launch_bounds__(256) k_top_planes(const float4* __restrict__ s, uint64_t S, uint8_t* axis, float* value) {
+    __shared__ float red[6][8];
+    __shared__ int ax_s;
+    const uint64_t h = (uint64_t)blockIdx.x + 1;
+    const int d = 63 - __clzll((long long)h);
+    const uint64_t j = h - (1ull << d);
+    const uint64_t seg = S >> d;
+    const uint64_t b = j * seg, e = b + seg;
+    float v6[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        float4 p = s[i];
+        v6[0] = fminf(v6[0], p.x); v6[3] = fmaxf(v6[3], p.x);
+        v6[1] = fminf(v6[1], p.y); v6[4] = fmaxf(v6[4], p.y);
+        v6[2] = fminf(v6[2], p.z); v6[5] = fmaxf(v6[5], p.z);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            float x = __shfl_xor_sync(0xffffffffu, v6[k], o);
+            v6[k] = k < 3 ? fminf(v6[k], x) : fmaxf(v6[k], x);
+        }
+        if (l == 0) red[k][w] = v6[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r[6];
+        for (int k = 0; k < 6; ++k) {
+            r[k] = red[k][0];
+            for (int q = 1; q < 8; ++q) r[k] = k < 3 ? fminf(r[k], red[k][q]) : fmaxf(r[k], red[k][q]);
+        }
+        float e0 = r[3] - r[0], e1 = r[4] - r[1], e2 = r[5] - r[2];
+        ax_s = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2 ? 1 : 2);
+    }
+    __syncthreads();
+    // the sample inside the node is k-d ordered with its two halves as the children, so the
+    // plane is the largest coordinate of the left half on the node's axis
+    const int ax = ax_s;
+    float vmax = -3.4e38f;
+    for (uint64_t i = b + threadIdx.x; i < b + seg / 2; i += blockDim.x) {
+        float4 p = s[i];
+        vmax = fmaxf(vmax, ax == 0 ? p.x : (ax == 1 ? p.y : p.z));
+    }
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    __syncthreads();
+    if (l == 0) red[0][w] = vmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = red[0][0];
+        for (int q = 1; q < 8; ++q) r = fmaxf(r, red[0][q]);
+        axis[h] = (uint8_t)ax;
+        value[h] = r;
+    }
+}
+
+__global__ void k_assign_cells(const float4* __restrict__ a, uint64_t n, int T, const uint8_t* __restrict__ axis,
+                               const float* __restrict__ value, uint64_t* keys, uint32_t* vals, unsigned* counts) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float4 p = a[i];
+        uint32_t h = 1;
+        for (int d = 0; d < T; ++d) {
+            int ax = axis[h];
+            float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+            h = 2 * h + (c > value[h] ? 1u : 0u);
+        }
+        uint32_t cell = h - (1u << T);
+        keys[i] = cell;
+        vals[i] = (uint32_t)i;
+        atomicAdd(counts + cell, 1u);
+    }
+}
+
+__global__ void k_pad_counts(const unsigned* __restrict__ counts, uint32_t ncell, unsigned* padded, unsigned* maxc) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        unsigned k = counts[c];
+        padded[c] = (k + 31u) & ~31u;
+        atomicMax(maxc, k);
+    }
+}
+
+// exact left-balanced k-d order inside one cell; writes the padded permutation
+__global__ void __launch_bounds__(kCellThreads) k_cell_kd(const float4* __restrict__ a, const uint32_t* __restrict__ perm,
+                                                          const unsigned* __restrict__ start,
+                                                          const unsigned* __restrict__ count,
+                                                          const unsigned* __restrict__ pstart, uint32_t* out) {
+    extern __shared__ unsigned char smraw[];
+    unsigned long long* key = (unsigned long long*)smraw;        // kCellMax
+    float* X = (float*)(key + kCellMax);
+    float* Y = X + kCellMax;
+    float* Z = Y + kCellMax;
+    uint32_t* ID = (uint32_t*)(Z + kCellMax);
+    unsigned* blo = (unsigned*)(ID + kCellMax);                  // 3 * (kCellMax / 32)
+    unsigned* bhi = blo + 3 * (kCellMax / 32);
+    const uint32_t cell = blockIdx.x;
+    const unsigned cnt = count[cell];
+    if (cnt == 0) return;
+    const unsigned P = (cnt + 31u) & ~31u;
+    const unsigned Lc = P / 32;
+    unsigned P2 = 32;
+    while (P2 < P) P2 <<= 1;
+    const unsigned s0 = start[cell];
+    const float qnan = __int_as_float(0x7fc00000);
+    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) {
+        if (j < cnt) {
+            uint32_t id = perm[s0 + j];
+            float4 p = a[id];
+            X[j] = p.x; Y[j] = p.y; Z[j] = p.z; ID[j] = id;
+        } else {
+            X[j] = qnan; Y[j] = qnan; Z[j] = qnan; ID[j] = kDummy;
+        }
+    }
+    __syncthreads();
+    int depth = 0;
+    while ((1u << depth) < Lc) ++depth;
+    for (int d = 0; d < depth; ++d) {
+        for (unsigned i = threadIdx.x; i < 3 * Lc; i += blockDim.x) {
+            blo[i] = 0xffffffffu;
+            bhi[i] = 0u;
+        }
+        __syncthreads();
+        for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) {
+            uint64_t na, nc;
+            kd_node(j / 32, Lc, d, na, nc);
+            if (nc > 1) {
+                atomicMin(blo + 3 * na, f2ord(X[j])); atomicMax(bhi + 3 * na, f2ord(X[j]));
+                atomicMin(blo + 3 * na + 1, f2ord(Y[j])); atomicMax(bhi + 3 * na + 1, f2ord(Y[j]));
+                atomicMin(blo + 3 * na + 2, f2ord(Z[j])); atomicMax(bhi + 3 * na + 2, f2ord(Z[j]));
+            }
+        }
+        __syncthreads();
+        for (unsigned j = threadIdx.x; j < P2; j += blockDim.x) {
+            unsigned long long k = ~0ull;
+            if (j < P) {
+                uint64_t na, nc;
+                kd_node(j / 32, Lc, d, na, nc);
+                uint64_t q = 0;
+                if (j >= cnt) {
+                    q = 0x1ffff;  // dummies sort last inside their node
+                } else if (nc > 1) {
+                    float l0 = ord2f(blo[3 * na]), l1 = ord2f(blo[3 * na + 1]), l2 = ord2f(blo[3 * na + 2]);
+                    float e0 = ord2f(bhi[3 * na]) - l0, e1 = ord2f(bhi[3 * na + 1]) - l1, e2 = ord2f(bhi[3 * na + 2]) - l2;
+                    float v, l, e;
+                    if (e0 >= e1 && e0 >= e2) { v = X[j]; l = l0; e = e0; }
+                    else if (e1 >= e2) { v = Y[j]; l = l1; e = e1; }
+                    else { v = Z[j]; l = l2; e = e2; }
+                    if (e > 0.f) q = (uint64_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
+                }
+                k = (((na << 17) | q) << 13) | j;  // j < 8192 keeps equal keys in place
+            }
+            key[j] = k;
+        }
+        __syncthreads();
+        // bitonic sort of P2 keys, ascending
+        for (unsigned kk = 2; kk <= P2; kk <<= 1) {
+            for (unsigned jj = kk >> 1; jj > 0; jj >>= 1) {
+                for (unsigned i = threadIdx.x; i < P2; i += blockDim.x) {
+                    unsigned p = i ^ jj;
+                    if (p > i) {
+                        unsigned long long x = key[i], y = key[p];
+                        bool up = (i & kk) == 0;
+                        if ((x > y) == up) {
+                            key[i] = y;
+                            key[p] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // gather the records into the new order (each thread keeps its own in registers)
+        float rx[kCellMax / kCellThreads], ry[kCellMax / kCellThreads], rz[kCellMax / kCellThreads];
+        uint32_t rid[kCellMax / kCellThreads];
+        int t = 0;
+        for (unsigned j = threadIdx.x; j < P; j += blockDim.x, ++t) {
+            unsigned src = (unsigned)(key[j] & 0x1fffull);
+            rx[t] = X[src]; ry[t] = Y[src]; rz[t] = Z[src]; rid[t] = ID[src];
+        }
+        __syncthreads();
+        t = 0;
+        for (unsigned j = threadIdx.x; j < P; j += blockDim.x, ++t) {
+            X[j] = rx[t]; Y[j] = ry[t]; Z[j] = rz[t]; ID[j] = rid[t];
+        }
+        __syncthreads();
+    }
+    const unsigned o = pstart[cell];
+    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) out[o + j] = ID[j];
+}
+
+// records in the padded k-d order; dummies get a NaN position (their w lane keeps the tag)
+__global__ void k_permute4_pad(const float4* __restrict__ src, const uint32_t* __restrict__ perm, float4* __restrict__ dst,
+                               uint64_t n) {
+    const float qnan = __int_as_float(0x7fc00000);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = perm[i];
+        dst[i] = p == kDummy ? make_float4(qnan, qnan, qnan, __uint_as_float(kDummy)) : src[p];
+    }
+}
+
+__global__ void k_permute_u32_pad(const uint32_t* __restrict__ src, const uint32_t* __restrict__ perm,
+                                  uint32_t* __restrict__ dst, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t p = perm[i];
+        dst[i] = p == kDummy ? kDummy : src[p];
+    }
+}
+
+static size_t cell_smem_bytes() {
+    return (size_t)kCellMax * 8 + (size_t)kCellMax * 16 + (size_t)2 * 3 * (kCellMax / 32) * 4;
+}
+
+// perm_out (capacity >= padded count) <- padded k-d order; returns the padded count or 0 on
+// failure (cells too large after retries)
+static uint64_t sampled_kd_order(Workspace& ws, const float4* a, uint64_t n, uint32_t* perm_out, uint64_t perm_cap,
+                                 cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_cell_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
+        attr_set = true;
+    }
+    int T = 0;
+    while ((n >> T) > (uint64_t)(kCellMax / 3)) ++T;
+    for (int attempt = 0; attempt < 4; ++attempt, ++T) {
+        size_t mark = ws.mark();
+        const uint32_t ncell = 1u << T;
+        uint8_t* axis = (uint8_t*)ws.take_bytes((uint64_t)ncell + 1);
+        float* value = (float*)ws.take_bytes(((uint64_t)ncell + 1) * 4);
+        if (T > 0) {
+            uint64_t S = std::min<uint64_t>((uint64_t)ncell * 32, n);
+            S = 1ull << (63 - __builtin_clzll(S));  // power of two
+            if (S < ((uint64_t)ncell << 1)) S = (uint64_t)ncell << 1;
+            uint64_t stride = std::max<uint64_t>(n / S, 1);
+            float4* smp = (float4*)ws.take_bytes(S * 16);
+            float4* smp2 = (float4*)ws.take_bytes(S * 16);
+            uint32_t* sp = ws.take_u32(S);
+            uint32_t* sp2 = ws.take_u32(S);
+            unsigned blocks = (unsigned)std::min<uint64_t>((S + 255) / 256, 8192);
+            k_take_sample<<<blocks, 256, 0, st>>>(a, n, stride, S, smp);
+            note_launch();
+            // k-d order of the sample with the level-synchronous builder: 32-record
+            // leaves, so levels above 5 split the sample in power-of-two halves
+            kd_order(ws, smp, S, sp, sp2, st);
+            k_permute4<<<blocks, 256, 0, st>>>(smp, sp, smp2, S);
+            note_launch();
+            k_top_planes<<<ncell - 1, 256, 0, st>>>(smp2, S, axis, value);
+            note_launch();
+        }
+        unsigned* counts = ws.take_u32(ncell);
+        unsigned* padded = ws.take_u32(ncell);
+        unsigned* starts = ws.take_u32(ncell);
+        unsigned* pstarts = ws.take_u32(ncell);
+        uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
+        uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
+        uint32_t* vals = ws.take_u32(n);
+        uint32_t* vals2 = ws.take_u32(n);
+        unsigned* maxc = ws.scratch_box();
+        cudaMemsetAsync(counts, 0, (size_t)ncell * 4, st);
+        cudaMemsetAsync(maxc, 0, 4, st);
+        unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
+        k_assign_cells<<<blocks, 256, 0, st>>>(a, n, T, axis, value, keys, vals, counts);
+        note_launch();
+        k_pad_counts<<<(ncell + 255) / 256, 256, 0, st>>>(counts, ncell, padded, maxc);
+        note_launch();
+        unsigned hmax = 0;
+        cudaMemcpyAsync(&hmax, maxc, 4, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        if (hmax > (unsigned)kCellMax) {  // unlucky sample: more cells
+            ws.release(mark);
+            continue;
+        }
+        cudaMemcpyAsync(starts, counts, (size_t)ncell * 4, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(pstarts, padded, (size_t)ncell * 4, cudaMemcpyDeviceToDevice, st);
+        exclusive_scan(ws, starts, ncell, st);
+        exclusive_scan(ws, pstarts, ncell, st);
+        unsigned last_ps = 0, last_pad = 0;
+        cudaMemcpyAsync(&last_ps, pstarts + ncell - 1, 4, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&last_pad, padded + ncell - 1, 4, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        uint64_t total = (uint64_t)last_ps + last_pad;
+        if (total > perm_cap) {
+            ws.release(mark);
+            return 0;
+        }
+        if (T > 0) radix_sort_pairs(ws, keys, vals, keys2, vals2, n, (uint64_t)ncell - 1, st);
+        k_cell_kd<<<ncell, kCellThreads, cell_smem_bytes(), st>>>(a, vals, starts, counts, pstarts, perm_out);
+        note_launch();
+        ws.release(mark);
+        return total;
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------
 // permutation and box tree
 // ------------------------------------------------------------------------------------------
 
@@ -569,6 +889,7 @@ int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float 
 // Sort the records of one channel into Morton order and build the box tree.
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st) {
     m.n = n;
+    m.n_real = n;
     if (n == 0) {
         m.nlevels = 0;
         return 0;
@@ -577,27 +898,33 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
     size_t mark = ws.mark();
-    uint32_t* vals = ws.take_u32(n);
-    uint32_t* vals2 = ws.take_u32(n);
-    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
-    kd_order(ws, rec.a, n, vals, vals2, st);
-    m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
-    m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, n);
-    k_permute4<<<blocks, 256, 0, st>>>(rec.a, vals, m.a, n);
+    const uint64_t cap = n + n / 4 + 64;  // padding is at most 31 dummies per cell
+    uint32_t* vals = ws.take_u32(cap);
+    uint64_t np = sampled_kd_order(ws, rec.a, n, vals, cap, st);
+    if (np == 0) {
+        ws.release(mark);
+        return -1;
+    }
+    m.n_real = n;
+    m.n = np;
+    unsigned blocks = (unsigned)std::min<uint64_t>((np + 255) / 256, 8192);
+    m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, np);
+    m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, np);
+    k_permute4_pad<<<blocks, 256, 0, st>>>(rec.a, vals, m.a, np);
     note_launch();
-    k_permute4<<<blocks, 256, 0, st>>>(rec.b, vals, m.b, n);
+    k_permute4_pad<<<blocks, 256, 0, st>>>(rec.b, vals, m.b, np);
     note_launch();
     if (rec.fwi) {
-        m.fwi = (float4*)ws.alloc_persistent(m.fwi, m.fwi_cap, n);
-        m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, n);
-        k_permute4<<<blocks, 256, 0, st>>>(rec.fwi, vals, m.fwi, n);
+        m.fwi = (float4*)ws.alloc_persistent(m.fwi, m.fwi_cap, np);
+        m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, np);
+        k_permute4_pad<<<blocks, 256, 0, st>>>(rec.fwi, vals, m.fwi, np);
         note_launch();
-        k_permute4<<<blocks, 256, 0, st>>>(rec.sfi, vals, m.sfi, n);
+        k_permute4_pad<<<blocks, 256, 0, st>>>(rec.sfi, vals, m.sfi, np);
         note_launch();
     }
     if (rec.id) {
-        m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, n);
-        k_permute_u32<<<blocks, 256, 0, st>>>(rec.id, vals, m.id, n);
+        m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, np);
+        k_permute_u32_pad<<<blocks, 256, 0, st>>>(rec.id, vals, m.id, np);
         note_launch();
     }
     build_box_tree(ws, m, st);
