@@ -845,8 +845,8 @@ extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* 
     if (rc) return rc;
     CK(cudaMemcpy(sorted_idx.data(), di, nq * k * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(dist, dd, nq * k * 8, cudaMemcpyDeviceToHost));
-    std::vector<float4> sa(m);
-    CK(cudaMemcpy(sa.data(), mi.a, m * 16, cudaMemcpyDeviceToHost));
+    std::vector<float4> sa(mi.n);  // the index may hold more slots than points
+    CK(cudaMemcpy(sa.data(), mi.a, mi.n * 16, cudaMemcpyDeviceToHost));
     cudaFree(mi.a); cudaFree(mi.b); cudaFree(mi.box_lo); cudaFree(mi.box_hi);
     ctx->ws.release(mark);
     for (uint64_t i = 0; i < nq * (uint64_t)k; ++i) {

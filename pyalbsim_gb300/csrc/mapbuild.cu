@@ -898,13 +898,10 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
     size_t mark = ws.mark();
-    const uint64_t cap = n + n / 4 + 64;  // padding is at most 31 dummies per cell
-    uint32_t* vals = ws.take_u32(cap);
-    uint64_t np = sampled_kd_order(ws, rec.a, n, vals, cap, st);
-    if (np == 0) {
-        ws.release(mark);
-        return -1;
-    }
+    uint32_t* vals = ws.take_u32(n);
+    uint32_t* vals2 = ws.take_u32(n);
+    kd_order(ws, rec.a, n, vals, vals2, st);
+    const uint64_t np = n;
     m.n_real = n;
     m.n = np;
     unsigned blocks = (unsigned)std::min<uint64_t>((np + 255) / 256, 8192);
