@@ -177,6 +177,21 @@ int alb_export_queries(AlbCtx* ctx, int kind, double* pos, float* dir, float* en
 int alb_knn(AlbCtx* ctx, const float* points, uint64_t m, const double* queries, uint64_t q,
             int k, int32_t* idx, double* dist);
 
+/* KDTree(points).query(queries, k) that allocates no device memory. It has no counterpart
+ * in the reference: it exists for callers that cannot call cudaMalloc (code running during
+ * a CUDA-graph stream capture, real-time loops that allocate only at start-up, processes
+ * whose device memory belongs to another framework's pool). All buffers are DEVICE
+ * pointers owned by the caller: points float[3m], queries double[3q], idx int32[q*k]
+ * (nearest first), dist double[q*k]; stream is a cudaStream_t (NULL = legacy default).
+ * The k-d index is built in a fixed static device array: m <= ALB_NOALLOC_MAX_POINTS,
+ * k <= 256, larger inputs are rejected with ALB_ERR_INVALID. The first call on a device
+ * resolves the array's address (make it before any stream capture); calls that overlap
+ * on the GPU share the array and race. Asynchronous on `stream`; the message of a failed
+ * call is alb_last_error(NULL). */
+#define ALB_NOALLOC_MAX_POINTS 4096
+int alb_knn_noalloc(const float* points_dev, uint64_t m, const double* queries_dev, uint64_t q, int k,
+                    int32_t* idx_dev, double* dist_dev, void* stream);
+
 /* Device-side counters of the last trace / gather (events, records, queries, launches). */
 int alb_stats(AlbCtx* ctx, int64_t* out, int n);
 

@@ -113,6 +113,7 @@ EXPORTED = [
     "alb_stats",
     "alb_phase_times",
     "alb_reset",
+    "alb_knn_noalloc",
 ]
 
 PHASES = ["trace_fwd", "map_build", "trace_bwd", "query_sort", "gather_bottom", "gather_scatter",
@@ -154,6 +155,7 @@ def load_library(path: str = LIB_PATH):
     lib.alb_stats.argtypes = [_P, _P, C.c_int]
     lib.alb_phase_times.argtypes = [_P, _P, _P, _P, C.c_int]
     lib.alb_reset.argtypes = [_P]
+    lib.alb_knn_noalloc.argtypes = [_P, C.c_uint64, _P, C.c_uint64, C.c_int, _P, _P, _P]
     _lib = lib
     return lib
 

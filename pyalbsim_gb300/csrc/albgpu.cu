@@ -190,6 +190,11 @@ static int check_device(AlbCtx* ctx, const char* where) {
 
 static thread_local std::string g_create_error;
 
+namespace alb {
+// message of a failure that has no context (alb_create, alb_knn_noalloc)
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace alb
+
 extern "C" const char* alb_last_error(const AlbCtx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
 extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {

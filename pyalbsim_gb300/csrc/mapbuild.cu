@@ -929,6 +929,36 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     return 0;
 }
 
+// Single-cell index build into caller-provided device memory (no allocation): the k-d
+// order of n <= kCellMax points (one CTA), the padded permuted copy and its box tree.
+// `cell` holds {start = 0, count = n, pstart = 0}; perm_in is the identity.
+int cell_index_max_points() { return kCellMax; }
+
+void launch_single_cell_index(const float4* pts, uint32_t n, const uint32_t* perm_in, const unsigned* cell,
+                              uint32_t* perm_out, float4* sorted, float4* box_lo, float4* box_hi,
+                              const uint64_t* lvl_off, const uint64_t* lvl_cnt, int nlevels, cudaStream_t st) {
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        cudaFuncSetAttribute(k_cell_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
+        attr_set[dev] = true;
+    }
+    const uint32_t P = (n + 31u) & ~31u;
+    k_cell_kd<<<1, kCellThreads, cell_smem_bytes(), st>>>(pts, perm_in, cell, cell + 1, cell + 2, perm_out);
+    note_launch();
+    k_permute4_pad<<<(P + 255) / 256, 256, 0, st>>>(pts, perm_out, sorted, P);
+    note_launch();
+    k_leaf_boxes<<<(unsigned)((lvl_cnt[0] * 32 + 255) / 256), 256, 0, st>>>(sorted, P, box_lo, box_hi, lvl_cnt[0]);
+    note_launch();
+    for (int l = 1; l < nlevels; ++l) {
+        k_parent_boxes<<<(unsigned)((lvl_cnt[l] * 32 + 255) / 256), 256, 0, st>>>(
+            box_lo + lvl_off[l - 1], box_hi + lvl_off[l - 1], lvl_cnt[l - 1], box_lo + lvl_off[l], box_hi + lvl_off[l],
+            lvl_cnt[l]);
+        note_launch();
+    }
+}
+
 // Spatial order of gather queries under a map's key grid (for cache locality).
 int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, uint32_t* perm,
                  cudaStream_t st) {
