@@ -293,8 +293,8 @@ int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*&
 // c leaves gives its left child the largest power of two below c, so every aligned run of
 // 32^j leaves is one k-d subtree and the implicit 32-ary box tree inherits k-d cells
 // (tight, non-overlapping boxes) instead of Morton runs that straddle far-apart cells.
-// Built level by level: node boxes -> key (node, 16-bit coordinate on the node's widest
-// axis) -> stable radix sort of (key, permutation).
+// Every split cuts the node's widest box axis at the 16-bit quantised coordinate that
+// leaves exactly the left child's record count on its side.
 // ------------------------------------------------------------------------------------------
 
 ALB_DEVICE void kd_node(uint64_t leaf, uint64_t L, int depth, uint64_t& a, uint64_t& c) {
@@ -311,266 +311,58 @@ ALB_DEVICE void kd_node(uint64_t leaf, uint64_t L, int depth, uint64_t& a, uint6
     }
 }
 
-__global__ void k_iota(uint32_t* p, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        p[i] = (uint32_t)i;
-}
-
-// node boxes of this level (ordered-int min/max), warp-aggregated when a warp is in one node
-__global__ void k_kd_bbox(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n, uint64_t L,
-                          int depth, unsigned* lo, unsigned* hi) {
-    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
-         base += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t i = base + (threadIdx.x & 31);
-        bool valid = i < n;
-        uint64_t na = 0, nc = 0;
-        float x = 0.f, y = 0.f, z = 0.f;
-        if (valid) {
-            kd_node(i / 32, L, depth, na, nc);
-            float4 p = a[perm[i]];
-            x = p.x; y = p.y; z = p.z;
-        }
-        unsigned long long key = valid ? na : ~0ull;
-        unsigned peers = __match_any_sync(0xffffffffu, key);
-        unsigned ox0 = f2ord(x), oy0 = f2ord(y), oz0 = f2ord(z);
-        unsigned ox1 = ox0, oy1 = oy0, oz1 = oz0;
-        if (peers == 0xffffffffu) {
-            for (int o = 16; o > 0; o >>= 1) {
-                ox0 = min(ox0, __shfl_xor_sync(0xffffffffu, ox0, o)); ox1 = max(ox1, __shfl_xor_sync(0xffffffffu, ox1, o));
-                oy0 = min(oy0, __shfl_xor_sync(0xffffffffu, oy0, o)); oy1 = max(oy1, __shfl_xor_sync(0xffffffffu, oy1, o));
-                oz0 = min(oz0, __shfl_xor_sync(0xffffffffu, oz0, o)); oz1 = max(oz1, __shfl_xor_sync(0xffffffffu, oz1, o));
-            }
-            if ((threadIdx.x & 31) != 0) continue;
-        }
-        if (!valid || nc <= 1) continue;
-        atomicMin(lo + 3 * na, ox0); atomicMin(lo + 3 * na + 1, oy0); atomicMin(lo + 3 * na + 2, oz0);
-        atomicMax(hi + 3 * na, ox1); atomicMax(hi + 3 * na + 1, oy1); atomicMax(hi + 3 * na + 2, oz1);
-    }
-}
-
-__global__ void k_kd_keys(const float4* __restrict__ a, const uint32_t* __restrict__ perm, uint64_t n, uint64_t L,
-                          int depth, const unsigned* __restrict__ lo, const unsigned* __restrict__ hi, uint64_t* keys,
-                          unsigned long long* or_and) {
-    unsigned long long o = 0ull, an = ~0ull;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t na, nc;
-        kd_node(i / 32, L, depth, na, nc);
-        uint64_t q = 0;
-        if (nc > 1) {
-            float l0 = ord2f(lo[3 * na]), l1 = ord2f(lo[3 * na + 1]), l2 = ord2f(lo[3 * na + 2]);
-            float e0 = ord2f(hi[3 * na]) - l0, e1 = ord2f(hi[3 * na + 1]) - l1, e2 = ord2f(hi[3 * na + 2]) - l2;
-            float4 p = a[perm[i]];
-            float v, l, e;
-            if (e0 >= e1 && e0 >= e2) { v = p.x; l = l0; e = e0; }
-            else if (e1 >= e2) { v = p.y; l = l1; e = e1; }
-            else { v = p.z; l = l2; e = e2; }
-            if (e > 0.f) q = (uint64_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
-        }
-        uint64_t key = (na << 16) | q;
-        keys[i] = key;
-        o |= key;
-        an &= key;
-    }
-    for (int s = 16; s > 0; s >>= 1) {
-        o |= __shfl_xor_sync(0xffffffffu, o, s);
-        an &= __shfl_xor_sync(0xffffffffu, an, s);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicOr(or_and, o);
-        atomicAnd(or_and + 1, an);
-    }
-}
-
-// perm <- k-d order of the n records of `a`
-static void kd_order(Workspace& ws, const float4* a, uint64_t n, uint32_t*& perm, uint32_t*& perm_alt,
-                     cudaStream_t st) {
-    const uint64_t L = (n + 31) / 32;
-    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
-    k_iota<<<blocks, 256, 0, st>>>(perm, n);
-    note_launch();
-    if (L <= 1) return;
-    int depth_max = 64 - __builtin_clzll((unsigned long long)(L - 1));  // ceil(log2 L)
-    size_t mark = ws.mark();
-    unsigned* lo = (unsigned*)ws.take_bytes(L * 12);
-    unsigned* hi = (unsigned*)ws.take_bytes(L * 12);
-    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
-    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
-    unsigned long long* oa = (unsigned long long*)ws.scratch_box();
-    for (int d = 0; d < depth_max; ++d) {
-        cudaMemsetAsync(lo, 0xff, L * 12, st);
-        cudaMemsetAsync(hi, 0x00, L * 12, st);
-        k_kd_bbox<<<blocks, 256, 0, st>>>(a, perm, n, L, d, lo, hi);
-        note_launch();
-        unsigned long long init[2] = {0ull, ~0ull};
-        cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
-        k_kd_keys<<<blocks, 256, 0, st>>>(a, perm, n, L, d, lo, hi, keys, oa);
-        note_launch();
-        unsigned long long h[2];
-        cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        uint64_t* k0 = keys;
-        uint64_t* k1 = keys2;
-        radix_sort_pairs(ws, k0, perm, k1, perm_alt, n, h[0] ^ h[1], st);
-    }
-    ws.release(mark);
-}
-
-// ------------------------------------------------------------------------------------------
-// Sample-partitioned k-d order (the build used for photon maps):
-//  1. a median-split k-d tree of T levels is built on a strided sample of the records
-//     (kd_order above, on the sample only);
-//  2. every record descends the T split planes to one of 2^T cells (one pass);
-//  3. one radix sort groups the records by cell;
-//  4. one CTA per cell finishes an exact left-balanced k-d order of the cell's records in
-//     shared memory and pads the cell to whole 32-record leaves with dummy records (NaN
-//     position: never admitted by the gather, ignored by the box reductions).
-// Leaves therefore never straddle cells and are exact k-d leaves inside them.
-// ------------------------------------------------------------------------------------------
-__global__ void k_permute4(const float4* __restrict__ src, const uint32_t* __restrict__ perm,
-                           float4* __restrict__ dst, uint64_t n);
-
-constexpr int kCellMax = 4096;     // records per cell handled by one CTA
+constexpr int kCellMax = 4096;  // records of one node ordered by one CTA in shared memory
 constexpr int kCellThreads = 512;
 constexpr uint32_t kDummy = 0xffffffffu;
 
-__global__ void k_take_sample(const float4* __restrict__ a, uint64_t n, uint64_t stride, uint64_t S, float4* out) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < S; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t j = i * stride;
-        out[i] = a[j < n ? j : n - 1];
-    }
+static size_t cell_smem_bytes() {
+    return (size_t)kCellMax * 8 + (size_t)kCellMax * 16 + (size_t)2 * 3 * (kCellMax / 32) * 4;
 }
 
-// split planes of the top tree (heap order, node 1 = root) from the k-d ordered sample:
-// node j of level d covers sample positions [j*seg, (j+1)*seg), seg = S >> d; its plane is
-// the widest axis of the node's sample box at the coordinate of the element seg/2.
-// one CTA (256 threads) per node h = blockIdx.x + 1
-__global__ void __launch_bounds__(256) k_top_planes(const float4* __restrict__ s, uint64_t S, uint8_t* axis, float* value) {
-    __shared__ float red[6][8];
-    __shared__ int ax_s;
-    const uint64_t h = (uint64_t)blockIdx.x + 1;
-    const int d = 63 - __clzll((long long)h);
-    const uint64_t j = h - (1ull << d);
-    const uint64_t seg = S >> d;
-    const uint64_t b = j * seg, e = b + seg;
-    float v6[6] = {3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
-    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        float4 p = s[i];
-        v6[0] = fminf(v6[0], p.x); v6[3] = fmaxf(v6[3], p.x);
-        v6[1] = fminf(v6[1], p.y); v6[4] = fmaxf(v6[4], p.y);
-        v6[2] = fminf(v6[2], p.z); v6[5] = fmaxf(v6[5], p.z);
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        for (int o = 16; o > 0; o >>= 1) {
-            float x = __shfl_xor_sync(0xffffffffu, v6[k], o);
-            v6[k] = k < 3 ? fminf(v6[k], x) : fmaxf(v6[k], x);
-        }
-        if (l == 0) red[k][w] = v6[k];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r[6];
-        for (int k = 0; k < 6; ++k) {
-            r[k] = red[k][0];
-            for (int q = 1; q < 8; ++q) r[k] = k < 3 ? fminf(r[k], red[k][q]) : fmaxf(r[k], red[k][q]);
-        }
-        float e0 = r[3] - r[0], e1 = r[4] - r[1], e2 = r[5] - r[2];
-        ax_s = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2 ? 1 : 2);
-    }
-    __syncthreads();
-    // the sample inside the node is k-d ordered with its two halves as the children, so the
-    // plane is the largest coordinate of the left half on the node's axis
-    const int ax = ax_s;
-    float vmax = -3.4e38f;
-    for (uint64_t i = b + threadIdx.x; i < b + seg / 2; i += blockDim.x) {
-        float4 p = s[i];
-        vmax = fmaxf(vmax, ax == 0 ? p.x : (ax == 1 ? p.y : p.z));
-    }
-    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    __syncthreads();
-    if (l == 0) red[0][w] = vmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = red[0][0];
-        for (int q = 1; q < 8; ++q) r = fmaxf(r, red[0][q]);
-        axis[h] = (uint8_t)ax;
-        value[h] = r;
-    }
+struct CellSmem {
+    unsigned long long* key;  // kCellMax sort keys
+    float *X, *Y, *Z;         // kCellMax coordinates
+    uint32_t* ID;             // kCellMax record ids
+    unsigned *blo, *bhi;      // 3 * (kCellMax / 32) ordered-int node boxes
+};
+
+ALB_DEVICE CellSmem cell_smem(unsigned char* raw) {
+    CellSmem s;
+    s.key = (unsigned long long*)raw;
+    s.X = (float*)(s.key + kCellMax);
+    s.Y = s.X + kCellMax;
+    s.Z = s.Y + kCellMax;
+    s.ID = (uint32_t*)(s.Z + kCellMax);
+    s.blo = (unsigned*)(s.ID + kCellMax);
+    s.bhi = s.blo + 3 * (kCellMax / 32);
+    return s;
 }
 
-__global__ void k_assign_cells(const float4* __restrict__ a, uint64_t n, int T, const uint8_t* __restrict__ axis,
-                               const float* __restrict__ value, uint64_t* keys, uint32_t* vals, unsigned* counts) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        float4 p = a[i];
-        uint32_t h = 1;
-        for (int d = 0; d < T; ++d) {
-            int ax = axis[h];
-            float c = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
-            h = 2 * h + (c > value[h] ? 1u : 0u);
-        }
-        uint32_t cell = h - (1u << T);
-        keys[i] = cell;
-        vals[i] = (uint32_t)i;
-        atomicAdd(counts + cell, 1u);
-    }
-}
-
-__global__ void k_pad_counts(const unsigned* __restrict__ counts, uint32_t ncell, unsigned* padded, unsigned* maxc) {
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        unsigned k = counts[c];
-        padded[c] = (k + 31u) & ~31u;
-        atomicMax(maxc, k);
-    }
-}
-
-// exact left-balanced k-d order inside one cell; writes the padded permutation
-__global__ void __launch_bounds__(kCellThreads) k_cell_kd(const float4* __restrict__ a, const uint32_t* __restrict__ perm,
-                                                          const unsigned* __restrict__ start,
-                                                          const unsigned* __restrict__ count,
-                                                          const unsigned* __restrict__ pstart, uint32_t* out) {
-    extern __shared__ unsigned char smraw[];
-    unsigned long long* key = (unsigned long long*)smraw;        // kCellMax
-    float* X = (float*)(key + kCellMax);
-    float* Y = X + kCellMax;
-    float* Z = Y + kCellMax;
-    uint32_t* ID = (uint32_t*)(Z + kCellMax);
-    unsigned* blo = (unsigned*)(ID + kCellMax);                  // 3 * (kCellMax / 32)
-    unsigned* bhi = blo + 3 * (kCellMax / 32);
-    const uint32_t cell = blockIdx.x;
-    const unsigned cnt = count[cell];
-    if (cnt == 0) return;
+// Exact left-balanced k-d order of one node's records held in shared memory: entries
+// [0, cnt) are records, [cnt, P) (P = cnt rounded up to 32) dummies with NaN positions.
+// Reorders X/Y/Z/ID in place, level by level: node boxes -> key (node, 16-bit coordinate
+// on the node's widest axis, slot) -> bitonic sort -> permute. Dummies sort last inside
+// their node, so they stay in the last leaf. Called by every thread of the CTA.
+ALB_DEVICE void cell_kd_sort(const CellSmem& s, unsigned cnt) {
     const unsigned P = (cnt + 31u) & ~31u;
     const unsigned Lc = P / 32;
     unsigned P2 = 32;
     while (P2 < P) P2 <<= 1;
-    const unsigned s0 = start[cell];
-    const float qnan = __int_as_float(0x7fc00000);
-    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) {
-        if (j < cnt) {
-            uint32_t id = perm[s0 + j];
-            float4 p = a[id];
-            X[j] = p.x; Y[j] = p.y; Z[j] = p.z; ID[j] = id;
-        } else {
-            X[j] = qnan; Y[j] = qnan; Z[j] = qnan; ID[j] = kDummy;
-        }
-    }
-    __syncthreads();
     int depth = 0;
     while ((1u << depth) < Lc) ++depth;
     for (int d = 0; d < depth; ++d) {
         for (unsigned i = threadIdx.x; i < 3 * Lc; i += blockDim.x) {
-            blo[i] = 0xffffffffu;
-            bhi[i] = 0u;
+            s.blo[i] = 0xffffffffu;
+            s.bhi[i] = 0u;
         }
         __syncthreads();
         for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) {
             uint64_t na, nc;
             kd_node(j / 32, Lc, d, na, nc);
             if (nc > 1) {
-                atomicMin(blo + 3 * na, f2ord(X[j])); atomicMax(bhi + 3 * na, f2ord(X[j]));
-                atomicMin(blo + 3 * na + 1, f2ord(Y[j])); atomicMax(bhi + 3 * na + 1, f2ord(Y[j]));
-                atomicMin(blo + 3 * na + 2, f2ord(Z[j])); atomicMax(bhi + 3 * na + 2, f2ord(Z[j]));
+                atomicMin(s.blo + 3 * na, f2ord(s.X[j])); atomicMax(s.bhi + 3 * na, f2ord(s.X[j]));
+                atomicMin(s.blo + 3 * na + 1, f2ord(s.Y[j])); atomicMax(s.bhi + 3 * na + 1, f2ord(s.Y[j]));
+                atomicMin(s.blo + 3 * na + 2, f2ord(s.Z[j])); atomicMax(s.bhi + 3 * na + 2, f2ord(s.Z[j]));
             }
         }
         __syncthreads();
@@ -581,55 +373,88 @@ __global__ void __launch_bounds__(kCellThreads) k_cell_kd(const float4* __restri
                 kd_node(j / 32, Lc, d, na, nc);
                 uint64_t q = 0;
                 if (j >= cnt) {
-                    q = 0x1ffff;  // dummies sort last inside their node
+                    q = 0x1ffff;
                 } else if (nc > 1) {
-                    float l0 = ord2f(blo[3 * na]), l1 = ord2f(blo[3 * na + 1]), l2 = ord2f(blo[3 * na + 2]);
-                    float e0 = ord2f(bhi[3 * na]) - l0, e1 = ord2f(bhi[3 * na + 1]) - l1, e2 = ord2f(bhi[3 * na + 2]) - l2;
+                    const unsigned* lo = s.blo + 3 * na;
+                    const unsigned* hi = s.bhi + 3 * na;
+                    float l0 = ord2f(lo[0]), l1 = ord2f(lo[1]), l2 = ord2f(lo[2]);
+                    float e0 = ord2f(hi[0]) - l0, e1 = ord2f(hi[1]) - l1, e2 = ord2f(hi[2]) - l2;
                     float v, l, e;
-                    if (e0 >= e1 && e0 >= e2) { v = X[j]; l = l0; e = e0; }
-                    else if (e1 >= e2) { v = Y[j]; l = l1; e = e1; }
-                    else { v = Z[j]; l = l2; e = e2; }
+                    if (e0 >= e1 && e0 >= e2) { v = s.X[j]; l = l0; e = e0; }
+                    else if (e1 >= e2) { v = s.Y[j]; l = l1; e = e1; }
+                    else { v = s.Z[j]; l = l2; e = e2; }
                     if (e > 0.f) q = (uint64_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
                 }
                 k = (((na << 17) | q) << 13) | j;  // j < 8192 keeps equal keys in place
             }
-            key[j] = k;
+            s.key[j] = k;
         }
         __syncthreads();
-        // bitonic sort of P2 keys, ascending
-        for (unsigned kk = 2; kk <= P2; kk <<= 1) {
+        for (unsigned kk = 2; kk <= P2; kk <<= 1) {  // bitonic sort of P2 keys, ascending
             for (unsigned jj = kk >> 1; jj > 0; jj >>= 1) {
                 for (unsigned i = threadIdx.x; i < P2; i += blockDim.x) {
                     unsigned p = i ^ jj;
                     if (p > i) {
-                        unsigned long long x = key[i], y = key[p];
+                        unsigned long long x = s.key[i], y = s.key[p];
                         bool up = (i & kk) == 0;
                         if ((x > y) == up) {
-                            key[i] = y;
-                            key[p] = x;
+                            s.key[i] = y;
+                            s.key[p] = x;
                         }
                     }
                 }
                 __syncthreads();
             }
         }
-        // gather the records into the new order (each thread keeps its own in registers)
-        float rx[kCellMax / kCellThreads], ry[kCellMax / kCellThreads], rz[kCellMax / kCellThreads];
-        uint32_t rid[kCellMax / kCellThreads];
-        int t = 0;
-        for (unsigned j = threadIdx.x; j < P; j += blockDim.x, ++t) {
-            unsigned src = (unsigned)(key[j] & 0x1fffull);
-            rx[t] = X[src]; ry[t] = Y[src]; rz[t] = Z[src]; rid[t] = ID[src];
+        constexpr int R = kCellMax / kCellThreads;  // each thread stages its slots in registers
+        float rx[R], ry[R], rz[R];
+        uint32_t rid[R];
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+            unsigned j = threadIdx.x + t * kCellThreads;
+            if (j < P) {
+                unsigned src = (unsigned)(s.key[j] & 0x1fffull);
+                rx[t] = s.X[src]; ry[t] = s.Y[src]; rz[t] = s.Z[src]; rid[t] = s.ID[src];
+            }
         }
         __syncthreads();
-        t = 0;
-        for (unsigned j = threadIdx.x; j < P; j += blockDim.x, ++t) {
-            X[j] = rx[t]; Y[j] = ry[t]; Z[j] = rz[t]; ID[j] = rid[t];
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+            unsigned j = threadIdx.x + t * kCellThreads;
+            if (j < P) {
+                s.X[j] = rx[t]; s.Y[j] = ry[t]; s.Z[j] = rz[t]; s.ID[j] = rid[t];
+            }
         }
         __syncthreads();
     }
-    const unsigned o = pstart[cell];
-    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) out[o + j] = ID[j];
+}
+
+// One cell of records a[perm[start + j]], j < count (<= kCellMax): writes its padded k-d
+// order (kDummy for padding) to out[pstart ..]. Used by the allocation-free k-NN index.
+__global__ void __launch_bounds__(kCellThreads) k_cell_kd(const float4* __restrict__ a, const uint32_t* __restrict__ perm,
+                                                          const unsigned* __restrict__ start,
+                                                          const unsigned* __restrict__ count,
+                                                          const unsigned* __restrict__ pstart, uint32_t* out) {
+    extern __shared__ unsigned char smraw[];
+    const CellSmem s = cell_smem(smraw);
+    const unsigned cnt = count[blockIdx.x];
+    if (cnt == 0 || cnt > (unsigned)kCellMax) return;
+    const unsigned P = (cnt + 31u) & ~31u;
+    const unsigned s0 = start[blockIdx.x];
+    const float qnan = __int_as_float(0x7fc00000);
+    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) {
+        if (j < cnt) {
+            uint32_t id = perm[s0 + j];
+            float4 p = a[id];
+            s.X[j] = p.x; s.Y[j] = p.y; s.Z[j] = p.z; s.ID[j] = id;
+        } else {
+            s.X[j] = qnan; s.Y[j] = qnan; s.Z[j] = qnan; s.ID[j] = kDummy;
+        }
+    }
+    __syncthreads();
+    cell_kd_sort(s, cnt);
+    const unsigned o = pstart[blockIdx.x];
+    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) out[o + j] = s.ID[j];
 }
 
 // records in the padded k-d order; dummies get a NaN position (their w lane keeps the tag)
@@ -650,108 +475,422 @@ __global__ void k_permute_u32_pad(const uint32_t* __restrict__ src, const uint32
     }
 }
 
-static size_t cell_smem_bytes() {
-    return (size_t)kCellMax * 8 + (size_t)kCellMax * 16 + (size_t)2 * 3 * (kCellMax / 32) * 4;
+// ------------------------------------------------------------------------------------------
+// Exact left-balanced k-d order by streaming partitions (the photon-map build).
+// Global levels 0..D-1 (nodes larger than one CTA's cell) each take three passes over
+// X = float4(x, y, z, record id) in position order:
+//   hist1: per node, 256-bin histogram of the top byte of a 16-bit coordinate quantised
+//          on the node's widest axis;
+//   hist2: per node, 256-bin histogram of the low byte inside the bucket that holds the
+//          cut (the node's left child takes exactly its power-of-two leaf count);
+//   split: every record goes left or right of that cut (ties at the 16-bit cut resolved
+//          by an atomic ticket), with warp-aggregated cursors, into X2; the children's
+//          boxes are reduced on the way for the next level's axis choice.
+// The remaining levels (nodes of <= kCellMax records) run in one CTA per node in shared
+// memory (k_local_kd). The result is the same tree shape as kd_order, with the cut placed
+// at 16-bit resolution.
+// ------------------------------------------------------------------------------------------
+
+// (start leaf a, leaf count c, path bits) of the depth-d node holding `leaf`
+ALB_DEVICE void kd_node_path(uint64_t leaf, uint64_t L, int depth, uint64_t& a, uint64_t& c, uint32_t& path,
+                             int& reached) {
+    a = 0;
+    c = L;
+    path = 0;
+    reached = 0;
+    for (int i = 0; i < depth && c > 1; ++i) {
+        uint64_t left = 1ull << (63 - __clzll((long long)(c - 1)));
+        if (leaf - a < left) {
+            c = left;
+            path = path << 1;
+        } else {
+            a += left;
+            c -= left;
+            path = (path << 1) | 1u;
+        }
+        ++reached;
+    }
 }
 
-// perm_out (capacity >= padded count) <- padded k-d order; returns the padded count or 0 on
-// failure (cells too large after retries)
-static uint64_t sampled_kd_order(Workspace& ws, const float4* a, uint64_t n, uint32_t* perm_out, uint64_t perm_cap,
-                                 cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_cell_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
-        attr_set = true;
+// node of the depth-d path: start leaf a and leaf count c (c == 0 if the path ends early)
+ALB_DEVICE void kd_node_of_path(uint32_t path, uint64_t L, int depth, uint64_t& a, uint64_t& c) {
+    a = 0;
+    c = L;
+    for (int i = depth - 1; i >= 0; --i) {
+        if (c <= 1) {
+            c = 0;
+            return;
+        }
+        uint64_t left = 1ull << (63 - __clzll((long long)(c - 1)));
+        if ((path >> i) & 1u) {
+            a += left;
+            c -= left;
+        } else {
+            c = left;
+        }
     }
-    int T = 0;
-    while ((n >> T) > (uint64_t)(kCellMax / 3)) ++T;
-    for (int attempt = 0; attempt < 4; ++attempt, ++T) {
-        size_t mark = ws.mark();
-        const uint32_t ncell = 1u << T;
-        uint8_t* axis = (uint8_t*)ws.take_bytes((uint64_t)ncell + 1);
-        float* value = (float*)ws.take_bytes(((uint64_t)ncell + 1) * 4);
-        if (T > 0) {
-            uint64_t S = std::min<uint64_t>((uint64_t)ncell * 32, n);
-            S = 1ull << (63 - __builtin_clzll(S));  // power of two
-            if (S < ((uint64_t)ncell << 1)) S = (uint64_t)ncell << 1;
-            uint64_t stride = std::max<uint64_t>(n / S, 1);
-            float4* smp = (float4*)ws.take_bytes(S * 16);
-            float4* smp2 = (float4*)ws.take_bytes(S * 16);
-            uint32_t* sp = ws.take_u32(S);
-            uint32_t* sp2 = ws.take_u32(S);
-            unsigned blocks = (unsigned)std::min<uint64_t>((S + 255) / 256, 8192);
-            k_take_sample<<<blocks, 256, 0, st>>>(a, n, stride, S, smp);
-            note_launch();
-            // k-d order of the sample with the level-synchronous builder: 32-record
-            // leaves, so levels above 5 split the sample in power-of-two halves
-            kd_order(ws, smp, S, sp, sp2, st);
-            k_permute4<<<blocks, 256, 0, st>>>(smp, sp, smp2, S);
-            note_launch();
-            k_top_planes<<<ncell - 1, 256, 0, st>>>(smp2, S, axis, value);
-            note_launch();
+}
+
+struct LevelNodes {
+    const unsigned* lo;  // [nodes][3] ordered-int box of this level
+    const unsigned* hi;
+};
+
+ALB_DEVICE uint32_t kd_quant16(float4 p, const unsigned* lo, const unsigned* hi, uint32_t path) {
+    float l0 = ord2f(lo[3 * path]), l1 = ord2f(lo[3 * path + 1]), l2 = ord2f(lo[3 * path + 2]);
+    float e0 = ord2f(hi[3 * path]) - l0, e1 = ord2f(hi[3 * path + 1]) - l1, e2 = ord2f(hi[3 * path + 2]) - l2;
+    float v, l, e;
+    if (e0 >= e1 && e0 >= e2) { v = p.x; l = l0; e = e0; }
+    else if (e1 >= e2) { v = p.y; l = l1; e = e1; }
+    else { v = p.z; l = l2; e = e2; }
+    if (!(e > 0.f)) return 0u;
+    return (uint32_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
+}
+
+// warp-aggregated atomicAdd of 1 on cnt[key]; returns this lane's ticket
+ALB_DEVICE unsigned agg_inc(unsigned* cnt, uint64_t key, unsigned active) {
+    unsigned peers = __match_any_sync(active, key);
+    int leader = __ffs(peers) - 1;
+    unsigned rank = __popc(peers & lanemask_lt());
+    unsigned base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(cnt, (unsigned)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + rank;
+}
+
+__global__ void k_kdl_hist1(const float4* __restrict__ X, uint64_t n, uint64_t L, int d, LevelNodes nb, unsigned* hist1) {
+    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+         base += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = base + lane_id();
+        bool act = false;
+        uint32_t path = 0, h = 0;
+        if (i < n) {
+            uint64_t a, c;
+            int r;
+            kd_node_path(i / 32, L, d, a, c, path, r);
+            if (r == d && c > 1) {
+                act = true;
+                h = kd_quant16(X[i], nb.lo, nb.hi, path) >> 8;
+            }
         }
-        unsigned* counts = ws.take_u32(ncell);
-        unsigned* padded = ws.take_u32(ncell);
-        unsigned* starts = ws.take_u32(ncell);
-        unsigned* pstarts = ws.take_u32(ncell);
-        uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
-        uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
-        uint32_t* vals = ws.take_u32(n);
-        uint32_t* vals2 = ws.take_u32(n);
-        unsigned* maxc = ws.scratch_box();
-        cudaMemsetAsync(counts, 0, (size_t)ncell * 4, st);
-        cudaMemsetAsync(maxc, 0, 4, st);
-        unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
-        k_assign_cells<<<blocks, 256, 0, st>>>(a, n, T, axis, value, keys, vals, counts);
-        note_launch();
-        k_pad_counts<<<(ncell + 255) / 256, 256, 0, st>>>(counts, ncell, padded, maxc);
-        note_launch();
-        unsigned hmax = 0;
-        cudaMemcpyAsync(&hmax, maxc, 4, cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        if (hmax > (unsigned)kCellMax) {  // unlucky sample: more cells
-            ws.release(mark);
-            continue;
+        unsigned am = __ballot_sync(0xffffffffu, act);
+        if (act) agg_inc(hist1 + (uint64_t)path * 256 + h, (uint64_t)path * 256 + h, am);
+    }
+}
+
+// one warp per node: locate the bucket of the cut; sel[node] = {bucket, need inside it}
+__global__ void k_kdl_select1(const unsigned* __restrict__ hist1, uint64_t L, int d, uint32_t nodes, uint2* sel) {
+    uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int l = lane_id();
+    if (w >= nodes) return;
+    uint64_t a, c;
+    kd_node_of_path(w, L, d, a, c);
+    if (c <= 1) {
+        if (l == 0) sel[w] = make_uint2(0xffffffffu, 0u);
+        return;
+    }
+    uint64_t left = 1ull << (63 - __clzll((long long)(c - 1)));
+    unsigned need = (unsigned)(left * 32);
+    const unsigned* h = hist1 + (uint64_t)w * 256;
+    unsigned v[8], run = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        v[j] = h[l * 8 + j];
+        run += v[j];
+    }
+    unsigned incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (l >= o) incl += t;
+    }
+    unsigned before = incl - run;
+    int bucket = -1;
+    unsigned below = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (bucket < 0 && before < need && before + v[j] >= need) {
+            bucket = l * 8 + j;
+            below = before;
         }
-        cudaMemcpyAsync(starts, counts, (size_t)ncell * 4, cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(pstarts, padded, (size_t)ncell * 4, cudaMemcpyDeviceToDevice, st);
-        exclusive_scan(ws, starts, ncell, st);
-        exclusive_scan(ws, pstarts, ncell, st);
-        unsigned last_ps = 0, last_pad = 0;
-        cudaMemcpyAsync(&last_ps, pstarts + ncell - 1, 4, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(&last_pad, padded + ncell - 1, 4, cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        uint64_t total = (uint64_t)last_ps + last_pad;
-        if (total > perm_cap) {
-            ws.release(mark);
-            return 0;
+        before += v[j];
+    }
+    // the node holds need + (right child's records) > need records, so one lane finds it
+    unsigned who = __ballot_sync(0xffffffffu, bucket >= 0);
+    int src = who ? __ffs(who) - 1 : 0;
+    bucket = __shfl_sync(0xffffffffu, bucket, src);
+    below = __shfl_sync(0xffffffffu, below, src);
+    if (l == 0) sel[w] = make_uint2((unsigned)bucket, need - below);
+}
+
+__global__ void k_kdl_hist2(const float4* __restrict__ X, uint64_t n, uint64_t L, int d, LevelNodes nb,
+                            const uint2* __restrict__ sel, unsigned* hist2) {
+    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+         base += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = base + lane_id();
+        bool act = false;
+        uint32_t path = 0, h = 0;
+        if (i < n) {
+            uint64_t a, c;
+            int r;
+            kd_node_path(i / 32, L, d, a, c, path, r);
+            if (r == d && c > 1) {
+                uint32_t q = kd_quant16(X[i], nb.lo, nb.hi, path);
+                if ((q >> 8) == sel[path].x) {
+                    act = true;
+                    h = q & 255u;
+                }
+            }
         }
-        if (T > 0) radix_sort_pairs(ws, keys, vals, keys2, vals2, n, (uint64_t)ncell - 1, st);
-        k_cell_kd<<<ncell, kCellThreads, cell_smem_bytes(), st>>>(a, vals, starts, counts, pstarts, perm_out);
-        note_launch();
+        unsigned am = __ballot_sync(0xffffffffu, act);
+        if (act) agg_inc(hist2 + (uint64_t)path * 256 + h, (uint64_t)path * 256 + h, am);
+    }
+}
+
+// one warp per node: the 16-bit cut value and how many records AT it go left
+__global__ void k_kdl_select2(const unsigned* __restrict__ hist2, uint32_t nodes, const uint2* __restrict__ sel,
+                              uint2* cut) {
+    uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int l = lane_id();
+    if (w >= nodes) return;
+    uint2 s = sel[w];
+    if (s.x >= 256u) {  // not an internal node of this level
+        if (l == 0) cut[w] = make_uint2(0xffffffffu, 0u);
+        return;
+    }
+    unsigned need = s.y;
+    const unsigned* h = hist2 + (uint64_t)w * 256;
+    unsigned v[8], run = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        v[j] = h[l * 8 + j];
+        run += v[j];
+    }
+    unsigned incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (l >= o) incl += t;
+    }
+    unsigned before = incl - run;
+    int sub = -1;
+    unsigned below = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (sub < 0 && before < need && before + v[j] >= need) {
+            sub = l * 8 + j;
+            below = before;
+        }
+        before += v[j];
+    }
+    unsigned who = __ballot_sync(0xffffffffu, sub >= 0);
+    int src = who ? __ffs(who) - 1 : 0;
+    sub = __shfl_sync(0xffffffffu, sub, src);
+    below = __shfl_sync(0xffffffffu, below, src);
+    // records with q16 < cutv go left, records with q16 == cutv: the first `ties` go left
+    if (l == 0) cut[w] = make_uint2((s.x << 8) | (unsigned)(sub < 0 ? 0 : sub), need - below);
+}
+
+__global__ void k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2, uint64_t n, uint64_t L, int d,
+                            LevelNodes nb, const uint2* __restrict__ cut, unsigned* cursors, unsigned* ties,
+                            unsigned* clo, unsigned* chi, unsigned* err) {
+    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+         base += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = base + lane_id();
+        bool valid = i < n;
+        bool moves = false;
+        uint32_t path = 0;
+        uint64_t a = 0, c = 0, left = 0;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        unsigned side = 0;
+        if (valid) {
+            int r;
+            kd_node_path(i / 32, L, d, a, c, path, r);
+            p = X[i];
+            if (r == d && c > 1) {
+                moves = true;
+                left = 1ull << (63 - __clzll((long long)(c - 1)));
+                uint2 ct = cut[path];
+                uint32_t q = kd_quant16(p, nb.lo, nb.hi, path);
+                if (q < ct.x) side = 0;
+                else if (q > ct.x) side = 1;
+                else side = (atomicAdd(ties + path, 1u) < ct.y) ? 0u : 1u;
+            } else {
+                X2[i] = p;  // already a leaf: stays
+            }
+        }
+        unsigned am = __ballot_sync(0xffffffffu, moves);
+        if (moves) {
+            unsigned t = agg_inc(cursors + 2 * (uint64_t)path + side, 2 * (uint64_t)path + side, am);
+            uint64_t dst = a * 32 + (side ? left * 32 : 0) + t;
+            uint64_t end = side ? min((a + c) * 32, n) : (a + left) * 32;
+            if (dst < end) X2[dst] = p;
+            else atomicOr(err, 1u);  // a cut that does not fill the left child exactly
+            // child box for the next level (warp-reduced per child)
+            uint32_t child = (path << 1) | side;
+            unsigned peers = __match_any_sync(am, child);
+            unsigned ox = f2ord(p.x), oy = f2ord(p.y), oz = f2ord(p.z);
+            unsigned mnx = __reduce_min_sync(peers, ox), mny = __reduce_min_sync(peers, oy), mnz = __reduce_min_sync(peers, oz);
+            unsigned mxx = __reduce_max_sync(peers, ox), mxy = __reduce_max_sync(peers, oy), mxz = __reduce_max_sync(peers, oz);
+            if ((int)lane_id() == __ffs(peers) - 1) {
+                atomicMin(clo + 3 * child, mnx); atomicMin(clo + 3 * child + 1, mny); atomicMin(clo + 3 * child + 2, mnz);
+                atomicMax(chi + 3 * child, mxx); atomicMax(chi + 3 * child + 1, mxy); atomicMax(chi + 3 * child + 2, mxz);
+            }
+        }
+    }
+}
+
+// One node of <= kCellMax records X[start + j] (id in .w) per CTA: writes the record ids
+// of its exact left-balanced k-d order to out[start ..].
+__global__ void __launch_bounds__(kCellThreads) k_local_kd(const float4* __restrict__ Xin,
+                                                           const unsigned* __restrict__ cstart,
+                                                           const unsigned* __restrict__ ccount, uint32_t* out,
+                                                           unsigned* err) {
+    extern __shared__ unsigned char smraw[];
+    const CellSmem s = cell_smem(smraw);
+    const unsigned cnt = ccount[blockIdx.x];
+    const unsigned s0 = cstart[blockIdx.x];
+    if (cnt == 0) return;
+    if (cnt > (unsigned)kCellMax) {
+        if (threadIdx.x == 0) atomicOr(err, 2u);
+        return;
+    }
+    const unsigned P = (cnt + 31u) & ~31u;
+    const float qnan = __int_as_float(0x7fc00000);
+    for (unsigned j = threadIdx.x; j < P; j += blockDim.x) {
+        if (j < cnt) {
+            float4 p = Xin[s0 + j];
+            s.X[j] = p.x; s.Y[j] = p.y; s.Z[j] = p.z; s.ID[j] = __float_as_uint(p.w);
+        } else {
+            s.X[j] = qnan; s.Y[j] = qnan; s.Z[j] = qnan; s.ID[j] = kDummy;
+        }
+    }
+    __syncthreads();
+    cell_kd_sort(s, cnt);
+    for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) out[s0 + j] = s.ID[j];
+}
+
+__global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float4 p = a[i];
+        X[i] = make_float4(p.x, p.y, p.z, __uint_as_float((uint32_t)i));
+    }
+}
+
+static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n, std::vector<unsigned>& st,
+                            std::vector<unsigned>& ct) {
+    if (depth == D || c <= 1) {
+        uint64_t s = a * 32, e = std::min<uint64_t>((a + c) * 32, n);
+        if (e > s) {
+            st.push_back((unsigned)s);
+            ct.push_back((unsigned)(e - s));
+        }
+        return;
+    }
+    uint64_t left = 1ull << (63 - __builtin_clzll((unsigned long long)(c - 1)));
+    enumerate_cells(a, left, depth + 1, D, n, st, ct);
+    enumerate_cells(a + left, c - left, depth + 1, D, n, st, ct);
+}
+
+// perm <- exact left-balanced k-d order (record ids) of the n records of `a`
+static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float blo[3], const float bhi[3],
+                         uint32_t* perm, cudaStream_t st) {
+    const uint64_t L = (n + 31) / 32;
+    int depth_max = L > 1 ? 64 - __builtin_clzll((unsigned long long)(L - 1)) : 0;
+    const int local_levels = 7;  // kCellMax / 32 = 128 leaves = 2^7
+    const int D = std::max(0, depth_max - local_levels);
+    size_t mark = ws.mark();
+    float4* X = (float4*)ws.take_bytes(n * 16);
+    float4* X2 = (float4*)ws.take_bytes(n * 16);
+    unsigned* err = ws.take_u32(1);
+    if (!X || !X2 || !err) {
         ws.release(mark);
-        return total;
+        return -1;
     }
-    return 0;
+    cudaMemsetAsync(err, 0, 4, st);
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
+    k_pack_ids<<<blocks, 256, 0, st>>>(a, n, X);
+    note_launch();
+    if (D > 0) {
+        const uint64_t maxnodes = 1ull << D;
+        unsigned* hist1 = ws.take_u32(maxnodes * 256);
+        unsigned* hist2 = ws.take_u32(maxnodes * 256);
+        uint2* sel = (uint2*)ws.take_bytes(maxnodes * 8);
+        uint2* cut = (uint2*)ws.take_bytes(maxnodes * 8);
+        unsigned* cursors = ws.take_u32(maxnodes * 2);
+        unsigned* ties = ws.take_u32(maxnodes);
+        unsigned* lo = ws.take_u32(maxnodes * 6);  // current level boxes
+        unsigned* hi = ws.take_u32(maxnodes * 6);
+        unsigned* clo = ws.take_u32(maxnodes * 6);  // children boxes
+        unsigned* chi = ws.take_u32(maxnodes * 6);
+        if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi) {
+            ws.release(mark);
+            return -1;
+        }
+        // level 0 box: the records' bounding box
+        unsigned h6[6];
+        for (int k = 0; k < 3; ++k) {
+            uint32_t u;
+            memcpy(&u, &blo[k], 4);
+            h6[k] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+            memcpy(&u, &bhi[k], 4);
+            h6[3 + k] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        }
+        unsigned init_lo[3] = {h6[0], h6[1], h6[2]}, init_hi[3] = {h6[3], h6[4], h6[5]};
+        cudaMemcpyAsync(lo, init_lo, 12, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(hi, init_hi, 12, cudaMemcpyHostToDevice, st);
+        for (int d = 0; d < D; ++d) {
+            const uint32_t nodes = 1u << d;
+            cudaMemsetAsync(hist1, 0, (size_t)nodes * 256 * 4, st);
+            cudaMemsetAsync(hist2, 0, (size_t)nodes * 256 * 4, st);
+            cudaMemsetAsync(cursors, 0, (size_t)nodes * 8, st);
+            cudaMemsetAsync(ties, 0, (size_t)nodes * 4, st);
+            cudaMemsetAsync(clo, 0xff, (size_t)nodes * 2 * 12, st);
+            cudaMemsetAsync(chi, 0x00, (size_t)nodes * 2 * 12, st);
+            LevelNodes nb{lo, hi};
+            k_kdl_hist1<<<blocks, 256, 0, st>>>(X, n, L, d, nb, hist1);
+            note_launch();
+            k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
+            note_launch();
+            k_kdl_hist2<<<blocks, 256, 0, st>>>(X, n, L, d, nb, sel, hist2);
+            note_launch();
+            k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
+            note_launch();
+            k_kdl_split<<<blocks, 256, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, clo, chi, err);
+            note_launch();
+            std::swap(X, X2);
+            std::swap(lo, clo);
+            std::swap(hi, chi);
+        }
+    }
+    // local levels: one CTA per remaining node
+    std::vector<unsigned> cs, cc;
+    enumerate_cells(0, L, 0, D, n, cs, cc);
+    unsigned* dcs = ws.take_u32(cs.size());
+    unsigned* dcc = ws.take_u32(cc.size());
+    if (!dcs || !dcc) {
+        ws.release(mark);
+        return -1;
+    }
+    cudaMemcpyAsync(dcs, cs.data(), cs.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dcc, cc.data(), cc.size() * 4, cudaMemcpyHostToDevice, st);
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        cudaFuncSetAttribute(k_local_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
+        attr_set[dev] = true;
+    }
+    k_local_kd<<<(unsigned)cs.size(), kCellThreads, cell_smem_bytes(), st>>>(X, dcs, dcc, perm, err);
+    note_launch();
+    unsigned herr = 0;
+    cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);  // also keeps the host vectors cs/cc alive for their copies
+    ws.release(mark);
+    return herr ? -1 : 0;
 }
 
 // ------------------------------------------------------------------------------------------
 // permutation and box tree
 // ------------------------------------------------------------------------------------------
-
-__global__ void k_permute4(const float4* __restrict__ src, const uint32_t* __restrict__ perm,
-                           float4* __restrict__ dst, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        dst[i] = src[perm[i]];
-}
-
-__global__ void k_permute_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ perm,
-                              uint32_t* __restrict__ dst, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        dst[i] = src[perm[i]];
-}
 
 // One warp per leaf: box of 32 consecutive sorted records.
 __global__ void k_leaf_boxes(const float4* __restrict__ a, uint64_t n, float4* lo, float4* hi, uint64_t nleaf) {
@@ -899,8 +1038,10 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     m.grid = make_key_grid(lo, hi);
     size_t mark = ws.mark();
     uint32_t* vals = ws.take_u32(n);
-    uint32_t* vals2 = ws.take_u32(n);
-    kd_order(ws, rec.a, n, vals, vals2, st);
+    if (!vals || kd_order_fast(ws, rec.a, n, lo, hi, vals, st) != 0) {
+        ws.release(mark);
+        return -1;
+    }
     const uint64_t np = n;
     m.n_real = n;
     m.n = np;
