@@ -10,6 +10,11 @@
 // of 2^-18 so that every point whose float64 distance could rank at the k-th place
 // survives, and the boundary band is resolved with float64 distances exactly as the
 // reference's KDTree (float64 on float32-cast map positions) orders them.
+//
+// Each warp takes contiguous chunks of the spatially sorted queries; from the second query
+// of a chunk on, the search starts with the threshold (r_k(prev) + |q - prev|)^2 (triangle
+// inequality: the previous query's k neighbours all lie within it), inflated by 2^-14 so
+// that every point of the float32 boundary band is still admitted.
 #include <cfloat>
 
 #include "device_common.cuh"
@@ -18,6 +23,7 @@
 namespace alb {
 
 constexpr int kGatherWarps = 4;
+constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one warp
 constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;        // candidate buffer; shrunk when more than kCap-32 are held
 constexpr float kRelMargin = 3.814697265625e-06f;  // 2^-18
@@ -159,87 +165,122 @@ struct KnnResult {
 };
 
 // Full k-NN search for one query. Returns false when the map has fewer than k records.
+// thr0: an upper bound of the squared k-th distance that already includes the band margin
+// (FLT_MAX when none is known).
 ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz,
-                         KnnResult& res) {
+                         float thr0, KnnResult& res) {
     const int l = lane_id();
     const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
     const float lx = (float)(qx - (double)fx), ly = (float)(qy - (double)fy), lz = (float)(qz - (double)fz);
     if (m.n_real < (uint64_t)k) return false;
-    float thr = FLT_MAX;  // admission threshold (float32 squared distance, with margin)
+    float thr = thr0;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
-    int sp = 0;
-    // roots
-    {
-        int top = m.nlevels - 1;
-        uint64_t ntop = m.lvl_cnt[top];
-        float d = FLT_MAX;
-        uint32_t c = (uint32_t)l;
-        if ((uint64_t)l < ntop) d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[top] + l], m.box_hi[m.lvl_off[top] + l]);
-        warp_sort32(d, c);
-        unsigned b = __ballot_sync(0xffffffffu, d < FLT_MAX);
-        int nv = __popc(b);
-        if (l < nv) {
-            s.stk[sp + nv - 1 - l] = ((uint32_t)top << 29) | c;
-            s.stk_d[sp + nv - 1 - l] = d;
-        }
-        sp += nv;
-        __syncwarp();
-    }
-    int guard = 0;
     res.leaves = res.nodes = res.selects = 0;
-    while (sp > 0) {
-        if (++guard > (1 << 22)) break;
-        --sp;
-        uint32_t e = s.stk[sp];
-        float ed = s.stk_d[sp];
-        __syncwarp();
-        if (ed > thr) continue;
-        int lev = (int)(e >> 29);
-        uint32_t node = e & 0x1fffffffu;
-        if (lev == 0) {
-            ++res.leaves;
-            uint64_t i = (uint64_t)node * 32 + l;
+    // A carried bound can only fail through a degenerate previous result (a clipped
+    // boundary band); the search is then repeated without it.
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        thr = attempt ? FLT_MAX : thr0;
+        cnt = 0;
+        int sp = 0;
+        // roots
+        {
+            int top = m.nlevels - 1;
+            uint64_t ntop = m.lvl_cnt[top];
             float d = FLT_MAX;
-            if (i < m.n) d = point_dist2(fx, fy, fz, lx, ly, lz, m.a[i]);
-            bool take = d <= thr;
-            unsigned b = __ballot_sync(0xffffffffu, take);
-            if (take) {
-                int pos = cnt + __popc(b & lanemask_lt());
-                s.cd[pos] = d;
-                s.ci[pos] = (uint32_t)i;
-            }
-            cnt += __popc(b);
-            __syncwarp();
-            if (cnt >= k && (thr == FLT_MAX || cnt > kCap - 32)) {
-                ++res.selects;
-                float kth = warp_kth(s, cnt, k);
-                thr = kth * (1.0f + 2.0f * kRelMargin);
-                cnt = warp_compact(s, cnt, thr);
-                if (cnt > kCap - 32) {  // pathological ties: fall back to the bare threshold
-                    thr = kth;
-                    cnt = warp_compact(s, cnt, thr);
-                }
-            }
-        } else {
-            ++res.nodes;
-            uint64_t c = (uint64_t)node * 32 + l;
-            float d = FLT_MAX;
-            int cl = lev - 1;
-            if (c < m.lvl_cnt[cl]) {
-                d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[cl] + c], m.box_hi[m.lvl_off[cl] + c]);
+            uint32_t c = (uint32_t)l;
+            if ((uint64_t)l < ntop) {
+                d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[top] + l], m.box_hi[m.lvl_off[top] + l]);
                 if (d > thr) d = FLT_MAX;
             }
-            uint32_t cc = (uint32_t)c;
-            warp_sort32(d, cc);
+            warp_sort32(d, c);
             unsigned b = __ballot_sync(0xffffffffu, d < FLT_MAX);
             int nv = __popc(b);
             if (l < nv) {
-                s.stk[sp + nv - 1 - l] = ((uint32_t)cl << 29) | cc;
+                s.stk[sp + nv - 1 - l] = ((uint32_t)top << 29) | c;
                 s.stk_d[sp + nv - 1 - l] = d;
             }
             sp += nv;
             __syncwarp();
         }
+        int guard = 0;
+        while (sp > 0) {
+            if (++guard > (1 << 22)) break;
+            // skip entries beyond the threshold, 32 at a time
+            {
+                int i = sp - 1 - l;
+                unsigned ok = __ballot_sync(0xffffffffu, i >= 0 && s.stk_d[i] <= thr);
+                if (!ok) {
+                    sp = sp > 32 ? sp - 32 : 0;
+                    __syncwarp();
+                    continue;
+                }
+                sp -= __ffs(ok) - 1;
+            }
+            --sp;
+            uint32_t e = s.stk[sp];
+            __syncwarp();
+            int lev = (int)(e >> 29);
+            uint32_t node = e & 0x1fffffffu;
+            if (lev == 0) {
+                ++res.leaves;
+                uint64_t i = (uint64_t)node * 32 + l;
+                float d = FLT_MAX;
+                if (i < m.n) d = point_dist2(fx, fy, fz, lx, ly, lz, m.a[i]);
+                bool take = d <= thr;
+                unsigned b = __ballot_sync(0xffffffffu, take);
+                if (take) {
+                    int pos = cnt + __popc(b & lanemask_lt());
+                    s.cd[pos] = d;
+                    s.ci[pos] = (uint32_t)i;
+                }
+                cnt += __popc(b);
+                __syncwarp();
+                if (cnt >= k && (thr == FLT_MAX || cnt > kCap - 32)) {
+                    ++res.selects;
+                    float kth = warp_kth(s, cnt, k);
+                    thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
+                    cnt = warp_compact(s, cnt, thr);
+                    if (cnt > kCap - 32) {  // pathological ties: fall back to the bare threshold
+                        thr = kth;
+                        cnt = warp_compact(s, cnt, thr);
+                    }
+                }
+            } else {
+                ++res.nodes;
+                uint64_t c = (uint64_t)node * 32 + l;
+                float d = FLT_MAX;
+                int cl = lev - 1;
+                if (c < m.lvl_cnt[cl]) {
+                    d = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[cl] + c], m.box_hi[m.lvl_off[cl] + c]);
+                    if (d > thr) d = FLT_MAX;
+                }
+                uint32_t cc = (uint32_t)c;
+                int nv = __popc(__ballot_sync(0xffffffffu, d < FLT_MAX));
+                if (nv <= 8) {
+                    // few children within the threshold: extract them nearest first
+                    // (non-negative floats order like their bit patterns)
+                    unsigned key = __float_as_uint(d);
+                    for (int r = 0; r < nv; ++r) {
+                        unsigned mn = __reduce_min_sync(0xffffffffu, key);
+                        int src = __ffs(__ballot_sync(0xffffffffu, key == mn)) - 1;
+                        if (l == src) {
+                            s.stk[sp + nv - 1 - r] = ((uint32_t)cl << 29) | cc;
+                            s.stk_d[sp + nv - 1 - r] = d;
+                            key = 0xffffffffu;
+                        }
+                    }
+                } else {
+                    warp_sort32(d, cc);
+                    if (l < nv) {
+                        s.stk[sp + nv - 1 - l] = ((uint32_t)cl << 29) | cc;
+                        s.stk_d[sp + nv - 1 - l] = d;
+                    }
+                }
+                sp += nv;
+                __syncwarp();
+            }
+        }
+        if (cnt >= k || thr0 == FLT_MAX) break;
     }
     // final: exact k with the float64 boundary band
     float kth = warp_kth(s, cnt, k);
@@ -427,68 +468,86 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
     const int w = threadIdx.x >> 5, l = lane_id();
     WarpSmem& s = smem[w];
     const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
-    for (uint64_t qi = (uint64_t)blockIdx.x * kGatherWarps + w; qi < q.n; qi += warps) {
-        uint64_t src = q.perm ? q.perm[qi] : qi;
-        float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
-        double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
-        KnnResult r;
-        if (!warp_knn(m, s, k, qx, qy, qz, r)) {
-            if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
-            break;
-        }
-        if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
-        if (q.stats && l == 0) {
-            atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
-            atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
-            atomicAdd(q.stats + 2, (unsigned long long)r.selects);
-            atomicAdd(q.stats + 3, 1ull);
-        }
-        const float Es = qa.w, ts = qb.w;
-        const float rk = (float)r.rk;
-        float norm;
-        if (CHANNEL == ALB_SCATTER) norm = 1.0f / ((4.0f / 3.0f) * 3.14159265358979f * rk * rk * rk);
-        else norm = 1.0f / (3.14159265358979f * rk * rk);
-        // query-constant pieces
-        float vinv = rsqrtf(fmaf(qb.x, qb.x, fmaf(qb.y, qb.y, qb.z * qb.z)));
-        float vx = -qb.x * vinv, vy = -qb.y * vinv, vz = -qb.z * vinv;  // normalize(-d_query)
-        float wconst = 0.f;
-        if (CHANNEL == ALB_BOTTOM_REFLECTION) wconst = (float)(sc.floor_albedo / kPi) * fmaxf(0.f, -qb.y);
-        if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
-        // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
-        const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
-        for (int j = l; j < k; j += 32) {
-            uint32_t idx = knn_index(s, r, j);
-            float4 pa = m.a[idx], pb = m.b[idx];
-            float w;
-            if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
-            else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
-            else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
-            float c = ((Es * pa.w) * norm) * w;
-            int bin = (int)((ts + pb.w) / (float)sc.mult);
-            if (bin >= 0 && bin < acc.nbins) {
-                bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-            } else {
-                atomicCAS(err, 0, ALB_ERR_CAPACITY);
+    const uint64_t chunks = (q.n + kQueryChunk - 1) / kQueryChunk;
+    bool failed = false;
+    for (uint64_t ch = (uint64_t)blockIdx.x * kGatherWarps + w; ch < chunks && !failed; ch += warps) {
+        const uint64_t q_end = min((ch + 1) * kQueryChunk, q.n);
+        double px = 0.0, py = 0.0, pz = 0.0, prk = -1.0;  // previous query of the chunk and its r_k
+        for (uint64_t qi = ch * kQueryChunk; qi < q_end; ++qi) {
+            uint64_t src = q.perm ? q.perm[qi] : qi;
+            float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
+            double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
+            float thr0 = FLT_MAX;
+            if (prk >= 0.0) {
+                double ddx = qx - px, ddy = qy - py, ddz = qz - pz;
+                double bound = prk + sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+                double t = bound * bound * (1.0 + 1.0 / 16384.0);
+                if (t < 1.0e38) thr0 = __double2float_ru(t);
             }
-            if (acc.hw_lo && m.fwi) {
-                // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61
-                float4 fw = m.fwi[idx], sf = m.sfi[idx];
-                Fix128 f = f32_to_fix(c);
-                if (fw.x == fw.x) {
-                    long long xi = (long long)(((double)fw.x - sc.wc[0] + sc.hm_wext) / sc.hm_wbin);
-                    long long zi = (long long)(((double)fw.z - sc.wc[2] + sc.hm_wext) / sc.hm_wbin);
-                    if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
-                        fix_atomic_add(acc.hw_lo + xi * sc.hm_bins + zi, acc.hw_hi + xi * sc.hm_bins + zi, f);
+            KnnResult r;
+            if (!warp_knn(m, s, k, qx, qy, qz, thr0, r)) {
+                if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
+                failed = true;
+                break;
+            }
+            px = qx;
+            py = qy;
+            pz = qz;
+            prk = r.rk;
+            if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
+            if (q.stats && l == 0) {
+                atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
+                atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
+                atomicAdd(q.stats + 2, (unsigned long long)r.selects);
+                atomicAdd(q.stats + 3, 1ull);
+            }
+            const float Es = qa.w, ts = qb.w;
+            const float rk = (float)r.rk;
+            float norm;
+            if (CHANNEL == ALB_SCATTER) norm = 1.0f / ((4.0f / 3.0f) * 3.14159265358979f * rk * rk * rk);
+            else norm = 1.0f / (3.14159265358979f * rk * rk);
+            // query-constant pieces
+            float vinv = rsqrtf(fmaf(qb.x, qb.x, fmaf(qb.y, qb.y, qb.z * qb.z)));
+            float vx = -qb.x * vinv, vy = -qb.y * vinv, vz = -qb.z * vinv;  // normalize(-d_query)
+            float wconst = 0.f;
+            if (CHANNEL == ALB_BOTTOM_REFLECTION) wconst = (float)(sc.floor_albedo / kPi) * fmaxf(0.f, -qb.y);
+            if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
+            // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
+            const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
+            for (int j = l; j < k; j += 32) {
+                uint32_t idx = knn_index(s, r, j);
+                float4 pa = m.a[idx], pb = m.b[idx];
+                float w;
+                if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+                else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+                else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+                float c = ((Es * pa.w) * norm) * w;
+                int bin = (int)((ts + pb.w) / (float)sc.mult);
+                if (bin >= 0 && bin < acc.nbins) {
+                    bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                } else {
+                    atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }
-                if (sf.x == sf.x) {
-                    long long xi = (long long)(((double)sf.x - sc.fc[0] + sc.hm_fext) / sc.hm_fbin);
-                    long long zi = (long long)(((double)sf.z - sc.fc[2] + sc.hm_fext) / sc.hm_fbin);
-                    if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
-                        fix_atomic_add(acc.hf_lo + xi * sc.hm_bins + zi, acc.hf_hi + xi * sc.hm_bins + zi, f);
+                if (acc.hw_lo && m.fwi) {
+                    // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61
+                    float4 fw = m.fwi[idx], sf = m.sfi[idx];
+                    Fix128 f = f32_to_fix(c);
+                    if (fw.x == fw.x) {
+                        long long xi = (long long)(((double)fw.x - sc.wc[0] + sc.hm_wext) / sc.hm_wbin);
+                        long long zi = (long long)(((double)fw.z - sc.wc[2] + sc.hm_wext) / sc.hm_wbin);
+                        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+                            fix_atomic_add(acc.hw_lo + xi * sc.hm_bins + zi, acc.hw_hi + xi * sc.hm_bins + zi, f);
+                    }
+                    if (sf.x == sf.x) {
+                        long long xi = (long long)(((double)sf.x - sc.fc[0] + sc.hm_fext) / sc.hm_fbin);
+                        long long zi = (long long)(((double)sf.z - sc.fc[2] + sc.hm_fext) / sc.hm_fbin);
+                        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+                            fix_atomic_add(acc.hf_lo + xi * sc.hm_bins + zi, acc.hf_hi + xi * sc.hm_bins + zi, f);
+                    }
                 }
             }
+            __syncwarp();
         }
-        __syncwarp();
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kBinCache; i += blockDim.x) {
@@ -511,7 +570,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const doubl
     for (uint64_t qi = (uint64_t)blockIdx.x * kGatherWarps + w; qi < nq; qi += warps) {
         double qx = qs[3 * qi], qy = qs[3 * qi + 1], qz = qs[3 * qi + 2];
         KnnResult r;
-        if (!warp_knn(m, s, k, qx, qy, qz, r)) {
+        if (!warp_knn(m, s, k, qx, qy, qz, FLT_MAX, r)) {
             if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
             return;
         }
