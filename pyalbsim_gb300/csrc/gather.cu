@@ -25,17 +25,28 @@ namespace alb {
 constexpr int kGatherWarps = 4;
 constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one warp
 constexpr int kStack = 32 * kMaxLevels;
-constexpr int kCap = 288;        // candidate buffer; shrunk when more than kCap-32 are held
-constexpr float kRelMargin = 3.814697265625e-06f;  // 2^-18
+constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
+constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
+constexpr int kLeafBatch = 1;     // leaves opened per round (loads of several overlap)
+constexpr int kBand = 32;         // near-tie entries resolved in float64
+constexpr int kWeightBatch = 1;   // neighbour rounds of 32 whose records are loaded together
+// Admission margin of the float32 screening distance (its error is below 2^-22 relative).
+constexpr float kRelMargin = 9.5367431640625e-07f;  // 2^-20
 
+// Candidates carry an error-free double-float squared distance, stored as its float32 high
+// part cd and a 16-bit fraction cl of one ulp of cd (key48 = cd bits : cl + 2^15 orders
+// them to ~2^-40 relative); only entries within one key unit of the k-th are resolved in
+// float64.
 struct WarpSmem {
     uint32_t stk[kStack];
     float stk_d[kStack];
     float cd[kCap];
     uint32_t ci[kCap];
-    uint32_t hist[256];
-    double bd[64];      // boundary band: float64 distances
-    uint32_t bi[64];
+    int16_t cl[kCap];
+    uint32_t hist[128];  // 256 radix bins, two 16-bit counters per word
+    double bd[kBand];    // near-tie band: float64 distances
+    uint32_t bi[kBand];  // map positions
+    uint64_t bt[kBand];  // tie keys from the record's content (or 0)
 };
 
 // Lower bound of the squared distance from the float64 query (qx + lx, ...) to a box:
@@ -65,6 +76,84 @@ ALB_DEVICE double point_dist2_f64(double qx, double qy, double qz, float4 p) {
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// Error-free transforms (Knuth two-sum); the _rn intrinsics keep the compiler from fusing
+// the operations into FMAs, which would break the error terms.
+ALB_DEVICE void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Squared distance from the query (f + l per axis) to p as hi + lo with about 2^-44
+// relative error: exact per-axis differences by two-sum, squares by FMA two-product.
+ALB_DEVICE void point_dist2_df(float fx, float fy, float fz, float lx, float ly, float lz, float4 p, float& hi,
+                               float& lo) {
+    float sx, ex, sy, ey, sz, ez;
+    two_sum(p.x, -fx, sx, ex);
+    two_sum(p.y, -fy, sy, ey);
+    two_sum(p.z, -fz, sz, ez);
+    float hx, tx, hy, ty, hz, tz;
+    two_sum(sx, __fsub_rn(ex, lx), hx, tx);
+    two_sum(sy, __fsub_rn(ey, ly), hy, ty);
+    two_sum(sz, __fsub_rn(ez, lz), hz, tz);
+    const float px = __fmul_rn(hx, hx), py = __fmul_rn(hy, hy), pz = __fmul_rn(hz, hz);
+    const float qx = fmaf(2.f * hx, tx, fmaf(hx, hx, -px));
+    const float qy = fmaf(2.f * hy, ty, fmaf(hy, hy, -py));
+    const float qz = fmaf(2.f * hz, tz, fmaf(hz, hz, -pz));
+    float s1, e1, s2, e2;
+    two_sum(px, py, s1, e1);
+    two_sum(s1, pz, s2, e2);
+    const float t = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(qx, qy), qz));
+    hi = __fadd_rn(__fadd_rn(s2, t), 0.f);  // (+0 for an exact zero)
+    lo = __fsub_rn(t, __fsub_rn(hi, s2));
+}
+
+// lo in units of 2^-16 ulp(hi), clamped to 16 bits
+ALB_DEVICE int16_t frac16(float hi, float lo) {
+    const int e = (int)((__float_as_uint(hi) >> 23) & 255u);
+    if (e == 0) return 0;
+    const int sh = min(166 - e, 127);  // 2^(16 + 23 - (e - 127))
+    float q = lo * __uint_as_float((uint32_t)(sh + 127) << 23);
+    q = fminf(fmaxf(rintf(q), -32767.f), 32767.f);
+    return (int16_t)q;
+}
+
+ALB_DEVICE uint64_t cand_key(const WarpSmem& s, int i) {
+    return ((uint64_t)__float_as_uint(s.cd[i]) << 16) | (uint32_t)((int)s.cl[i] + 32768);
+}
+
+// float32(sqrt(x)) for a double x >= 0, correctly rounded (equal to casting the float64
+// square root, as double rounding is harmless for sqrt from 53 to 24 bits): a float32
+// estimate corrected against the squared float midpoints, which are exact in float64.
+ALB_DEVICE float sqrt_to_f32(double x) {
+    if (!(x > 0.0)) return 0.f;
+    float s = sqrtf(__double2float_rn(x));
+    const float up = __int_as_float(__float_as_int(s) + 1);
+    const float dn = __int_as_float(__float_as_int(s) - 1);
+    const double mh = 0.5 * ((double)s + (double)up), ml = 0.5 * ((double)s + (double)dn);
+    const double mh2 = mh * mh, ml2 = ml * ml;
+    if (x > mh2 || (x == mh2 && (__float_as_int(up) & 1) == 0)) s = up;
+    else if (x < ml2 || (x == ml2 && (__float_as_int(dn) & 1) == 0)) s = dn;
+    return s;
+}
+
+// Tie key of a map record: its time bits (high word; times are non-negative) and a 32-bit
+// mix of its direction, time and energy bits (low word).
+ALB_DEVICE uint64_t record_tie_key(float4 a, float4 b) {
+    uint32_t h = 0x9e3779b9u;
+    const uint32_t w[4] = {__float_as_uint(b.x), __float_as_uint(b.y), __float_as_uint(b.z), __float_as_uint(a.w)};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        h ^= w[i] * 0x85ebca6bu;
+        h = (h << 13) | (h >> 19);
+        h = h * 5u + 0xe6546b64u;
+    }
+    h ^= h >> 16;
+    h *= 0x7feb352du;
+    h ^= h >> 15;
+    return ((uint64_t)__float_as_uint(b.w) << 32) | h;
+}
+
 // Warp bitonic sort of 32 (key, value) pairs, ascending by key.
 ALB_DEVICE void warp_sort32(float& key, uint32_t& val) {
     const int l = lane_id();
@@ -85,25 +174,34 @@ ALB_DEVICE void warp_sort32(float& key, uint32_t& val) {
     }
 }
 
-// k-th smallest (1-based) of cnt float distances in cd[] (all >= 0): warp radix select.
-ALB_DEVICE float warp_kth(WarpSmem& s, int cnt, int k) {
+// k-th smallest (1-based) 48-bit candidate key by warp radix select over its top
+// 8 * PASSES bits (PASSES = 4: the float32 part only; the lower bits return as 0).
+template <int PASSES>
+ALB_DEVICE uint64_t warp_kth_key(WarpSmem& s, int cnt, int k) {
     const int l = lane_id();
-    uint32_t prefix = 0u, pmask = 0u;
+    uint64_t prefix = 0ull, pmask = 0ull;
     int need = k;
-    for (int shift = 24; shift >= 0; shift -= 8) {
-        for (int i = l; i < 256; i += 32) s.hist[i] = 0u;
+#pragma unroll 1
+    for (int pass = 0; pass < PASSES; ++pass) {
+        const int shift = 40 - 8 * pass;
+        for (int i = l; i < 128; i += 32) s.hist[i] = 0u;
         __syncwarp();
         for (int i = l; i < cnt; i += 32) {
-            uint32_t u = __float_as_uint(s.cd[i]);
-            if ((u & pmask) == prefix) atomicAdd(&s.hist[(u >> shift) & 255u], 1u);
+            const uint64_t u = cand_key(s, i);
+            if ((u & pmask) == prefix) {
+                const uint32_t d = (uint32_t)(u >> shift) & 255u;
+                atomicAdd(&s.hist[d >> 1], 1u << ((d & 1u) * 16u));
+            }
         }
         __syncwarp();
         // inclusive scan over 256 bins, 8 per lane
         uint32_t h[8], run = 0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            h[j] = s.hist[l * 8 + j];
-            run += h[j];
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t w = s.hist[l * 4 + j];
+            h[2 * j] = w & 0xffffu;
+            h[2 * j + 1] = w >> 16;
+            run += h[2 * j] + h[2 * j + 1];
         }
         uint32_t incl = run;
         for (int o = 1; o < 32; o <<= 1) {
@@ -125,15 +223,15 @@ ALB_DEVICE float warp_kth(WarpSmem& s, int cnt, int k) {
         int src = __ffs(who) - 1;
         digit = __shfl_sync(0xffffffffu, digit, src);
         below = __shfl_sync(0xffffffffu, below, src);
-        prefix |= ((uint32_t)digit) << shift;
-        pmask |= 255u << shift;
+        prefix |= ((uint64_t)digit) << shift;
+        pmask |= 255ull << shift;
         need -= (int)below;
         __syncwarp();
     }
-    return __uint_as_float(prefix);
+    return prefix;
 }
 
-// Keep the candidates with distance <= thr (order not preserved).
+// Keep the candidates whose float32 part is <= thr (order not preserved).
 ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
     const int l = lane_id();
     int out = 0;
@@ -141,6 +239,7 @@ ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
         int i = base + l;
         float d = i < cnt ? s.cd[i] : FLT_MAX;
         uint32_t id = i < cnt ? s.ci[i] : 0u;
+        int16_t lo = i < cnt ? s.cl[i] : (int16_t)0;
         bool keep = i < cnt && d <= thr;
         unsigned b = __ballot_sync(0xffffffffu, keep);
         __syncwarp();
@@ -148,6 +247,7 @@ ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
             int pos = out + __popc(b & lanemask_lt());
             s.cd[pos] = d;
             s.ci[pos] = id;
+            s.cl[pos] = lo;
         }
         out += __popc(b);
         __syncwarp();
@@ -158,7 +258,8 @@ ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
 struct KnnResult {
     int n_in;          // candidates in cd/ci that are definitely among the k nearest
     int n_band_take;   // band entries bi[0..n_band_take) also taken
-    double rk;         // float64 distance of the k-th neighbour
+    double rk2;        // float64 squared distance of the k-th neighbour
+    float rkf;         // float32(sqrt(rk2)), correctly rounded
     int leaves;        // leaves opened (32 records each)
     int nodes;         // internal nodes expanded
     int selects;       // candidate-buffer reductions
@@ -167,11 +268,15 @@ struct KnnResult {
 // Full k-NN search for one query. Returns false when the map has fewer than k records.
 // thr0: an upper bound of the squared k-th distance that already includes the band margin
 // (FLT_MAX when none is known).
-ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz,
-                         float thr0, KnnResult& res) {
+// The query is (fx + lx, fy + ly, fz + lz) = (qx, qy, qz) exactly, |l*| <= half an ulp of f*.
+// Points at exactly the same float64 distance rank by a key taken from their record content
+// (time, then a hash of direction, time and energy; when tie_rec is given) and then by map
+// position, so that the chosen neighbours do not depend on the order in which the map's
+// records are stored (records equal in all of these contribute identically).
+ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz, float fx,
+                         float fy, float fz, float lx, float ly, float lz, float thr0, const float4* tie_rec,
+                         KnnResult& res) {
     const int l = lane_id();
-    const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
-    const float lx = (float)(qx - (double)fx), ly = (float)(qy - (double)fy), lz = (float)(qz - (double)fz);
     if (m.n_real < (uint64_t)k) return false;
     float thr = thr0;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
@@ -205,48 +310,94 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         int guard = 0;
         while (sp > 0) {
             if (++guard > (1 << 22)) break;
-            // skip entries beyond the threshold, 32 at a time
-            {
-                int i = sp - 1 - l;
-                unsigned ok = __ballot_sync(0xffffffffu, i >= 0 && s.stk_d[i] <= thr);
-                if (!ok) {
-                    sp = sp > 32 ? sp - 32 : 0;
+            // the top 32 stack entries, one per lane (lane 0 = top)
+            const int i = sp - 1 - l;
+            uint32_t e = 0u;
+            bool ok = false;
+            if (i >= 0) {
+                e = s.stk[i];
+                ok = s.stk_d[i] <= thr;
+            }
+            const unsigned okm = __ballot_sync(0xffffffffu, ok);
+            if (!okm) {  // 32 entries beyond the threshold
+                sp = sp > 32 ? sp - 32 : 0;
+                __syncwarp();
+                continue;
+            }
+            const int f = __ffs(okm) - 1;
+            const uint32_t etop = __shfl_sync(0xffffffffu, e, f);
+            if ((etop >> 29) == 0) {
+                // leaves: the valid leaf entries above the first valid node entry, at most
+                // kLeafBatch and as many as the buffer has room for
+                const unsigned leafm = __ballot_sync(0xffffffffu, ok && (e >> 29) == 0);
+                const unsigned nodem = okm & ~leafm;
+                unsigned takem = nodem ? (leafm & ((1u << (__ffs(nodem) - 1)) - 1u)) : leafm;
+                const int room = (kCap - cnt) >> 5;
+                const int want = room < kLeafBatch ? room : kLeafBatch;
+                uint32_t leaf[kLeafBatch];
+                int nt = 0, last = f;
+#pragma unroll
+                for (int t = 0; t < kLeafBatch; ++t) {
+                    leaf[t] = 0u;
+                    if (t < want && takem) {
+                        const int ln = __ffs(takem) - 1;
+                        takem &= takem - 1u;
+                        leaf[t] = __shfl_sync(0xffffffffu, e, ln);
+                        last = ln;
+                        ++nt;
+                    }
+                }
+                if (nt == 0) {  // no room (only after pathological ties): drop the entry
+                    sp -= f + 1;
                     __syncwarp();
                     continue;
                 }
-                sp -= __ffs(ok) - 1;
-            }
-            --sp;
-            uint32_t e = s.stk[sp];
-            __syncwarp();
-            int lev = (int)(e >> 29);
-            uint32_t node = e & 0x1fffffffu;
-            if (lev == 0) {
-                ++res.leaves;
-                uint64_t i = (uint64_t)node * 32 + l;
-                float d = FLT_MAX;
-                if (i < m.n) d = point_dist2(fx, fy, fz, lx, ly, lz, m.a[i]);
-                bool take = d <= thr;
-                unsigned b = __ballot_sync(0xffffffffu, take);
-                if (take) {
-                    int pos = cnt + __popc(b & lanemask_lt());
-                    s.cd[pos] = d;
-                    s.ci[pos] = (uint32_t)i;
-                }
-                cnt += __popc(b);
+                sp -= last + 1;
                 __syncwarp();
-                if (cnt >= k && (thr == FLT_MAX || cnt > kCap - 32)) {
-                    ++res.selects;
-                    float kth = warp_kth(s, cnt, k);
-                    thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
-                    cnt = warp_compact(s, cnt, thr);
-                    if (cnt > kCap - 32) {  // pathological ties: fall back to the bare threshold
-                        thr = kth;
-                        cnt = warp_compact(s, cnt, thr);
+                float4 p[kLeafBatch];
+#pragma unroll
+                for (int t = 0; t < kLeafBatch; ++t) {
+                    const uint64_t r = (uint64_t)leaf[t] * 32 + l;
+                    p[t] = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+                    if (t < nt && r < m.n) p[t] = m.a[r];
+                }
+#pragma unroll
+                for (int t = 0; t < kLeafBatch; ++t) {
+                    if (t < nt) {
+                        const uint64_t r = (uint64_t)leaf[t] * 32 + l;
+                        const bool real = r < m.n;  // the last leaf may be partial
+                        const float d = real ? point_dist2(fx, fy, fz, lx, ly, lz, p[t]) : FLT_MAX;
+                        const bool take = real && d <= thr;
+                        const unsigned b = __ballot_sync(0xffffffffu, take);
+                        if (take) {
+                            float hi, lo;
+                            point_dist2_df(fx, fy, fz, lx, ly, lz, p[t], hi, lo);
+                            const int pos = cnt + __popc(b & lanemask_lt());
+                            s.cd[pos] = hi;
+                            s.ci[pos] = (uint32_t)r;
+                            s.cl[pos] = frac16(hi, lo);
+                        }
+                        cnt += __popc(b);
                     }
                 }
+                res.leaves += nt;
+                __syncwarp();
+                if (cnt >= k && (thr == FLT_MAX || cnt > kSelectAt)) {
+                    ++res.selects;
+                    const float kth = __uint_as_float((uint32_t)(warp_kth_key<4>(s, cnt, k) >> 16));
+                    thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
+                    // refined distances within one float32 ulp of the k-th can still rank
+                    // among the k nearest; nothing beyond can
+                    cnt = warp_compact(s, cnt, __uint_as_float(__float_as_uint(kth) + 1u));
+                    if (cnt > kCap - 32) cnt = warp_compact(s, cnt, kth);  // mass ties
+                    if (cnt > kCap - 32) cnt = kCap - 32;  // keeps the buffer in bounds
+                }
             } else {
+                sp -= f + 1;
+                __syncwarp();
                 ++res.nodes;
+                const int lev = (int)(etop >> 29);
+                const uint32_t node = etop & 0x1fffffffu;
                 uint64_t c = (uint64_t)node * 32 + l;
                 float d = FLT_MAX;
                 int cl = lev - 1;
@@ -282,30 +433,26 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         }
         if (cnt >= k || thr0 == FLT_MAX) break;
     }
-    // final: exact k with the float64 boundary band
-    float kth = warp_kth(s, cnt, k);
-    float band_lo = kth * (1.0f - 2.0f * kRelMargin);
-    float band_hi = kth * (1.0f + 2.0f * kRelMargin);
-    // partition: definitely-in to the front, band to bd/bi
+    // final: the k-th 48-bit key; keys more than one unit below it are in, keys within one
+    // unit of it are ranked in float64
+    const uint64_t K = warp_kth_key<6>(s, cnt, k);
     int n_in = 0, n_band = 0;
     for (int base = 0; base < cnt; base += 32) {
         int i = base + l;
-        float d = i < cnt ? s.cd[i] : FLT_MAX;
-        uint32_t id = i < cnt ? s.ci[i] : 0u;
-        bool in = i < cnt && d < band_lo;
-        bool band = i < cnt && d >= band_lo && d <= band_hi;
+        const bool valid = i < cnt;
+        const uint64_t key = valid ? cand_key(s, i) : ~0ull;
+        uint32_t id = valid ? s.ci[i] : 0u;
+        bool in = valid && key + 1ull < K;
+        bool band = valid && !in && key <= K + 1ull;
         unsigned bin = __ballot_sync(0xffffffffu, in);
         unsigned bb = __ballot_sync(0xffffffffu, band);
         __syncwarp();
-        if (in) {
-            int pos = n_in + __popc(bin & lanemask_lt());
-            s.cd[pos] = d;
-            s.ci[pos] = id;
-        }
+        if (in) s.ci[n_in + __popc(bin & lanemask_lt())] = id;
         if (band) {
             int pos = n_band + __popc(bb & lanemask_lt());
-            if (pos < 64) {
+            if (pos < kBand) {
                 s.bi[pos] = id;
+                s.bt[pos] = tie_rec ? record_tie_key(m.a[id], tie_rec[id]) : 0ull;
                 s.bd[pos] = point_dist2_f64(qx, qy, qz, m.a[id]);
             }
         }
@@ -313,37 +460,34 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         n_band += __popc(bb);
         __syncwarp();
     }
-    if (n_band > 64) n_band = 64;
+    if (n_band > kBand) n_band = kBand;
     int take = k - n_in;
-    // rank band entries by (float64 distance, index); keep the `take` smallest, in rank order
-    double rk2 = 0.0;
-    for (int base = 0; base < n_band; base += 32) {
-        int i = base + l;
-        int rank = 0;
-        double di = 0.0;
-        uint32_t ii = 0;
-        if (i < n_band) {
-            di = s.bd[i];
-            ii = s.bi[i];
-            for (int j = 0; j < n_band; ++j) {
-                double dj = s.bd[j];
-                uint32_t ij = s.bi[j];
-                rank += (dj < di || (dj == di && ij < ii)) ? 1 : 0;
-            }
+    // rank band entries by (float64 distance, tie key, map position); keep the `take`
+    // smallest, in rank order
+    // (kBand <= 32: one band entry per lane)
+    int rank = 0;
+    double di = 0.0;
+    uint32_t ii = 0;
+    if (l < n_band) {
+        di = s.bd[l];
+        ii = s.bi[l];
+        const uint64_t ti = s.bt[l];
+        for (int j = 0; j < n_band; ++j) {
+            const double dj = s.bd[j];
+            const uint64_t tj = s.bt[j];
+            rank += (dj < di || (dj == di && (tj < ti || (tj == ti && s.bi[j] < ii)))) ? 1 : 0;
         }
-        __syncwarp();
-        if (i < n_band && rank < take) {
-            s.hist[rank] = ii;  // reuse as the taken list, ordered by rank
-            if (rank == take - 1) rk2 = di;
-        }
-        __syncwarp();
     }
-    // broadcast the k-th distance (lane holding rank take-1)
-    double rk2_all = rk2;
-    for (int o = 16; o > 0; o >>= 1) rk2_all = fmax(rk2_all, __shfl_xor_sync(0xffffffffu, rk2_all, o));
+    __syncwarp();
+    const bool kth_lane = l < n_band && rank == take - 1;
+    if (l < n_band && rank < take) s.hist[rank] = ii;  // reuse as the taken list, ordered by rank
+    // broadcast the k-th distance from the lane that holds rank take-1
+    const unsigned owner = __ballot_sync(0xffffffffu, kth_lane);
+    const double rk2 = owner ? __shfl_sync(0xffffffffu, di, __ffs(owner) - 1) : 0.0;
     res.n_in = n_in;
     res.n_band_take = take;
-    res.rk = sqrt(rk2_all);
+    res.rk2 = rk2;
+    res.rkf = sqrt_to_f32(rk2);
     __syncwarp();
     return true;
 }
@@ -455,7 +599,7 @@ ALB_DEVICE void bin_add(BinCache& bc, const Accum& acc, int channel, int bin, co
 }
 
 template <int CHANNEL>
-__global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
+__global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
     __shared__ WarpSmem smem[kGatherWarps];
     __shared__ BinCache bc;
@@ -472,20 +616,22 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
     bool failed = false;
     for (uint64_t ch = (uint64_t)blockIdx.x * kGatherWarps + w; ch < chunks && !failed; ch += warps) {
         const uint64_t q_end = min((ch + 1) * kQueryChunk, q.n);
-        double px = 0.0, py = 0.0, pz = 0.0, prk = -1.0;  // previous query of the chunk and its r_k
+        double px = 0.0, py = 0.0, pz = 0.0;  // previous query of the chunk
+        float prk = -1.f;                     // and its k-th neighbour distance
         for (uint64_t qi = ch * kQueryChunk; qi < q_end; ++qi) {
             uint64_t src = q.perm ? q.perm[qi] : qi;
             float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
             double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
             float thr0 = FLT_MAX;
-            if (prk >= 0.0) {
-                double ddx = qx - px, ddy = qy - py, ddz = qz - pz;
-                double bound = prk + sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
-                double t = bound * bound * (1.0 + 1.0 / 16384.0);
-                if (t < 1.0e38) thr0 = __double2float_ru(t);
+            if (prk >= 0.f) {
+                // float32 rounding here is far inside the 2^-14 inflation
+                float ddx = (float)(qx - px), ddy = (float)(qy - py), ddz = (float)(qz - pz);
+                float bound = (prk + sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)))) * (1.f + 1.f / 32768.f);
+                float t = bound * bound * (1.f + 1.f / 16384.f);
+                if (t < 1.0e37f) thr0 = t;
             }
             KnnResult r;
-            if (!warp_knn(m, s, k, qx, qy, qz, thr0, r)) {
+            if (!warp_knn(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0, m.b, r)) {
                 if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
                 failed = true;
                 break;
@@ -493,8 +639,8 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
             px = qx;
             py = qy;
             pz = qz;
-            prk = r.rk;
-            if (q.rk_out && l == 0) q.rk_out[src] = r.rk;
+            prk = r.rkf;
+            if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
             if (q.stats && l == 0) {
                 atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
                 atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
@@ -502,7 +648,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
                 atomicAdd(q.stats + 3, 1ull);
             }
             const float Es = qa.w, ts = qb.w;
-            const float rk = (float)r.rk;
+            const float rk = r.rkf;
             float norm;
             if (CHANNEL == ALB_SCATTER) norm = 1.0f / ((4.0f / 3.0f) * 3.14159265358979f * rk * rk * rk);
             else norm = 1.0f / (3.14159265358979f * rk * rk);
@@ -514,22 +660,52 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(SceneDev sc, MapDe
             if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
             // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
             const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
-            for (int j = l; j < k; j += 32) {
-                uint32_t idx = knn_index(s, r, j);
-                float4 pa = m.a[idx], pb = m.b[idx];
-                float w;
-                if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
-                else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
-                else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
-                float c = ((Es * pa.w) * norm) * w;
-                int bin = (int)((ts + pb.w) / (float)sc.mult);
-                if (bin >= 0 && bin < acc.nbins) {
-                    bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-                } else {
-                    atomicCAS(err, 0, ALB_ERR_CAPACITY);
+            // neighbour records are fetched for kWeightBatch rounds of 32 before any is used,
+            // so their loads overlap
+            for (int j0 = 0; j0 < k; j0 += 32 * kWeightBatch) {
+                float nE[kWeightBatch];
+                float4 nb[kWeightBatch];
+#pragma unroll
+                for (int t = 0; t < kWeightBatch; ++t) {
+                    const int j = j0 + 32 * t + l;
+                    nE[t] = 0.f;
+                    nb[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (j < k) {
+                        const uint32_t idx = knn_index(s, r, j);
+                        nE[t] = __ldg(&m.a[idx].w);
+                        nb[t] = __ldg(&m.b[idx]);
+                    }
                 }
-                if (acc.hw_lo && m.fwi) {
-                    // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61
+#pragma unroll
+                for (int t = 0; t < kWeightBatch; ++t) {
+                    const int j = j0 + 32 * t + l;
+                    if (j >= k) continue;
+                    const float4 pb = nb[t];
+                    float w;
+                    if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+                    else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+                    else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+                    float c = ((Es * nE[t]) * norm) * w;
+                    int bin = (int)((ts + pb.w) / (float)sc.mult);
+                    if (bin >= 0 && bin < acc.nbins) {
+                        bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                    } else {
+                        atomicCAS(err, 0, ALB_ERR_CAPACITY);
+                    }
+                }
+            }
+            if (acc.hw_lo && m.fwi) {
+                // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61 (a separate,
+                // non-unrolled pass: heatmaps are off in production runs)
+#pragma unroll 1
+                for (int j = l; j < k; j += 32) {
+                    const uint32_t idx = knn_index(s, r, j);
+                    const float4 pb = m.b[idx];
+                    float w;
+                    if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+                    else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+                    else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+                    const float c = ((Es * m.a[idx].w) * norm) * w;
                     float4 fw = m.fwi[idx], sf = m.sfi[idx];
                     Fix128 f = f32_to_fix(c);
                     if (fw.x == fw.x) {
@@ -570,7 +746,9 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const doubl
     for (uint64_t qi = (uint64_t)blockIdx.x * kGatherWarps + w; qi < nq; qi += warps) {
         double qx = qs[3 * qi], qy = qs[3 * qi + 1], qz = qs[3 * qi + 2];
         KnnResult r;
-        if (!warp_knn(m, s, k, qx, qy, qz, FLT_MAX, r)) {
+        const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+        if (!warp_knn(m, s, k, qx, qy, qz, fx, fy, fz, (float)(qx - (double)fx), (float)(qy - (double)fy),
+                      (float)(qz - (double)fz), FLT_MAX, nullptr, r)) {
             if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
             return;
         }

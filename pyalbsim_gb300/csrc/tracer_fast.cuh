@@ -30,7 +30,8 @@ struct PhF {
     int s;
 };
 
-ALB_DEVICE float uf(uint32_t x) { return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f; }
+// (x / 2^9 + 0.5) / 2^23: an exact float strictly inside (0, 1), 2^23 equally spaced values
+ALB_DEVICE float uf(uint32_t x) { return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f; }
 
 ALB_DEVICE int layer_of_f(const SceneDev& sc, float y) {
     float depth = -(y - (float)sc.ys);
@@ -266,25 +267,26 @@ ALB_DEVICE void emit_photon_fast(const SceneDev& sc, PhF& ph, PhiloxSrc& src) {
     ph.sfi[0] = ph.sfi[1] = ph.sfi[2] = qnan;
     U4 b = src.block();
     if (PASS == ALB_FORWARD) {
-        float th = (float)sc.rayleigh_sigma * sqrtf(-2.f * __logf(1.f - uf(b.x) * (float)sc.rayleigh_mass));
+        // once per photon: accurate logf / sincosf keep the beam footprint unquantised
+        float th = (float)sc.rayleigh_sigma * sqrtf(-2.f * log1pf(-uf(b.x) * (float)sc.rayleigh_mass));
         float st, ct, sp, cp;
-        __sincosf(th, &st, &ct);
-        __sincosf(6.283185307179586f * uf(b.y), &sp, &cp);
+        sincosf(th, &st, &ct);
+        sincospif(2.f * uf(b.y), &sp, &cp);
         float l0 = st * cp, l1 = st * sp, l2 = ct;
         ph.dx = l0 * R[0] + l1 * R[1] + l2 * R[2];
         ph.dy = l0 * R[3] + l1 * R[4] + l2 * R[5];
         ph.dz = l0 * R[6] + l1 * R[7] + l2 * R[8];
-        float pulse = (float)sc.pulse_sigma32 * sqrtf(-2.f * __logf(uf(b.z))) * __cosf(6.283185307179586f * uf(b.w));
+        float pulse = (float)sc.pulse_sigma32 * sqrtf(-2.f * logf(uf(b.z))) * cospif(2.f * uf(b.w));
         ph.t0 = pulse / (float)sc.eff_rate32;
     } else {
         float r = (float)sc.aperture * sqrtf(uf(b.x));
         float sa, ca;
-        __sincosf(6.283185307179586f * uf(b.y), &sa, &ca);
+        sincospif(2.f * uf(b.y), &sa, &ca);
         float d0 = r * ca, d1 = r * sa;
         float z = (float)sc.cos_fov + (1.f - (float)sc.cos_fov) * uf(b.z);
         float st = sqrtf(fmaxf(0.f, 1.f - z * z));
         float sp, cp;
-        __sincosf(6.283185307179586f * uf(b.w), &sp, &cp);
+        sincospif(2.f * uf(b.w), &sp, &cp);
         float l0 = st * cp, l1 = st * sp;
         // aperture point added to the direction, as the reference does
         ph.dx = (d0 * R[0] + d1 * R[1]) + (l0 * R[0] + l1 * R[1] + z * R[2]);
