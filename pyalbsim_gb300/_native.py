@@ -377,9 +377,10 @@ class NativeContext:
 
     def stats(self):
         """Counters of the last trace (events, photons) and gathers (per channel: leaves
-        opened, internal nodes expanded, candidate reductions, queries)."""
-        out = np.zeros(20, np.int64)
-        self._check(self.lib.alb_stats(self.h, _ptr(out), 20))
+        opened, internal nodes expanded, candidate reductions, queries, and queries whose
+        answer a buffer bound made inexact, which takes mass ties of distances)."""
+        out = np.zeros(32, np.int64)
+        self._check(self.lib.alb_stats(self.h, _ptr(out), 32))
         st = {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2])}
         for c, name in enumerate(("bottom", "scatter", "surface_reflection", "transmission_up")):
             lv, nd, se, nq = (int(x) for x in out[4 + 4 * c: 8 + 4 * c])
@@ -388,6 +389,7 @@ class NativeContext:
                 "leaves_per_query": lv / nq if nq else 0.0,
                 "nodes_per_query": nd / nq if nq else 0.0,
                 "selects_per_query": se / nq if nq else 0.0,
+                "inexact": int(out[24 + c]),
             }
         return st
 

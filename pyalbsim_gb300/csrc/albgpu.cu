@@ -599,6 +599,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         q.n = nq;
         q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
         q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
+        q.inexact = ctx->d_stats + 24 + c;
         if (ctx->sort_q) {
             PhaseTimer ps(ctx, 3);
             sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);

@@ -27,9 +27,7 @@ constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one wa
 constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
 constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
-constexpr int kLeafBatch = 1;     // leaves opened per round (loads of several overlap)
 constexpr int kBand = 32;         // near-tie entries resolved in float64
-constexpr int kWeightBatch = 1;   // neighbour rounds of 32 whose records are loaded together
 // Admission margin of the float32 screening distance (its error is below 2^-22 relative).
 constexpr float kRelMargin = 9.5367431640625e-07f;  // 2^-20
 
@@ -174,10 +172,70 @@ ALB_DEVICE void warp_sort32(float& key, uint32_t& val) {
     }
 }
 
+// Shared radix-select step: from the 256-bin histogram in s.hist (two 16-bit counters per
+// word) pick the digit holding the need-th (1-based) entry; need becomes its rank inside.
+ALB_DEVICE uint32_t radix_pick(const WarpSmem& s, int& need) {
+    const int l = lane_id();
+    uint32_t h[8], run = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t w = s.hist[l * 4 + j];
+        h[2 * j] = w & 0xffffu;
+        h[2 * j + 1] = w >> 16;
+        run += h[2 * j] + h[2 * j + 1];
+    }
+    uint32_t incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (l >= o) incl += t;
+    }
+    uint32_t before = incl - run;
+    int digit = -1;
+    uint32_t below = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (digit < 0 && before + h[j] >= (uint32_t)need) {
+            digit = l * 8 + j;
+            below = before;
+        }
+        before += h[j];
+    }
+    const unsigned who = __ballot_sync(0xffffffffu, digit >= 0);
+    const int src = __ffs(who) - 1;
+    digit = __shfl_sync(0xffffffffu, digit, src);
+    below = __shfl_sync(0xffffffffu, below, src);
+    need -= (int)below;
+    return (uint32_t)digit;
+}
+
+// k-th smallest (1-based) float32 part cd[off .. off + cnt) (all >= 0): warp radix select.
+ALB_DEVICE float warp_kth32(WarpSmem& s, int off, int cnt, int k) {
+    const int l = lane_id();
+    uint32_t prefix = 0u, pmask = 0u;
+    int need = k;
+#pragma unroll 1
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int i = l; i < 128; i += 32) s.hist[i] = 0u;
+        __syncwarp();
+        for (int i = l; i < cnt; i += 32) {
+            const uint32_t u = __float_as_uint(s.cd[off + i]);
+            if ((u & pmask) == prefix) {
+                const uint32_t d = (u >> shift) & 255u;
+                atomicAdd(&s.hist[d >> 1], 1u << ((d & 1u) * 16u));
+            }
+        }
+        __syncwarp();
+        prefix |= radix_pick(s, need) << shift;
+        pmask |= 255u << shift;
+        __syncwarp();
+    }
+    return __uint_as_float(prefix);
+}
+
 // k-th smallest (1-based) 48-bit candidate key by warp radix select over its top
 // 8 * PASSES bits (PASSES = 4: the float32 part only; the lower bits return as 0).
 template <int PASSES>
-ALB_DEVICE uint64_t warp_kth_key(WarpSmem& s, int cnt, int k) {
+ALB_DEVICE uint64_t warp_kth_key(WarpSmem& s, int off, int cnt, int k) {
     const int l = lane_id();
     uint64_t prefix = 0ull, pmask = 0ull;
     int need = k;
@@ -187,45 +245,15 @@ ALB_DEVICE uint64_t warp_kth_key(WarpSmem& s, int cnt, int k) {
         for (int i = l; i < 128; i += 32) s.hist[i] = 0u;
         __syncwarp();
         for (int i = l; i < cnt; i += 32) {
-            const uint64_t u = cand_key(s, i);
+            const uint64_t u = cand_key(s, off + i);
             if ((u & pmask) == prefix) {
                 const uint32_t d = (uint32_t)(u >> shift) & 255u;
                 atomicAdd(&s.hist[d >> 1], 1u << ((d & 1u) * 16u));
             }
         }
         __syncwarp();
-        // inclusive scan over 256 bins, 8 per lane
-        uint32_t h[8], run = 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t w = s.hist[l * 4 + j];
-            h[2 * j] = w & 0xffffu;
-            h[2 * j + 1] = w >> 16;
-            run += h[2 * j] + h[2 * j + 1];
-        }
-        uint32_t incl = run;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (l >= o) incl += t;
-        }
-        uint32_t before = incl - run;
-        int digit = -1;
-        uint32_t below = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            if (digit < 0 && before + h[j] >= (uint32_t)need) {
-                digit = l * 8 + j;
-                below = before;
-            }
-            before += h[j];
-        }
-        unsigned who = __ballot_sync(0xffffffffu, digit >= 0);
-        int src = __ffs(who) - 1;
-        digit = __shfl_sync(0xffffffffu, digit, src);
-        below = __shfl_sync(0xffffffffu, below, src);
-        prefix |= ((uint64_t)digit) << shift;
+        prefix |= ((uint64_t)radix_pick(s, need)) << shift;
         pmask |= 255ull << shift;
-        need -= (int)below;
         __syncwarp();
     }
     return prefix;
@@ -255,17 +283,86 @@ ALB_DEVICE int warp_compact(WarpSmem& s, int cnt, float thr) {
     return out;
 }
 
+
 struct KnnResult {
-    int n_in;          // candidates in cd/ci that are definitely among the k nearest
-    int n_band_take;   // band entries bi[0..n_band_take) also taken
-    double rk2;        // float64 squared distance of the k-th neighbour
-    float rkf;         // float32(sqrt(rk2)), correctly rounded
-    int leaves;        // leaves opened (32 records each)
-    int nodes;         // internal nodes expanded
-    int selects;       // candidate-buffer reductions
+    double rk2;    // float64 squared distance of the k-th neighbour
+    float rkf;     // float32(sqrt(rk2)), correctly rounded
+    int leaves;    // leaves opened (32 records each)
+    int nodes;     // internal nodes expanded
+    int selects;   // candidate-buffer reductions
+    int clipped;   // 1 if a buffer bound forced an inexact answer (mass ties)
 };
 
-// Full k-NN search for one query. Returns false when the map has fewer than k records.
+// float64 ranking of the band entries bi[0..nb) by (distance, tie key, map position); the
+// `take` smallest go to ci[dst ..] in rank order. Returns the float64 squared distance of
+// the take-th (0 if the band holds fewer).
+ALB_DEVICE double rank_band(const MapDev& m, WarpSmem& s, int dst, int nb, int take, double qx, double qy,
+                            double qz, const float4* tie_rec) {
+    const int l = lane_id();
+    double di = 0.0;
+    uint64_t ti = 0ull;
+    uint32_t ii = 0u;
+    int rank = 0;
+    if (l < nb) {
+        ii = s.bi[l];
+        const float4 a = m.a[ii];
+        di = point_dist2_f64(qx, qy, qz, a);
+        ti = tie_rec ? record_tie_key(a, tie_rec[ii]) : 0ull;
+        s.bd[l] = di;
+        s.bt[l] = ti;
+    }
+    __syncwarp();
+    if (l < nb) {
+        for (int j = 0; j < nb; ++j) {
+            const double dj = s.bd[j];
+            const uint64_t tj = s.bt[j];
+            rank += (dj < di || (dj == di && (tj < ti || (tj == ti && s.bi[j] < ii)))) ? 1 : 0;
+        }
+    }
+    __syncwarp();
+    if (l < nb && rank < take) s.ci[dst + rank] = ii;
+    const unsigned owner = __ballot_sync(0xffffffffu, l < nb && rank == take - 1);
+    const double rk2 = owner ? __shfl_sync(0xffffffffu, di, __ffs(owner) - 1) : 0.0;
+    __syncwarp();
+    return rk2;
+}
+
+// The k_sub nearest among the entries [off, off + n) whose cd/cl hold refined keys: keys more
+// than one unit below the k_sub-th are in, keys within one unit of it are ranked in float64.
+// The chosen map positions end up in ci[off .. off + k_sub).
+ALB_DEVICE double select_refined(const MapDev& m, WarpSmem& s, int off, int n, int k_sub, double qx, double qy,
+                                 double qz, const float4* tie_rec, int& clipped) {
+    const int l = lane_id();
+    const uint64_t K = warp_kth_key<6>(s, off, n, k_sub);
+    int n_in = 0, n_band = 0;
+    for (int base = 0; base < n; base += 32) {
+        const bool valid = base + l < n;
+        const int i = off + base + l;
+        const uint64_t key = valid ? cand_key(s, i) : ~0ull;
+        const uint32_t id = valid ? s.ci[i] : 0u;
+        const bool in = valid && key + 1ull < K;
+        const bool band = valid && !in && key <= K + 1ull;
+        const unsigned bin = __ballot_sync(0xffffffffu, in);
+        const unsigned bb = __ballot_sync(0xffffffffu, band);
+        __syncwarp();
+        if (in) s.ci[off + n_in + __popc(bin & lanemask_lt())] = id;
+        if (band) {
+            const int pos = n_band + __popc(bb & lanemask_lt());
+            if (pos < kBand) s.bi[pos] = id;
+        }
+        n_in += __popc(bin);
+        n_band += __popc(bb);
+        __syncwarp();
+    }
+    if (n_band > kBand) {
+        n_band = kBand;
+        clipped = 1;
+    }
+    return rank_band(m, s, off + n_in, n_band, k_sub - n_in, qx, qy, qz, tie_rec);
+}
+
+// Full k-NN search for one query. Returns false when the map has fewer than k records; the
+// k nearest map positions are then in s.ci[0 .. k).
 // thr0: an upper bound of the squared k-th distance that already includes the band margin
 // (FLT_MAX when none is known).
 // The query is (fx + lx, fy + ly, fz + lz) = (qx, qy, qz) exactly, |l*| <= half an ulp of f*.
@@ -273,6 +370,11 @@ struct KnnResult {
 // (time, then a hash of direction, time and energy; when tie_rec is given) and then by map
 // position, so that the chosen neighbours do not depend on the order in which the map's
 // records are stored (records equal in all of these contribute identically).
+// REFINE: candidates carry double-float distances from admission on, so the buffer only ever
+// holds entries within one float32 ulp of the k-th: needed where many points sit at nearly
+// the same distance (queries far from a dense planar map). Without it candidates carry the
+// float32 screening distance and only a crowded final band is refined.
+template <bool REFINE>
 ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz, float fx,
                          float fy, float fz, float lx, float ly, float lz, float thr0, const float4* tie_rec,
                          KnnResult& res) {
@@ -280,7 +382,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
     if (m.n_real < (uint64_t)k) return false;
     float thr = thr0;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
-    res.leaves = res.nodes = res.selects = 0;
+    res.leaves = res.nodes = res.selects = res.clipped = 0;
     // A carried bound can only fail through a degenerate previous result (a clipped
     // boundary band); the search is then repeated without it.
     for (int attempt = 0; attempt < 2; ++attempt) {
@@ -326,75 +428,47 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
             }
             const int f = __ffs(okm) - 1;
             const uint32_t etop = __shfl_sync(0xffffffffu, e, f);
+            sp -= f + 1;
+            __syncwarp();
             if ((etop >> 29) == 0) {
-                // leaves: the valid leaf entries above the first valid node entry, at most
-                // kLeafBatch and as many as the buffer has room for
-                const unsigned leafm = __ballot_sync(0xffffffffu, ok && (e >> 29) == 0);
-                const unsigned nodem = okm & ~leafm;
-                unsigned takem = nodem ? (leafm & ((1u << (__ffs(nodem) - 1)) - 1u)) : leafm;
-                const int room = (kCap - cnt) >> 5;
-                const int want = room < kLeafBatch ? room : kLeafBatch;
-                uint32_t leaf[kLeafBatch];
-                int nt = 0, last = f;
-#pragma unroll
-                for (int t = 0; t < kLeafBatch; ++t) {
-                    leaf[t] = 0u;
-                    if (t < want && takem) {
-                        const int ln = __ffs(takem) - 1;
-                        takem &= takem - 1u;
-                        leaf[t] = __shfl_sync(0xffffffffu, e, ln);
-                        last = ln;
-                        ++nt;
+                // a leaf: admit its points within the threshold
+                ++res.leaves;
+                const uint64_t r = (uint64_t)etop * 32 + l;
+                const bool real = r < m.n;  // the last leaf may be partial
+                float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (real) p = m.a[r];
+                const float d = real ? point_dist2(fx, fy, fz, lx, ly, lz, p) : FLT_MAX;
+                const bool take = real && d <= thr;
+                const unsigned b = __ballot_sync(0xffffffffu, take);
+                if (take) {
+                    const int pos = cnt + __popc(b & lanemask_lt());
+                    s.ci[pos] = (uint32_t)r;
+                    if (REFINE) {
+                        float hi, lo;
+                        point_dist2_df(fx, fy, fz, lx, ly, lz, p, hi, lo);
+                        s.cd[pos] = hi;
+                        s.cl[pos] = frac16(hi, lo);
+                    } else {
+                        s.cd[pos] = d;
                     }
                 }
-                if (nt == 0) {  // no room (only after pathological ties): drop the entry
-                    sp -= f + 1;
-                    __syncwarp();
-                    continue;
-                }
-                sp -= last + 1;
-                __syncwarp();
-                float4 p[kLeafBatch];
-#pragma unroll
-                for (int t = 0; t < kLeafBatch; ++t) {
-                    const uint64_t r = (uint64_t)leaf[t] * 32 + l;
-                    p[t] = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
-                    if (t < nt && r < m.n) p[t] = m.a[r];
-                }
-#pragma unroll
-                for (int t = 0; t < kLeafBatch; ++t) {
-                    if (t < nt) {
-                        const uint64_t r = (uint64_t)leaf[t] * 32 + l;
-                        const bool real = r < m.n;  // the last leaf may be partial
-                        const float d = real ? point_dist2(fx, fy, fz, lx, ly, lz, p[t]) : FLT_MAX;
-                        const bool take = real && d <= thr;
-                        const unsigned b = __ballot_sync(0xffffffffu, take);
-                        if (take) {
-                            float hi, lo;
-                            point_dist2_df(fx, fy, fz, lx, ly, lz, p[t], hi, lo);
-                            const int pos = cnt + __popc(b & lanemask_lt());
-                            s.cd[pos] = hi;
-                            s.ci[pos] = (uint32_t)r;
-                            s.cl[pos] = frac16(hi, lo);
-                        }
-                        cnt += __popc(b);
-                    }
-                }
-                res.leaves += nt;
+                cnt += __popc(b);
                 __syncwarp();
                 if (cnt >= k && (thr == FLT_MAX || cnt > kSelectAt)) {
                     ++res.selects;
-                    const float kth = __uint_as_float((uint32_t)(warp_kth_key<4>(s, cnt, k) >> 16));
+                    const float kth = warp_kth32(s, 0, cnt, k);
                     thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
-                    // refined distances within one float32 ulp of the k-th can still rank
-                    // among the k nearest; nothing beyond can
-                    cnt = warp_compact(s, cnt, __uint_as_float(__float_as_uint(kth) + 1u));
-                    if (cnt > kCap - 32) cnt = warp_compact(s, cnt, kth);  // mass ties
+                    // REFINE: refined distances within one float32 ulp of the k-th can still
+                    // rank among the k nearest, nothing beyond can; otherwise the float32
+                    // screening margin decides
+                    cnt = warp_compact(s, cnt, REFINE ? __uint_as_float(__float_as_uint(kth) + 1u) : thr);
+                    if (cnt > kCap - 32) {  // mass ties
+                        cnt = warp_compact(s, cnt, kth);
+                        res.clipped = 1;
+                    }
                     if (cnt > kCap - 32) cnt = kCap - 32;  // keeps the buffer in bounds
                 }
             } else {
-                sp -= f + 1;
-                __syncwarp();
                 ++res.nodes;
                 const int lev = (int)(etop >> 29);
                 const uint32_t node = etop & 0x1fffffffu;
@@ -433,67 +507,59 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         }
         if (cnt >= k || thr0 == FLT_MAX) break;
     }
-    // final: the k-th 48-bit key; keys more than one unit below it are in, keys within one
-    // unit of it are ranked in float64
-    const uint64_t K = warp_kth_key<6>(s, cnt, k);
-    int n_in = 0, n_band = 0;
-    for (int base = 0; base < cnt; base += 32) {
-        int i = base + l;
-        const bool valid = i < cnt;
-        const uint64_t key = valid ? cand_key(s, i) : ~0ull;
-        uint32_t id = valid ? s.ci[i] : 0u;
-        bool in = valid && key + 1ull < K;
-        bool band = valid && !in && key <= K + 1ull;
-        unsigned bin = __ballot_sync(0xffffffffu, in);
-        unsigned bb = __ballot_sync(0xffffffffu, band);
-        __syncwarp();
-        if (in) s.ci[n_in + __popc(bin & lanemask_lt())] = id;
-        if (band) {
-            int pos = n_band + __popc(bb & lanemask_lt());
-            if (pos < kBand) {
-                s.bi[pos] = id;
-                s.bt[pos] = tie_rec ? record_tie_key(m.a[id], tie_rec[id]) : 0ull;
-                s.bd[pos] = point_dist2_f64(qx, qy, qz, m.a[id]);
+    double rk2;
+    if (REFINE) {
+        rk2 = select_refined(m, s, 0, cnt, k, qx, qy, qz, tie_rec, res.clipped);
+    } else {
+        // float32 k-th; entries clearly below it are in, the band within the screening
+        // margin around it is resolved exactly (refined keys when it is crowded)
+        const float kth = warp_kth32(s, 0, cnt, k);
+        const float blo = kth * (1.0f - 2.0f * kRelMargin), bhi = kth * (1.0f + 2.0f * kRelMargin);
+        int n_in = 0, n_band = 0;
+        for (int base = 0; base < cnt; base += 32) {
+            const int i = base + l;
+            const bool valid = i < cnt;
+            const float d = valid ? s.cd[i] : FLT_MAX;
+            const uint32_t id = valid ? s.ci[i] : 0u;
+            const bool in = valid && d < blo;
+            const bool band = valid && d >= blo && d <= bhi;
+            const unsigned bin = __ballot_sync(0xffffffffu, in);
+            const unsigned bb = __ballot_sync(0xffffffffu, band);
+            __syncwarp();
+            if (in) s.ci[n_in + __popc(bin & lanemask_lt())] = id;
+            if (band) {
+                const int pos = n_band + __popc(bb & lanemask_lt());
+                if (pos < kStack) s.stk[pos] = id;  // the stack is free after the search
             }
+            n_in += __popc(bin);
+            n_band += __popc(bb);
+            __syncwarp();
         }
-        n_in += __popc(bin);
-        n_band += __popc(bb);
-        __syncwarp();
-    }
-    if (n_band > kBand) n_band = kBand;
-    int take = k - n_in;
-    // rank band entries by (float64 distance, tie key, map position); keep the `take`
-    // smallest, in rank order
-    // (kBand <= 32: one band entry per lane)
-    int rank = 0;
-    double di = 0.0;
-    uint32_t ii = 0;
-    if (l < n_band) {
-        di = s.bd[l];
-        ii = s.bi[l];
-        const uint64_t ti = s.bt[l];
-        for (int j = 0; j < n_band; ++j) {
-            const double dj = s.bd[j];
-            const uint64_t tj = s.bt[j];
-            rank += (dj < di || (dj == di && (tj < ti || (tj == ti && s.bi[j] < ii)))) ? 1 : 0;
+        if (n_band > kStack) {
+            n_band = kStack;
+            res.clipped = 1;
+        }
+        const int take = k - n_in;
+        if (n_band <= kBand) {
+            if (l < n_band) s.bi[l] = s.stk[l];
+            __syncwarp();
+            rk2 = rank_band(m, s, n_in, n_band, take, qx, qy, qz, tie_rec);
+        } else {
+            for (int j = l; j < n_band; j += 32) {
+                const uint32_t id = s.stk[j];
+                float hi, lo;
+                point_dist2_df(fx, fy, fz, lx, ly, lz, m.a[id], hi, lo);
+                s.cd[n_in + j] = hi;
+                s.cl[n_in + j] = frac16(hi, lo);
+                s.ci[n_in + j] = id;
+            }
+            __syncwarp();
+            rk2 = select_refined(m, s, n_in, n_band, take, qx, qy, qz, tie_rec, res.clipped);
         }
     }
-    __syncwarp();
-    const bool kth_lane = l < n_band && rank == take - 1;
-    if (l < n_band && rank < take) s.hist[rank] = ii;  // reuse as the taken list, ordered by rank
-    // broadcast the k-th distance from the lane that holds rank take-1
-    const unsigned owner = __ballot_sync(0xffffffffu, kth_lane);
-    const double rk2 = owner ? __shfl_sync(0xffffffffu, di, __ffs(owner) - 1) : 0.0;
-    res.n_in = n_in;
-    res.n_band_take = take;
     res.rk2 = rk2;
     res.rkf = sqrt_to_f32(rk2);
-    __syncwarp();
     return true;
-}
-
-ALB_DEVICE uint32_t knn_index(const WarpSmem& s, const KnnResult& r, int j) {
-    return j < r.n_in ? s.ci[j] : s.hist[j - r.n_in];
 }
 
 // ----------------------------------------------------------------------------------------
@@ -631,7 +697,8 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
                 if (t < 1.0e37f) thr0 = t;
             }
             KnnResult r;
-            if (!warp_knn(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0, m.b, r)) {
+            if (!warp_knn<CHANNEL != ALB_SCATTER>(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0,
+                                                   m.b, r)) {
                 if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
                 failed = true;
                 break;
@@ -641,6 +708,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
             pz = qz;
             prk = r.rkf;
             if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
+            if (q.inexact && r.clipped && l == 0) atomicAdd(q.inexact, 1ull);
             if (q.stats && l == 0) {
                 atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
                 atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
@@ -660,38 +728,19 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
             if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
             // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
             const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
-            // neighbour records are fetched for kWeightBatch rounds of 32 before any is used,
-            // so their loads overlap
-            for (int j0 = 0; j0 < k; j0 += 32 * kWeightBatch) {
-                float nE[kWeightBatch];
-                float4 nb[kWeightBatch];
-#pragma unroll
-                for (int t = 0; t < kWeightBatch; ++t) {
-                    const int j = j0 + 32 * t + l;
-                    nE[t] = 0.f;
-                    nb[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (j < k) {
-                        const uint32_t idx = knn_index(s, r, j);
-                        nE[t] = __ldg(&m.a[idx].w);
-                        nb[t] = __ldg(&m.b[idx]);
-                    }
-                }
-#pragma unroll
-                for (int t = 0; t < kWeightBatch; ++t) {
-                    const int j = j0 + 32 * t + l;
-                    if (j >= k) continue;
-                    const float4 pb = nb[t];
-                    float w;
-                    if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
-                    else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
-                    else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
-                    float c = ((Es * nE[t]) * norm) * w;
-                    int bin = (int)((ts + pb.w) / (float)sc.mult);
-                    if (bin >= 0 && bin < acc.nbins) {
-                        bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-                    } else {
-                        atomicCAS(err, 0, ALB_ERR_CAPACITY);
-                    }
+            for (int j = l; j < k; j += 32) {
+                const uint32_t idx = s.ci[j];
+                const float4 pb = m.b[idx];
+                float w;
+                if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+                else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+                else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+                const float c = ((Es * m.a[idx].w) * norm) * w;
+                const int bin = (int)((ts + pb.w) / (float)sc.mult);
+                if (bin >= 0 && bin < acc.nbins) {
+                    bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                } else {
+                    atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }
             }
             if (acc.hw_lo && m.fwi) {
@@ -699,7 +748,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
                 // non-unrolled pass: heatmaps are off in production runs)
 #pragma unroll 1
                 for (int j = l; j < k; j += 32) {
-                    const uint32_t idx = knn_index(s, r, j);
+                    const uint32_t idx = s.ci[j];
                     const float4 pb = m.b[idx];
                     float w;
                     if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
@@ -747,18 +796,18 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const doubl
         double qx = qs[3 * qi], qy = qs[3 * qi + 1], qz = qs[3 * qi + 2];
         KnnResult r;
         const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
-        if (!warp_knn(m, s, k, qx, qy, qz, fx, fy, fz, (float)(qx - (double)fx), (float)(qy - (double)fy),
+        if (!warp_knn<true>(m, s, k, qx, qy, qz, fx, fy, fz, (float)(qx - (double)fx), (float)(qy - (double)fy),
                       (float)(qz - (double)fz), FLT_MAX, nullptr, r)) {
             if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
             return;
         }
         // float64 distances of the k neighbours, then rank-sort them (k <= kMaxK)
         for (int j = l; j < k; j += 32) {
-            uint32_t idx = knn_index(s, r, j);
+            uint32_t idx = s.ci[j];
             double d = point_dist2_f64(qx, qy, qz, m.a[idx]);
             int rank = 0;
             for (int t = 0; t < k; ++t) {
-                uint32_t it = knn_index(s, r, t);
+                uint32_t it = s.ci[t];
                 double dt = point_dist2_f64(qx, qy, qz, m.a[it]);
                 rank += (dt < d || (dt == d && it < idx)) ? 1 : 0;
             }

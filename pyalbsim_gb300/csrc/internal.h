@@ -80,7 +80,8 @@ struct QueryDev {
     const uint32_t* perm;  // optional processing order
     uint64_t n;
     double* rk_out;    // optional per-query k-th neighbour distance
-    unsigned long long* stats;  // optional [leaves, nodes, selects, queries] accumulators
+    unsigned long long* stats;    // optional [leaves, nodes, selects, queries] accumulators
+    unsigned long long* inexact;  // optional count of answers a buffer bound made inexact (mass ties)
 };
 
 // Waveform / heatmap accumulators (128-bit fixed point, lo and hi words).
