@@ -165,13 +165,13 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large", choices=["large", "small"])
     ap.add_argument("--photons", type=float, default=1e8, help="forward photons per step (backward = 1/4)")
-    ap.add_argument("--ref-photons", type=int, default=4000)
-    ap.add_argument("--cpu-sample", type=int, default=4000)
+    ap.add_argument("--ref-photons", type=int, default=20000)
+    ap.add_argument("--cpu-sample", type=int, default=40000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--precise", action="store_true", help="float64-geometry tracer instead of the float32 one")
     args = ap.parse_args()
@@ -258,6 +258,10 @@ def main():
         "clocks": clk.summary(),
         "waveform_total": float(wf.sum()),
     }
+    # the timed context holds the full photon maps: free it before the end-to-end run,
+    # which builds its own
+    eng.close()
+    eng = None
     if rank == 0:
         # CPU baseline: the oracle on a bounded sample of the same workload, all host threads
         threads = os.cpu_count() or 1
@@ -269,7 +273,6 @@ def main():
         if not args.no_e2e:
             line["e2e"] = e2e_measure(cfg, nf, nb)
         print(json.dumps(line), flush=True)
-    eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

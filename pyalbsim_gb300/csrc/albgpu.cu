@@ -63,7 +63,7 @@ static void* grow(void* old, uint64_t& cap, uint64_t n, size_t elem, bool& faile
         cudaDeviceSynchronize();
         cudaFree(old);
     }
-    uint64_t want = std::max<uint64_t>(n + n / 8, 256);
+    uint64_t want = std::max<uint64_t>(n + n / 32, 256);
     void* p = nullptr;
     if (cudaMalloc(&p, want * elem) != cudaSuccess) {
         cudaGetLastError();
@@ -98,6 +98,9 @@ struct AlbCtx {
     double rec_rate[ALB_CHANNELS] = {2.0, 8.0, 1.05, 1.05};
     MapIndex map[ALB_CHANNELS];
     bool maps_built = false;
+    // records of a channel live either in its append store or, once indexed, only in the
+    // index (the store is released to make room; restored if more records are appended)
+    bool rec_released[ALB_CHANNELS] = {false, false, false, false};
     // backward queries
     float4* qa[3] = {nullptr, nullptr, nullptr};
     float4* qb[3] = {nullptr, nullptr, nullptr};
@@ -369,12 +372,15 @@ extern "C" int alb_set_option(AlbCtx* ctx, int key, int64_t v) {
 }
 
 // grow a record store to hold `need` records, preserving the first `keep`
+// backward photons traced and gathered per chunk when no per-photon state is exported
+constexpr uint64_t kBackwardChunk = 1ull << 22;
+
 static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
     RecordStore& r = ctx->rec[c];
     bool want_hm = ctx->sc.heatmap != 0;
     bool want_id = ctx->keep_ids != 0;
     if (r.cap >= need && (!want_id || r.id) && (!want_hm || r.fwi)) return ALB_OK;
-    uint64_t cap = std::max<uint64_t>(need + need / 4, 1024);
+    uint64_t cap = std::max<uint64_t>(need + need / 16, 1024);
     float4 *a, *b, *fwi = nullptr, *sfi = nullptr;
     uint32_t* id = nullptr;
     CK(cudaMalloc(&a, cap * 16));
@@ -396,6 +402,34 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
     CK(cudaStreamSynchronize(ctx->st));
     cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id);
     r.a = a; r.b = b; r.fwi = fwi; r.sfi = sfi; r.id = id; r.cap = cap;
+    return ALB_OK;
+}
+
+static void release_records(AlbCtx* ctx, int c) {
+    RecordStore& r = ctx->rec[c];
+    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id);
+    r = RecordStore{};
+}
+
+// Bring a channel's records back into an append store (from its index) before appending.
+static int restore_records(AlbCtx* ctx, int c, uint64_t need) {
+    if (!ctx->rec_released[c]) return ALB_OK;
+    const uint64_t n = ctx->h_rec_count[c];
+    int rc = ensure_records(ctx, c, need, 0);
+    if (rc) return rc;
+    const MapIndex& m = ctx->map[c];
+    RecordStore& r = ctx->rec[c];
+    if (n) {
+        CK(cudaMemcpyAsync(r.a, m.a, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        CK(cudaMemcpyAsync(r.b, m.b, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        if (r.fwi && m.fwi) {
+            CK(cudaMemcpyAsync(r.fwi, m.fwi, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
+            CK(cudaMemcpyAsync(r.sfi, m.sfi, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        }
+        if (r.id && m.id) CK(cudaMemcpyAsync(r.id, m.id, n * 4, cudaMemcpyDeviceToDevice, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    ctx->rec_released[c] = false;
     return ALB_OK;
 }
 
@@ -510,9 +544,10 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         size_t hb = ctx->sc.heatmap ? (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins : 0;
         for (int attempt = 0; attempt < 3; ++attempt) {
             for (int c = 0; c < ALB_CHANNELS; ++c) {
-                uint64_t est = (uint64_t)(ctx->rec_rate[c] * (double)n * 1.2) + 4096;
+                uint64_t est = (uint64_t)(ctx->rec_rate[c] * (double)n * 1.03) + 4096;
                 if (ctx->map_cap_hint > 0) est = std::max<uint64_t>(est, (uint64_t)ctx->map_cap_hint);
-                int rc = ensure_records(ctx, c, before[c] + est, before[c]);
+                int rc = ctx->rec_released[c] ? restore_records(ctx, c, before[c] + est)
+                                               : ensure_records(ctx, c, before[c] + est, before[c]);
                 if (rc) return rc;
             }
             if (hb && attempt == 0) {
@@ -546,35 +581,9 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         }
         return fail(ctx, ALB_ERR_CAPACITY, "photon-map capacity could not be established");
     }
-    // backward: trace -> queries -> gathers
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        for (int k = 0; k < 3; ++k) {
-            uint64_t est = (uint64_t)(ctx->q_rate[k] * (double)n * 1.2) + 4096;
-            int rc = ensure_queries(ctx, k, est);
-            if (rc) return rc;
-        }
-        CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
-        TraceOut o = make_out(ctx);
-        PhaseTimer pt(ctx, 2);
-        launch_trace(ctx->sc, o, ALB_BACKWARD, n, first, seed, rp ? &drp : nullptr, &ctx->launches, ctx->st,
-                         ctx->precise ? nullptr : &ctx->fast);
-        pt.stop();
-        int rc = check_device(ctx, "backward trace");
-        if (rc) return rc;
-        unsigned long long cnt[3];
-        CK(cudaMemcpy(cnt, ctx->d_q_count, sizeof cnt, cudaMemcpyDeviceToHost));
-        bool overflow = false;
-        for (int k = 0; k < 3; ++k) {
-            if (n > 0) ctx->q_rate[k] = std::max(ctx->q_rate[k] * 0.5, (double)cnt[k] / (double)n);
-            if (cnt[k] > ctx->qcap[k]) overflow = true;
-            ctx->h_q_count[k] = cnt[k];
-        }
-        if (!overflow) break;
-        for (int k = 0; k < 3; ++k) ctx->q_rate[k] = (double)cnt[k] / (double)n;
-        if (attempt == 2) return fail(ctx, ALB_ERR_CAPACITY, "query capacity could not be established");
-    }
-    int rc = check_map_sizes(ctx);
-    if (rc) return rc;
+    // backward: trace -> queries -> gathers. Without per-photon exports the photons go in
+    // chunks, so that query buffers stay bounded whatever n is (the waveform sums are
+    // integer and order independent, so chunking cannot change the result).
     Accum acc{};
     acc.wf_lo = ctx->wf;
     acc.wf_hi = ctx->wf + (size_t)ALB_CHANNELS * ctx->sc.nbins;
@@ -586,34 +595,70 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         acc.hf_lo = ctx->hm + 2 * hb;
         acc.hf_hi = ctx->hm + 3 * hb;
     }
-    static const int kinds[4] = {kQueryBottom, kQueryScatter, kQuerySurface, kQuerySurface};
-    static const int chans[4] = {ALB_BOTTOM_REFLECTION, ALB_SCATTER, ALB_SURFACE_REFLECTION, ALB_SURFACE_TRANSMISSION_UP};
-    for (int g = 0; g < 4; ++g) {
-        int k = kinds[g], c = chans[g];
-        uint64_t nq = ctx->h_q_count[k];
-        if (nq == 0) continue;
-        QueryDev q{};
-        q.a = ctx->qa[k];
-        q.b = ctx->qb[k];
-        q.c = ctx->qc[k];
-        q.n = nq;
-        q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
-        q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
-        q.inexact = ctx->d_stats + 24 + c;
-        if (ctx->sort_q) {
-            PhaseTimer ps(ctx, 3);
-            sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
-            ps.stop();
-            q.perm = ctx->qperm[k];
+    const bool chunked = !ctx->keep_exit && !ctx->keep_ids && !rp;
+    const uint64_t chunk = chunked ? kBackwardChunk : std::max<uint64_t>(n, 1);
+    for (uint64_t c0 = 0; c0 == 0 || c0 < n; c0 += chunk) {
+        const uint64_t nc = std::min<uint64_t>(chunk, n - c0);
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            for (int k = 0; k < 3; ++k) {
+                uint64_t est = (uint64_t)(ctx->q_rate[k] * (double)nc * 1.1) + 4096;
+                int rc = ensure_queries(ctx, k, est);
+                if (rc) return rc;
+            }
+            CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
+            TraceOut o = make_out(ctx);
+            PhaseTimer pt(ctx, 2);
+            launch_trace(ctx->sc, o, ALB_BACKWARD, nc, first + c0, seed, rp ? &drp : nullptr, &ctx->launches,
+                         ctx->st, ctx->precise ? nullptr : &ctx->fast);
+            pt.stop();
+            int rc = check_device(ctx, "backward trace");
+            if (rc) return rc;
+            unsigned long long cnt[3];
+            CK(cudaMemcpy(cnt, ctx->d_q_count, sizeof cnt, cudaMemcpyDeviceToHost));
+            bool overflow = false;
+            for (int k = 0; k < 3; ++k) {
+                if (nc > 0) ctx->q_rate[k] = std::max(ctx->q_rate[k] * 0.5, (double)cnt[k] / (double)nc);
+                if (cnt[k] > ctx->qcap[k]) overflow = true;
+                ctx->h_q_count[k] = cnt[k];
+            }
+            if (!overflow) break;
+            for (int k = 0; k < 3; ++k) ctx->q_rate[k] = (double)cnt[k] / (double)nc;
+            if (attempt == 2) return fail(ctx, ALB_ERR_CAPACITY, "query capacity could not be established");
         }
-        PhaseTimer pg(ctx, 4 + c);
-        launch_gather(ctx->sc, map_dev(ctx->map[c]), q, c, acc, ctx->d_err, &ctx->launches, ctx->st);
-        pg.stop();
-        ctx->gathered[c] += (int64_t)nq;
+        int rc = check_map_sizes(ctx);
+        if (rc) return rc;
+        static const int kinds[4] = {kQueryBottom, kQueryScatter, kQuerySurface, kQuerySurface};
+        static const int chans[4] = {ALB_BOTTOM_REFLECTION, ALB_SCATTER, ALB_SURFACE_REFLECTION,
+                                     ALB_SURFACE_TRANSMISSION_UP};
+        for (int g = 0; g < 4; ++g) {
+            int k = kinds[g], c = chans[g];
+            uint64_t nq = ctx->h_q_count[k];
+            if (nq == 0) continue;
+            QueryDev q{};
+            q.a = ctx->qa[k];
+            q.b = ctx->qb[k];
+            q.c = ctx->qc[k];
+            q.n = nq;
+            q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
+            q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
+            q.inexact = ctx->d_stats + 24 + c;
+            if (ctx->sort_q) {
+                PhaseTimer ps(ctx, 3);
+                sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
+                ps.stop();
+                q.perm = ctx->qperm[k];
+            }
+            PhaseTimer pg(ctx, 4 + c);
+            launch_gather(ctx->sc, map_dev(ctx->map[c]), q, c, acc, ctx->d_err, &ctx->launches, ctx->st);
+            pg.stop();
+            ctx->gathered[c] += (int64_t)nq;
+        }
+        rc = check_device(ctx, "gather");
+        if (rc) return rc;
+        if (n == 0) break;
     }
-    rc = check_device(ctx, "gather");
     ctx->ws.release(mark);
-    return rc;
+    return ALB_OK;
 }
 
 extern "C" int alb_build_maps(AlbCtx* ctx) {
@@ -621,8 +666,12 @@ extern "C" int alb_build_maps(AlbCtx* ctx) {
     CK(cudaSetDevice(ctx->device));
     PhaseTimer pt(ctx, 1);
     for (int c = 0; c < ALB_CHANNELS; ++c) {
+        if (ctx->rec_released[c]) continue;  // already indexed, nothing appended since
         if (build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st) != 0)
-            return fail(ctx, ALB_ERR_CAPACITY, "photon-map index build failed (cell partition)");
+            return fail(ctx, ALB_ERR_CAPACITY, "photon-map index build failed (device memory or partition)");
+        CK(cudaStreamSynchronize(ctx->st));
+        release_records(ctx, c);
+        ctx->rec_released[c] = true;
     }
     pt.stop();
     int rc = check_device(ctx, "map build");
@@ -645,8 +694,13 @@ extern "C" int alb_export_map(AlbCtx* ctx, int c, float* pos, float* dir, float*
     if (m == 0) return ALB_OK;
     const float4 *a, *b, *fw, *sf;
     const uint32_t* id;
-    // records in append order (the index holds them in k-d order with padding dummies)
-    a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
+    // records in append order, or in index order once the channel has been indexed
+    if (ctx->rec_released[c]) {
+        const MapIndex& mi = ctx->map[c];
+        a = mi.a; b = mi.b; id = mi.id; fw = mi.fwi; sf = mi.sfi;
+    } else {
+        a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
+    }
     std::vector<float4> ha(m), hb(m), hf, hs;
     CK(cudaMemcpy(ha.data(), a, m * 16, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hb.data(), b, m * 16, cudaMemcpyDeviceToHost));
@@ -746,10 +800,13 @@ extern "C" int alb_reset(AlbCtx* ctx) {
     CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
     if (ctx->hm_radius)
         CK(cudaMemsetAsync(ctx->hm_radius, 0, (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins * 4, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     for (int c = 0; c < ALB_CHANNELS; ++c) {
         ctx->h_rec_count[c] = 0;
+        release_map_index(ctx->map[c]);  // an empty simulation holds no index memory
         ctx->map[c].n = 0;
         ctx->map[c].n_real = 0;
+        ctx->rec_released[c] = false;
     }
     for (int k = 0; k < 3; ++k) ctx->h_q_count[k] = 0;
     ctx->maps_built = false;

@@ -125,6 +125,7 @@ int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*&
                      uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st);
 int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st);
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st);
+void release_map_index(MapIndex& m);
 int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st);
 int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, uint32_t* perm,
                  cudaStream_t st);

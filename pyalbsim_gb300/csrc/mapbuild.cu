@@ -738,12 +738,10 @@ __global__ void k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X
     }
 }
 
-// One node of <= kCellMax records X[start + j] (id in .w) per CTA: writes the record ids
-// of its exact left-balanced k-d order to out[start ..].
-__global__ void __launch_bounds__(kCellThreads) k_local_kd(const float4* __restrict__ Xin,
-                                                           const unsigned* __restrict__ cstart,
-                                                           const unsigned* __restrict__ ccount, uint32_t* out,
-                                                           unsigned* err) {
+// One node of <= kCellMax records X[start + j] (id in .w) per CTA, reordered in place into
+// its exact left-balanced k-d order (the CTA holds the whole node in shared memory).
+__global__ void __launch_bounds__(kCellThreads) k_local_kd(float4* X, const unsigned* __restrict__ cstart,
+                                                           const unsigned* __restrict__ ccount, unsigned* err) {
     extern __shared__ unsigned char smraw[];
     const CellSmem s = cell_smem(smraw);
     const unsigned cnt = ccount[blockIdx.x];
@@ -757,7 +755,7 @@ __global__ void __launch_bounds__(kCellThreads) k_local_kd(const float4* __restr
     const float qnan = __int_as_float(0x7fc00000);
     for (unsigned j = threadIdx.x; j < P; j += blockDim.x) {
         if (j < cnt) {
-            float4 p = Xin[s0 + j];
+            float4 p = X[s0 + j];
             s.X[j] = p.x; s.Y[j] = p.y; s.Z[j] = p.z; s.ID[j] = __float_as_uint(p.w);
         } else {
             s.X[j] = qnan; s.Y[j] = qnan; s.Z[j] = qnan; s.ID[j] = kDummy;
@@ -765,7 +763,8 @@ __global__ void __launch_bounds__(kCellThreads) k_local_kd(const float4* __restr
     }
     __syncthreads();
     cell_kd_sort(s, cnt);
-    for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) out[s0 + j] = s.ID[j];
+    for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x)
+        X[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
 }
 
 __global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) {
@@ -790,21 +789,25 @@ static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n
     enumerate_cells(a + left, c - left, depth + 1, D, n, st, ct);
 }
 
-// perm <- exact left-balanced k-d order (record ids) of the n records of `a`
+// out[i] <- (position, record id) of the i-th record of `a` in exact left-balanced k-d order.
+// `out` (n float4) is one of the two ping-pong buffers, so the build needs one temporary of
+// the same size besides it.
 static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float blo[3], const float bhi[3],
-                         uint32_t* perm, cudaStream_t st) {
+                         float4* out, cudaStream_t st) {
     const uint64_t L = (n + 31) / 32;
     int depth_max = L > 1 ? 64 - __builtin_clzll((unsigned long long)(L - 1)) : 0;
     const int local_levels = 7;  // kCellMax / 32 = 128 leaves = 2^7
     const int D = std::max(0, depth_max - local_levels);
     size_t mark = ws.mark();
-    float4* X = (float4*)ws.take_bytes(n * 16);
-    float4* X2 = (float4*)ws.take_bytes(n * 16);
+    float4* tmp = (float4*)ws.take_bytes(n * 16);
     unsigned* err = ws.take_u32(1);
-    if (!X || !X2 || !err) {
+    if (!tmp || !err) {
         ws.release(mark);
         return -1;
     }
+    // D partition levels swap the buffers D times: start so that the result lands in `out`
+    float4* X = (D % 2 == 0) ? out : tmp;
+    float4* X2 = (D % 2 == 0) ? tmp : out;
     cudaMemsetAsync(err, 0, 4, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
     k_pack_ids<<<blocks, 256, 0, st>>>(a, n, X);
@@ -879,7 +882,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         cudaFuncSetAttribute(k_local_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
         attr_set[dev] = true;
     }
-    k_local_kd<<<(unsigned)cs.size(), kCellThreads, cell_smem_bytes(), st>>>(X, dcs, dcc, perm, err);
+    k_local_kd<<<(unsigned)cs.size(), kCellThreads, cell_smem_bytes(), st>>>(X, dcs, dcc, err);
     note_launch();
     unsigned herr = 0;
     cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st);
@@ -1025,7 +1028,32 @@ int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float 
     return 0;
 }
 
-// Sort the records of one channel into Morton order and build the box tree.
+// a[i] holds (position, record id) in index order: gather every record field into index
+// order, a last (in place: each thread reads its id before overwriting the entry).
+__global__ void k_finalize(float4* a, float4* __restrict__ b, float4* __restrict__ fwi, float4* __restrict__ sfi,
+                           uint32_t* __restrict__ id, RecordStore rec, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = __float_as_uint(a[i].w);
+        b[i] = rec.b[r];
+        if (fwi) {
+            fwi[i] = rec.fwi[r];
+            sfi[i] = rec.sfi[r];
+        }
+        if (id) id[i] = rec.id[r];
+        a[i] = rec.a[r];
+    }
+}
+
+void release_map_index(MapIndex& m) {
+    cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id);
+    m.a = m.b = m.fwi = m.sfi = nullptr;
+    m.id = nullptr;
+    m.a_cap = m.b_cap = m.fwi_cap = m.sfi_cap = m.id_cap = 0;
+}
+
+// Build the k-d index of one channel's n records: records in exact left-balanced k-d order
+// over 32-record leaves, plus the box tree. The previous index arrays are released first,
+// so the peak is the record store plus two n-record float4 buffers.
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st) {
     m.n = n;
     m.n_real = n;
@@ -1033,40 +1061,27 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
         m.nlevels = 0;
         return 0;
     }
+    if (n >= (1ull << 32)) return -1;  // record ids are 32-bit
     float lo[3], hi[3];
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
-    size_t mark = ws.mark();
-    uint32_t* vals = ws.take_u32(n);
-    if (!vals || kd_order_fast(ws, rec.a, n, lo, hi, vals, st) != 0) {
-        ws.release(mark);
-        return -1;
-    }
-    const uint64_t np = n;
-    m.n_real = n;
-    m.n = np;
-    unsigned blocks = (unsigned)std::min<uint64_t>((np + 255) / 256, 8192);
-    m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, np);
-    m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, np);
-    k_permute4_pad<<<blocks, 256, 0, st>>>(rec.a, vals, m.a, np);
-    note_launch();
-    k_permute4_pad<<<blocks, 256, 0, st>>>(rec.b, vals, m.b, np);
-    note_launch();
+    cudaStreamSynchronize(st);
+    release_map_index(m);
+    m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
+    if (!m.a || kd_order_fast(ws, rec.a, n, lo, hi, m.a, st) != 0) return -1;
+    cudaStreamSynchronize(st);  // the build temporary is back in the pool
+    m.b = (float4*)ws.alloc_persistent(m.b, m.b_cap, n);
     if (rec.fwi) {
-        m.fwi = (float4*)ws.alloc_persistent(m.fwi, m.fwi_cap, np);
-        m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, np);
-        k_permute4_pad<<<blocks, 256, 0, st>>>(rec.fwi, vals, m.fwi, np);
-        note_launch();
-        k_permute4_pad<<<blocks, 256, 0, st>>>(rec.sfi, vals, m.sfi, np);
-        note_launch();
+        m.fwi = (float4*)ws.alloc_persistent(m.fwi, m.fwi_cap, n);
+        m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, n);
     }
-    if (rec.id) {
-        m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, np);
-        k_permute_u32_pad<<<blocks, 256, 0, st>>>(rec.id, vals, m.id, np);
-        note_launch();
-    }
+    if (rec.id) m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, n);
+    if (!m.b || (rec.fwi && (!m.fwi || !m.sfi)) || (rec.id && !m.id)) return -1;
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
+    k_finalize<<<blocks, 256, 0, st>>>(m.a, m.b, rec.fwi ? m.fwi : nullptr, rec.fwi ? m.sfi : nullptr,
+                                       rec.id ? m.id : nullptr, rec, n);
+    note_launch();
     build_box_tree(ws, m, st);
-    ws.release(mark);
     return 0;
 }
 
