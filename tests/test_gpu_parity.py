@@ -158,6 +158,39 @@ def test_knn_neighbour_sets_bit_exact(gpu_available):
         eng.close()
 
 
+@pytest.mark.parametrize("shape", ["cloud", "planar"])
+def test_knn_large_map_matches_kdtree(gpu_available, shape):
+    """Maps large enough for the streaming partition levels of the index build (3e6 points:
+    more than ten levels above the per-CTA cells): every query's k nearest match scipy's
+    cKDTree (float64 distances on the float32 points; sets agree except for exact ties at
+    the k-th distance). Includes far queries, whose neighbours crowd at nearly one distance."""
+    sp = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(11)
+    m, k = 3_000_000, 100
+    if shape == "cloud":
+        pts = rng.normal(scale=[0.4, 5.0, 0.4], size=(m, 3)) + [0.0, -410.0, 0.0]
+    else:
+        r = 0.4 * np.sqrt(rng.random(m))
+        a = 2 * np.pi * rng.random(m)
+        pts = np.stack([r * np.cos(a), np.full(m, -400.0), r * np.sin(a)], 1)
+    pts = pts.astype(np.float32)
+    near = pts[rng.integers(0, m, 1500)].astype(np.float64) + rng.normal(scale=0.05, size=(1500, 3))
+    far = np.stack([rng.uniform(-40, 40, 500), np.full(500, -400.0), rng.uniform(-40, 40, 500)], 1)
+    if shape == "cloud":
+        far[:, 1] = rng.uniform(-430, -390, 500)
+    qs = np.concatenate([near, far])
+    eng = GpuEngine(config_from_fixture(load("replay_small.npz")))
+    try:
+        dist, idx = eng.ctx.knn(pts, qs, k)
+    finally:
+        eng.close()
+    ref_d, ref_i = sp.cKDTree(pts.astype(np.float64)).query(qs, k)
+    np.testing.assert_allclose(dist, ref_d, rtol=1e-12, atol=0)
+    for i in range(len(qs)):
+        strict = set(ref_i[i][ref_d[i] < ref_d[i][-1]])
+        assert strict <= set(idx[i]), (shape, i)
+
+
 def _philox_run(cfg, nf, nb, seed, ids=True, precise=True):
     eng = _engine(cfg, ids=ids, exits=True, precise=precise)
     eng.forward(nf, seed)
