@@ -350,7 +350,11 @@ ALB_DEVICE void cell_kd_sort(const CellSmem& s, unsigned cnt) {
     while (P2 < P) P2 <<= 1;
     int depth = 0;
     while ((1u << depth) < Lc) ++depth;
+    // In a full cell of a power-of-two leaf count every node of level d is an aligned block
+    // of P >> d keys: sorting the blocks separately gives the same order as the full sort.
+    const bool perfect = cnt == P && (Lc & (Lc - 1)) == 0;
     for (int d = 0; d < depth; ++d) {
+        const unsigned S = perfect ? (P >> d) : P2;
         for (unsigned i = threadIdx.x; i < 3 * Lc; i += blockDim.x) {
             s.blo[i] = 0xffffffffu;
             s.bhi[i] = 0u;
@@ -390,13 +394,15 @@ ALB_DEVICE void cell_kd_sort(const CellSmem& s, unsigned cnt) {
             s.key[j] = k;
         }
         __syncthreads();
-        for (unsigned kk = 2; kk <= P2; kk <<= 1) {  // bitonic sort of P2 keys, ascending
+        // bitonic sort of every aligned block of S keys, ascending (the last merge of a block
+        // runs ascending everywhere)
+        for (unsigned kk = 2; kk <= S; kk <<= 1) {
             for (unsigned jj = kk >> 1; jj > 0; jj >>= 1) {
                 for (unsigned i = threadIdx.x; i < P2; i += blockDim.x) {
                     unsigned p = i ^ jj;
                     if (p > i) {
                         unsigned long long x = s.key[i], y = s.key[p];
-                        bool up = (i & kk) == 0;
+                        bool up = kk == S || (i & kk) == 0;
                         if ((x > y) == up) {
                             s.key[i] = y;
                             s.key[p] = x;
@@ -498,7 +504,19 @@ ALB_DEVICE void kd_node_path(uint64_t leaf, uint64_t L, int depth, uint64_t& a, 
     c = L;
     path = 0;
     reached = 0;
-    for (int i = 0; i < depth && c > 1; ++i) {
+    while (reached < depth && c > 1) {
+        if ((c & (c - 1)) == 0) {
+            // a perfect subtree of c = 2^e leaves: the remaining path is the leading bits of
+            // the leaf's offset in it
+            const int e = 63 - __clzll((long long)c);
+            const int take = min(depth - reached, e);
+            const uint64_t top = (leaf - a) >> (e - take);
+            path = (path << take) | (uint32_t)top;
+            a += top << (e - take);
+            c = 1ull << (e - take);
+            reached += take;
+            return;
+        }
         uint64_t left = 1ull << (63 - __clzll((long long)(c - 1)));
         if (leaf - a < left) {
             c = left;
@@ -558,23 +576,71 @@ ALB_DEVICE unsigned agg_inc(unsigned* cnt, uint64_t key, unsigned active) {
     return base + rank;
 }
 
-__global__ void k_kdl_hist1(const float4* __restrict__ X, uint64_t n, uint64_t L, int d, LevelNodes nb, unsigned* hist1) {
-    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
-         base += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t i = base + lane_id();
+// Level passes run persistent blocks over contiguous record ranges (records of a node are
+// contiguous, so a block meets few nodes at the upper levels, where global atomics would
+// collide): per-node counters live in kSlots tagged shared-memory slots, records of nodes
+// that find no slot go to global memory directly.
+constexpr int kLvlThreads = 256;
+constexpr int kSlots = 8;
+constexpr unsigned kNoTag = 0xffffffffu;
+
+// claim the slot of `key` (path or child id); returns the slot or -1
+ALB_DEVICE int slot_of(unsigned* tag, unsigned key) {
+    const int sl = (int)(key & (kSlots - 1));
+    unsigned t = tag[sl];
+    if (t == kNoTag) {
+        const unsigned old = atomicCAS(&tag[sl], kNoTag, key);
+        t = (old == kNoTag) ? key : old;
+    }
+    return t == key ? sl : -1;
+}
+
+// PASS 1: per node, 256-bin histogram of the top byte of the 16-bit coordinate.
+// PASS 2: per node, histogram of the low byte inside the bucket holding the cut.
+template <int PASS>
+__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restrict__ X, uint64_t n, uint64_t L,
+                                                          int d, LevelNodes nb, const uint2* __restrict__ sel,
+                                                          unsigned* hist, uint64_t per) {
+    __shared__ unsigned tag[kSlots];
+    __shared__ unsigned sh[kSlots * 256];
+    for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) sh[j] = 0u;
+    if (threadIdx.x < kSlots) tag[threadIdx.x] = kNoTag;
+    __syncthreads();
+    const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
+    for (uint64_t base = r0 + (threadIdx.x & ~31u); base < r1; base += blockDim.x) {
+        const uint64_t i = base + lane_id();
         bool act = false;
         uint32_t path = 0, h = 0;
-        if (i < n) {
+        if (i < r1) {
             uint64_t a, c;
             int r;
             kd_node_path(i / 32, L, d, a, c, path, r);
             if (r == d && c > 1) {
-                act = true;
-                h = kd_quant16(X[i], nb.lo, nb.hi, path) >> 8;
+                const uint32_t q = kd_quant16(X[i], nb.lo, nb.hi, path);
+                if (PASS == 1) {
+                    act = true;
+                    h = q >> 8;
+                } else if ((q >> 8) == sel[path].x) {
+                    act = true;
+                    h = q & 255u;
+                }
             }
         }
-        unsigned am = __ballot_sync(0xffffffffu, act);
-        if (act) agg_inc(hist1 + (uint64_t)path * 256 + h, (uint64_t)path * 256 + h, am);
+        const unsigned am = __ballot_sync(0xffffffffu, act);
+        if (act) {
+            const unsigned key = (path << 8) | h;
+            const unsigned peers = __match_any_sync(am, key);
+            if ((int)lane_id() == __ffs(peers) - 1) {
+                const int sl = slot_of(tag, path);
+                if (sl >= 0) atomicAdd(&sh[sl * 256 + h], (unsigned)__popc(peers));
+                else atomicAdd(hist + (uint64_t)path * 256 + h, (unsigned)__popc(peers));
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) {
+        const unsigned t = tag[j >> 8];
+        if (t != kNoTag && sh[j]) atomicAdd(hist + (uint64_t)t * 256 + (j & 255), sh[j]);
     }
 }
 
@@ -622,30 +688,6 @@ __global__ void k_kdl_select1(const unsigned* __restrict__ hist1, uint64_t L, in
     if (l == 0) sel[w] = make_uint2((unsigned)bucket, need - below);
 }
 
-__global__ void k_kdl_hist2(const float4* __restrict__ X, uint64_t n, uint64_t L, int d, LevelNodes nb,
-                            const uint2* __restrict__ sel, unsigned* hist2) {
-    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
-         base += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t i = base + lane_id();
-        bool act = false;
-        uint32_t path = 0, h = 0;
-        if (i < n) {
-            uint64_t a, c;
-            int r;
-            kd_node_path(i / 32, L, d, a, c, path, r);
-            if (r == d && c > 1) {
-                uint32_t q = kd_quant16(X[i], nb.lo, nb.hi, path);
-                if ((q >> 8) == sel[path].x) {
-                    act = true;
-                    h = q & 255u;
-                }
-            }
-        }
-        unsigned am = __ballot_sync(0xffffffffu, act);
-        if (act) agg_inc(hist2 + (uint64_t)path * 256 + h, (uint64_t)path * 256 + h, am);
-    }
-}
-
 // one warp per node: the 16-bit cut value and how many records AT it go left
 __global__ void k_kdl_select2(const unsigned* __restrict__ hist2, uint32_t nodes, const uint2* __restrict__ sel,
                               uint2* cut) {
@@ -689,51 +731,138 @@ __global__ void k_kdl_select2(const unsigned* __restrict__ hist2, uint32_t nodes
     if (l == 0) cut[w] = make_uint2((s.x << 8) | (unsigned)(sub < 0 ? 0 : sub), need - below);
 }
 
-__global__ void k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2, uint64_t n, uint64_t L, int d,
-                            LevelNodes nb, const uint2* __restrict__ cut, unsigned* cursors, unsigned* ties,
-                            unsigned* clo, unsigned* chi, unsigned* err) {
-    for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
-         base += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t i = base + lane_id();
-        bool valid = i < n;
-        bool moves = false;
-        uint32_t path = 0;
-        uint64_t a = 0, c = 0, left = 0;
-        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-        unsigned side = 0;
-        if (valid) {
-            int r;
-            kd_node_path(i / 32, L, d, a, c, path, r);
-            p = X[i];
-            if (r == d && c > 1) {
-                moves = true;
-                left = 1ull << (63 - __clzll((long long)(c - 1)));
-                uint2 ct = cut[path];
-                uint32_t q = kd_quant16(p, nb.lo, nb.hi, path);
-                if (q < ct.x) side = 0;
-                else if (q > ct.x) side = 1;
-                else side = (atomicAdd(ties + path, 1u) < ct.y) ? 0u : 1u;
-            } else {
-                X2[i] = p;  // already a leaf: stays
+// Every record goes left or right of its node's cut into X2. A tile of kSplitItems records
+// per thread is read once; per tile, shared counters per (node slot, side) give each record
+// its rank and one global atomic per (node, side) reserves the tile's range. The children's
+// boxes (for the next level's axis choice) are reduced in shared memory over the block's
+// whole range and flushed once.
+constexpr int kSplitItems = 4;
+
+__global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
+                                                           uint64_t n, uint64_t L, int d, LevelNodes nb,
+                                                           const uint2* __restrict__ cut, unsigned* cursors,
+                                                           unsigned* ties, unsigned* clo, unsigned* chi,
+                                                           unsigned* err, uint64_t per) {
+    __shared__ unsigned ntag[kSlots];           // node slots of the current tile
+    __shared__ unsigned ncnt[kSlots * 2];       // records per (slot, side) in the tile
+    __shared__ unsigned nbase[kSlots * 2];      // their global start (cursor reservation)
+    __shared__ unsigned btag[kSlots];           // child slots (whole block range)
+    __shared__ unsigned bmin[kSlots * 3], bmax[kSlots * 3];
+    if (threadIdx.x < kSlots) btag[threadIdx.x] = kNoTag;
+    for (int j = threadIdx.x; j < kSlots * 3; j += blockDim.x) {
+        bmin[j] = 0xffffffffu;
+        bmax[j] = 0u;
+    }
+    const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
+    const uint64_t tile = (uint64_t)kSplitItems * blockDim.x;
+    for (uint64_t t0 = r0; t0 < r1; t0 += tile) {
+        if (threadIdx.x < kSlots) ntag[threadIdx.x] = kNoTag;
+        if (threadIdx.x < kSlots * 2) ncnt[threadIdx.x] = 0u;
+        __syncthreads();
+        float4 p[kSplitItems];
+        uint64_t dst0[kSplitItems];  // start of the record's child range
+        uint64_t dend[kSplitItems];  // end of that range (bounds check)
+        uint32_t path[kSplitItems], rank[kSplitItems];
+        int code[kSplitItems];       // slot * 2 + side while the tile reservation is pending, else -1
+#pragma unroll
+        for (int t = 0; t < kSplitItems; ++t) {
+            const uint64_t i = t0 + (uint64_t)t * blockDim.x + threadIdx.x;
+            code[t] = -1;
+            dst0[t] = 0;
+            dend[t] = 0;
+            path[t] = 0;
+            rank[t] = 0;
+            bool moves = false;
+            unsigned side = 0;
+            uint64_t a = 0, c = 0, left = 0;
+            if (i < r1) {
+                int r;
+                kd_node_path(i / 32, L, d, a, c, path[t], r);
+                p[t] = X[i];
+                if (r == d && c > 1) {
+                    moves = true;
+                    left = 1ull << (63 - __clzll((long long)(c - 1)));
+                    const uint2 ct = cut[path[t]];
+                    const uint32_t q = kd_quant16(p[t], nb.lo, nb.hi, path[t]);
+                    if (q < ct.x) side = 0;
+                    else if (q > ct.x) side = 1;
+                    else side = (atomicAdd(ties + path[t], 1u) < ct.y) ? 0u : 1u;
+                    dst0[t] = a * 32 + (side ? left * 32 : 0);
+                    dend[t] = side ? min((a + c) * 32, n) : (a + left) * 32;
+                } else {
+                    X2[i] = p[t];  // already in place (a leaf of an earlier level)
+                }
+            }
+            // per-warp aggregation of (path, side) for the tile counters
+            const unsigned am = __ballot_sync(0xffffffffu, moves);
+            if (moves) {
+                const unsigned key = (path[t] << 1) | side;
+                const unsigned peers = __match_any_sync(am, key);
+                const int leader = __ffs(peers) - 1;
+                const unsigned lrank = __popc(peers & lanemask_lt());
+                unsigned b = 0;
+                int cd = -1;
+                if ((int)lane_id() == leader) {
+                    const int sl = slot_of(ntag, path[t]);
+                    if (sl >= 0) {
+                        cd = sl * 2 + (int)side;
+                        b = atomicAdd(&ncnt[cd], (unsigned)__popc(peers));
+                    } else {
+                        b = atomicAdd(cursors + 2 * (uint64_t)path[t] + side, (unsigned)__popc(peers));
+                    }
+                }
+                cd = __shfl_sync(peers, cd, leader);
+                b = __shfl_sync(peers, b, leader);
+                code[t] = cd;
+                rank[t] = b + lrank;
+                if (cd < 0) {  // global cursor: final position known now
+                    const uint64_t dst = dst0[t] + rank[t];
+                    if (dst < dend[t]) X2[dst] = p[t];
+                    else atomicOr(err, 1u);
+                }
+                // child box: shared slots per child id, global otherwise
+                const unsigned child = (path[t] << 1) | side;
+                const unsigned cpeers = __match_any_sync(am, child);
+                const unsigned ox = f2ord(p[t].x), oy = f2ord(p[t].y), oz = f2ord(p[t].z);
+                const unsigned mnx = __reduce_min_sync(cpeers, ox), mny = __reduce_min_sync(cpeers, oy),
+                               mnz = __reduce_min_sync(cpeers, oz);
+                const unsigned mxx = __reduce_max_sync(cpeers, ox), mxy = __reduce_max_sync(cpeers, oy),
+                               mxz = __reduce_max_sync(cpeers, oz);
+                if ((int)lane_id() == __ffs(cpeers) - 1) {
+                    const int bs = slot_of(btag, child);
+                    unsigned* lo = bs >= 0 ? bmin + 3 * bs : clo + 3 * (uint64_t)child;
+                    unsigned* hi = bs >= 0 ? bmax + 3 * bs : chi + 3 * (uint64_t)child;
+                    atomicMin(lo, mnx); atomicMin(lo + 1, mny); atomicMin(lo + 2, mnz);
+                    atomicMax(hi, mxx); atomicMax(hi + 1, mxy); atomicMax(hi + 2, mxz);
+                }
             }
         }
-        unsigned am = __ballot_sync(0xffffffffu, moves);
-        if (moves) {
-            unsigned t = agg_inc(cursors + 2 * (uint64_t)path + side, 2 * (uint64_t)path + side, am);
-            uint64_t dst = a * 32 + (side ? left * 32 : 0) + t;
-            uint64_t end = side ? min((a + c) * 32, n) : (a + left) * 32;
-            if (dst < end) X2[dst] = p;
-            else atomicOr(err, 1u);  // a cut that does not fill the left child exactly
-            // child box for the next level (warp-reduced per child)
-            uint32_t child = (path << 1) | side;
-            unsigned peers = __match_any_sync(am, child);
-            unsigned ox = f2ord(p.x), oy = f2ord(p.y), oz = f2ord(p.z);
-            unsigned mnx = __reduce_min_sync(peers, ox), mny = __reduce_min_sync(peers, oy), mnz = __reduce_min_sync(peers, oz);
-            unsigned mxx = __reduce_max_sync(peers, ox), mxy = __reduce_max_sync(peers, oy), mxz = __reduce_max_sync(peers, oz);
-            if ((int)lane_id() == __ffs(peers) - 1) {
-                atomicMin(clo + 3 * child, mnx); atomicMin(clo + 3 * child + 1, mny); atomicMin(clo + 3 * child + 2, mnz);
-                atomicMax(chi + 3 * child, mxx); atomicMax(chi + 3 * child + 1, mxy); atomicMax(chi + 3 * child + 2, mxz);
+        __syncthreads();
+        if (threadIdx.x < kSlots * 2) {
+            const unsigned tg = ntag[threadIdx.x >> 1];
+            const unsigned cntv = ncnt[threadIdx.x];
+            nbase[threadIdx.x] = (tg != kNoTag && cntv) ? atomicAdd(cursors + 2 * (uint64_t)tg + (threadIdx.x & 1), cntv) : 0u;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < kSplitItems; ++t) {
+            if (code[t] >= 0) {
+                const uint64_t dst = dst0[t] + nbase[code[t]] + rank[t];
+                if (dst < dend[t]) X2[dst] = p[t];
+                else atomicOr(err, 1u);
             }
+        }
+        __syncthreads();
+    }
+    // flush the children's boxes
+    if (threadIdx.x < kSlots) {
+        const unsigned ch = btag[threadIdx.x];
+        if (ch != kNoTag) {
+            const int j = threadIdx.x;
+            atomicMin(clo + 3 * (uint64_t)ch, bmin[3 * j]); atomicMin(clo + 3 * (uint64_t)ch + 1, bmin[3 * j + 1]);
+            atomicMin(clo + 3 * (uint64_t)ch + 2, bmin[3 * j + 2]);
+            atomicMax(chi + 3 * (uint64_t)ch, bmax[3 * j]); atomicMax(chi + 3 * (uint64_t)ch + 1, bmax[3 * j + 1]);
+            atomicMax(chi + 3 * (uint64_t)ch + 2, bmax[3 * j + 2]);
         }
     }
 }
@@ -840,6 +969,14 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         unsigned init_lo[3] = {h6[0], h6[1], h6[2]}, init_hi[3] = {h6[3], h6[4], h6[5]};
         cudaMemcpyAsync(lo, init_lo, 12, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(hi, init_hi, 12, cudaMemcpyHostToDevice, st);
+        // persistent level blocks over contiguous ranges (a multiple of the split tile)
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const uint64_t lvl_blocks = std::max<uint64_t>(1, std::min<uint64_t>((n + 4095) / 4096, (uint64_t)sms * 8));
+        uint64_t per = (n + lvl_blocks - 1) / lvl_blocks;
+        per = (per + 1023) & ~1023ull;
+        const unsigned lb = (unsigned)((n + per - 1) / per);
         for (int d = 0; d < D; ++d) {
             const uint32_t nodes = 1u << d;
             cudaMemsetAsync(hist1, 0, (size_t)nodes * 256 * 4, st);
@@ -849,15 +986,15 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
             cudaMemsetAsync(clo, 0xff, (size_t)nodes * 2 * 12, st);
             cudaMemsetAsync(chi, 0x00, (size_t)nodes * 2 * 12, st);
             LevelNodes nb{lo, hi};
-            k_kdl_hist1<<<blocks, 256, 0, st>>>(X, n, L, d, nb, hist1);
+            k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, nullptr, hist1, per);
             note_launch();
             k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
             note_launch();
-            k_kdl_hist2<<<blocks, 256, 0, st>>>(X, n, L, d, nb, sel, hist2);
+            k_kdl_hist<2><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, sel, hist2, per);
             note_launch();
             k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
             note_launch();
-            k_kdl_split<<<blocks, 256, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, clo, chi, err);
+            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, clo, chi, err, per);
             note_launch();
             std::swap(X, X2);
             std::swap(lo, clo);
