@@ -896,6 +896,152 @@ __global__ void __launch_bounds__(kCellThreads) k_local_kd(float4* X, const unsi
         X[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
 }
 
+// Full cells (128 leaves = 4096 records, the bulk of every large map): the same k-d order as
+// k_local_kd, with the sort keys (16-bit coordinate : 13-bit slot) held in registers, 8
+// consecutive per thread. Bitonic strides below 8 swap inside a thread, strides 8..128 use
+// warp shuffles, and only strides of 256 or more go through shared memory; node boxes come
+// from segmented warp reductions.
+constexpr int kFullCell = 4096;
+constexpr int kFullThreads = 512;
+
+struct FullCellSmem {
+    float X[kFullCell], Y[kFullCell], Z[kFullCell];
+    uint32_t ID[kFullCell];
+    uint32_t sk[kFullCell];
+    unsigned blo[3 * 64], bhi[3 * 64];
+};
+
+__global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, const unsigned* __restrict__ cstart) {
+    extern __shared__ unsigned char smraw[];
+    FullCellSmem& s = *reinterpret_cast<FullCellSmem*>(smraw);
+    const uint64_t s0 = cstart[blockIdx.x];
+    const int t = threadIdx.x;
+    const int lane = t & 31;
+    for (int j = t; j < kFullCell; j += kFullThreads) {
+        const float4 p = Xg[s0 + j];
+        s.X[j] = p.x;
+        s.Y[j] = p.y;
+        s.Z[j] = p.z;
+        s.ID[j] = __float_as_uint(p.w);
+    }
+    for (int d = 0; d < 7; ++d) {
+        const unsigned S = (unsigned)kFullCell >> d;  // records per node at this level
+        for (int i = t; i < 3 * 64; i += kFullThreads) {
+            s.blo[i] = 0xffffffffu;
+            s.bhi[i] = 0u;
+        }
+        __syncthreads();
+        // node boxes: this thread's 8 records, then the node's lanes
+        unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int j = t * 8 + e;
+            const unsigned o[3] = {f2ord(s.X[j]), f2ord(s.Y[j]), f2ord(s.Z[j])};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = min(mn[k], o[k]);
+                mx[k] = max(mx[k], o[k]);
+            }
+        }
+        const int G = S >= 256 ? 32 : (int)(S >> 3);  // lanes per node within a warp
+        for (int o = 1; o < G; o <<= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+                mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+            }
+        }
+        const unsigned node = (unsigned)(t * 8) / S;
+        if ((lane & (G - 1)) == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&s.blo[3 * node + k], mn[k]);
+                atomicMax(&s.bhi[3 * node + k], mx[k]);
+            }
+        }
+        __syncthreads();
+        // keys: 16-bit coordinate on the node's widest axis, then the slot
+        const float l0 = ord2f(s.blo[3 * node]), l1 = ord2f(s.blo[3 * node + 1]), l2 = ord2f(s.blo[3 * node + 2]);
+        const float e0 = ord2f(s.bhi[3 * node]) - l0, e1 = ord2f(s.bhi[3 * node + 1]) - l1,
+                    e2 = ord2f(s.bhi[3 * node + 2]) - l2;
+        const int axis = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2 ? 1 : 2);
+        const float lo = axis == 0 ? l0 : (axis == 1 ? l1 : l2);
+        const float ext = axis == 0 ? e0 : (axis == 1 ? e1 : e2);
+        const float* V = axis == 0 ? s.X : (axis == 1 ? s.Y : s.Z);
+        uint32_t key[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int j = t * 8 + e;
+            uint32_t q = 0;
+            if (ext > 0.f) q = (uint32_t)fminf(fmaxf((V[j] - lo) / ext * 65535.f, 0.f), 65535.f);
+            key[e] = (q << 13) | (uint32_t)j;
+        }
+        // bitonic sort of every node's block of S keys, ascending
+        for (unsigned kk = 2; kk <= S; kk <<= 1) {
+            for (unsigned jj = kk >> 1; jj > 0; jj >>= 1) {
+                if (jj >= 256) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) s.sk[t * 8 + e] = key[e];
+                    __syncthreads();
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const unsigned i = (unsigned)(t * 8 + e);
+                        const uint32_t o = s.sk[i ^ jj];
+                        const bool lower = (i & jj) == 0, up = kk == S || (i & kk) == 0;
+                        key[e] = (lower == up) ? min(key[e], o) : max(key[e], o);
+                    }
+                    __syncthreads();
+                } else if (jj >= 8) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const unsigned i = (unsigned)(t * 8 + e);
+                        const uint32_t o = __shfl_xor_sync(0xffffffffu, key[e], (int)(jj >> 3));
+                        const bool lower = (i & jj) == 0, up = kk == S || (i & kk) == 0;
+                        key[e] = (lower == up) ? min(key[e], o) : max(key[e], o);
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        if ((e & (int)jj) == 0) {
+                            const int f = e | (int)jj;
+                            const unsigned i = (unsigned)(t * 8 + e);
+                            const bool up = kk == S || (i & kk) == 0;
+                            const uint32_t a = key[e], b = key[f];
+                            if ((a > b) == up) {
+                                key[e] = b;
+                                key[f] = a;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        // reorder the records by the sorted slots
+        float rx[8], ry[8], rz[8];
+        uint32_t rid[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const uint32_t src = key[e] & 0x1fffu;
+            rx[e] = s.X[src];
+            ry[e] = s.Y[src];
+            rz[e] = s.Z[src];
+            rid[e] = s.ID[src];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int j = t * 8 + e;
+            s.X[j] = rx[e];
+            s.Y[j] = ry[e];
+            s.Z[j] = rz[e];
+            s.ID[j] = rid[e];
+        }
+        __syncthreads();
+    }
+    for (int j = t; j < kFullCell; j += kFullThreads)
+        Xg[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
+}
+
 __global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         float4 p = a[i];
@@ -903,19 +1049,23 @@ __global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) 
     }
 }
 
-static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n, std::vector<unsigned>& st,
-                            std::vector<unsigned>& ct) {
+// nodes of depth D (or leaves above it): full 128-leaf cells go to `full`, the rest to
+// (st, ct)
+static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n, std::vector<unsigned>& full,
+                            std::vector<unsigned>& st, std::vector<unsigned>& ct) {
     if (depth == D || c <= 1) {
         uint64_t s = a * 32, e = std::min<uint64_t>((a + c) * 32, n);
-        if (e > s) {
+        if (e - s == (uint64_t)kFullCell && c * 32 == (uint64_t)kFullCell) {
+            full.push_back((unsigned)s);
+        } else if (e > s) {
             st.push_back((unsigned)s);
             ct.push_back((unsigned)(e - s));
         }
         return;
     }
     uint64_t left = 1ull << (63 - __builtin_clzll((unsigned long long)(c - 1)));
-    enumerate_cells(a, left, depth + 1, D, n, st, ct);
-    enumerate_cells(a + left, c - left, depth + 1, D, n, st, ct);
+    enumerate_cells(a, left, depth + 1, D, n, full, st, ct);
+    enumerate_cells(a + left, c - left, depth + 1, D, n, full, st, ct);
 }
 
 // out[i] <- (position, record id) of the i-th record of `a` in exact left-balanced k-d order.
@@ -1002,28 +1152,39 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         }
     }
     // local levels: one CTA per remaining node
-    std::vector<unsigned> cs, cc;
-    enumerate_cells(0, L, 0, D, n, cs, cc);
-    unsigned* dcs = ws.take_u32(cs.size());
-    unsigned* dcc = ws.take_u32(cc.size());
-    if (!dcs || !dcc) {
+    std::vector<unsigned> fs, cs, cc;
+    enumerate_cells(0, L, 0, D, n, fs, cs, cc);
+    unsigned* dfs = ws.take_u32(fs.size() + 1);
+    unsigned* dcs = ws.take_u32(cs.size() + 1);
+    unsigned* dcc = ws.take_u32(cc.size() + 1);
+    if (!dfs || !dcs || !dcc) {
         ws.release(mark);
         return -1;
     }
-    cudaMemcpyAsync(dcs, cs.data(), cs.size() * 4, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dcc, cc.data(), cc.size() * 4, cudaMemcpyHostToDevice, st);
+    if (!fs.empty()) cudaMemcpyAsync(dfs, fs.data(), fs.size() * 4, cudaMemcpyHostToDevice, st);
+    if (!cs.empty()) {
+        cudaMemcpyAsync(dcs, cs.data(), cs.size() * 4, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dcc, cc.data(), cc.size() * 4, cudaMemcpyHostToDevice, st);
+    }
     static bool attr_set[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
         cudaFuncSetAttribute(k_local_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
+        cudaFuncSetAttribute(k_local_kd_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FullCellSmem));
         attr_set[dev] = true;
     }
-    k_local_kd<<<(unsigned)cs.size(), kCellThreads, cell_smem_bytes(), st>>>(X, dcs, dcc, err);
-    note_launch();
+    if (!fs.empty()) {
+        k_local_kd_full<<<(unsigned)fs.size(), kFullThreads, sizeof(FullCellSmem), st>>>(X, dfs);
+        note_launch();
+    }
+    if (!cs.empty()) {
+        k_local_kd<<<(unsigned)cs.size(), kCellThreads, cell_smem_bytes(), st>>>(X, dcs, dcc, err);
+        note_launch();
+    }
     unsigned herr = 0;
     cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);  // also keeps the host vectors cs/cc alive for their copies
+    cudaStreamSynchronize(st);  // also keeps the host vectors alive for their copies
     ws.release(mark);
     return herr ? -1 : 0;
 }
