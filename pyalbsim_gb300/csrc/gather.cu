@@ -12,9 +12,10 @@
 // reference's KDTree (float64 on float32-cast map positions) orders them.
 //
 // Each warp takes contiguous chunks of the spatially sorted queries; from the second query
-// of a chunk on, the search starts with the threshold (r_k(prev) + |q - prev|)^2 (triangle
-// inequality: the previous query's k neighbours all lie within it), inflated by 2^-14 so
-// that every point of the float32 boundary band is still admitted.
+// of a chunk on, the search starts with the largest distance from the query to the previous
+// query's k neighbours (k points lie within it, so it bounds the k-th distance; never looser
+// than the triangle bound r_k(prev) + |q - prev|), inflated by 2^-14 so that every point of
+// the float32 boundary band is still admitted.
 #include <cfloat>
 
 #include "device_common.cuh"
@@ -481,7 +482,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 }
                 uint32_t cc = (uint32_t)c;
                 int nv = __popc(__ballot_sync(0xffffffffu, d < FLT_MAX));
-                if (nv <= 8) {
+                if (nv <= 16) {
                     // few children within the threshold: extract them nearest first
                     // (non-negative floats order like their bit patterns)
                     unsigned key = __float_as_uint(d);
@@ -680,20 +681,23 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
     const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
     const uint64_t chunks = (q.n + kQueryChunk - 1) / kQueryChunk;
     bool failed = false;
+    unsigned long long st_leaves = 0, st_nodes = 0, st_selects = 0, st_queries = 0, st_inexact = 0;
     for (uint64_t ch = (uint64_t)blockIdx.x * kGatherWarps + w; ch < chunks && !failed; ch += warps) {
         const uint64_t q_end = min((ch + 1) * kQueryChunk, q.n);
-        double px = 0.0, py = 0.0, pz = 0.0;  // previous query of the chunk
-        float prk = -1.f;                     // and its k-th neighbour distance
+        bool have_prev = false;  // s.ci[0 .. k) holds the previous query's neighbours
         for (uint64_t qi = ch * kQueryChunk; qi < q_end; ++qi) {
             uint64_t src = q.perm ? q.perm[qi] : qi;
             float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
             double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
             float thr0 = FLT_MAX;
-            if (prk >= 0.f) {
-                // float32 rounding here is far inside the 2^-14 inflation
-                float ddx = (float)(qx - px), ddy = (float)(qy - py), ddz = (float)(qz - pz);
-                float bound = (prk + sqrtf(fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)))) * (1.f + 1.f / 32768.f);
-                float t = bound * bound * (1.f + 1.f / 16384.f);
+            if (have_prev) {
+                // the float32 screening error (below 2^-21) is far inside the 2^-14 inflation
+                unsigned mx = 0u;
+                for (int j = l; j < k; j += 32) {
+                    const float d = point_dist2(qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, m.a[s.ci[j]]);
+                    mx = max(mx, __float_as_uint(d));  // non-negative floats order like their bits
+                }
+                const float t = __uint_as_float(__reduce_max_sync(0xffffffffu, mx)) * (1.f + 1.f / 16384.f);
                 if (t < 1.0e37f) thr0 = t;
             }
             KnnResult r;
@@ -703,18 +707,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
                 failed = true;
                 break;
             }
-            px = qx;
-            py = qy;
-            pz = qz;
-            prk = r.rkf;
+            have_prev = true;
             if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
-            if (q.inexact && r.clipped && l == 0) atomicAdd(q.inexact, 1ull);
-            if (q.stats && l == 0) {
-                atomicAdd(q.stats + 0, (unsigned long long)r.leaves);
-                atomicAdd(q.stats + 1, (unsigned long long)r.nodes);
-                atomicAdd(q.stats + 2, (unsigned long long)r.selects);
-                atomicAdd(q.stats + 3, 1ull);
-            }
+            st_leaves += r.leaves;
+            st_nodes += r.nodes;
+            st_selects += r.selects;
+            st_inexact += r.clipped;
+            ++st_queries;
             const float Es = qa.w, ts = qb.w;
             const float rk = r.rkf;
             float norm;
@@ -773,6 +772,15 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, Ma
             }
             __syncwarp();
         }
+    }
+    if (l == 0) {
+        if (q.stats && st_queries) {
+            atomicAdd(q.stats + 0, st_leaves);
+            atomicAdd(q.stats + 1, st_nodes);
+            atomicAdd(q.stats + 2, st_selects);
+            atomicAdd(q.stats + 3, st_queries);
+        }
+        if (q.inexact && st_inexact) atomicAdd(q.inexact, st_inexact);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kBinCache; i += blockDim.x) {
