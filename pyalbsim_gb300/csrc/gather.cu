@@ -23,7 +23,7 @@
 
 namespace alb {
 
-constexpr int kGatherWarps = 4;
+constexpr int kGatherWarps = 8;   // 8-warp CTAs, 4 per SM: 32 warps hide the gather's latency
 constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one warp
 constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
@@ -643,7 +643,7 @@ ALB_DEVICE Fix128 f32_to_fix(float v) {
 // claimed once by CAS on its tag; hits are exact 128-bit integer adds in shared memory,
 // misses go to global memory. Flushed once when the CTA finishes. The sum is integer, so
 // the split between cache and global memory cannot change the result.
-constexpr int kBinCache = 1024;
+constexpr int kBinCache = 256;
 struct BinCache {
     int tag[kBinCache];
     unsigned long long lo[kBinCache];
@@ -666,7 +666,7 @@ ALB_DEVICE void bin_add(BinCache& bc, const Accum& acc, int channel, int bin, co
 }
 
 template <int CHANNEL>
-__global__ void __launch_bounds__(kGatherWarps * 32, 5) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
+__global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
     __shared__ WarpSmem smem[kGatherWarps];
     __shared__ BinCache bc;
