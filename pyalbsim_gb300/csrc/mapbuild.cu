@@ -549,20 +549,33 @@ ALB_DEVICE void kd_node_of_path(uint32_t path, uint64_t L, int depth, uint64_t& 
     }
 }
 
+// Per node of a level: the widest box axis (x = axis bits, -1 for an empty extent), its low
+// end and 65535 / extent, so that a record's 16-bit coordinate is one multiply.
 struct LevelNodes {
-    const unsigned* lo;  // [nodes][3] ordered-int box of this level
-    const unsigned* hi;
+    const float4* par;
 };
 
-ALB_DEVICE uint32_t kd_quant16(float4 p, const unsigned* lo, const unsigned* hi, uint32_t path) {
-    float l0 = ord2f(lo[3 * path]), l1 = ord2f(lo[3 * path + 1]), l2 = ord2f(lo[3 * path + 2]);
-    float e0 = ord2f(hi[3 * path]) - l0, e1 = ord2f(hi[3 * path + 1]) - l1, e2 = ord2f(hi[3 * path + 2]) - l2;
-    float v, l, e;
-    if (e0 >= e1 && e0 >= e2) { v = p.x; l = l0; e = e0; }
-    else if (e1 >= e2) { v = p.y; l = l1; e = e1; }
-    else { v = p.z; l = l2; e = e2; }
-    if (!(e > 0.f)) return 0u;
-    return (uint32_t)fminf(fmaxf((v - l) / e * 65535.f, 0.f), 65535.f);
+__global__ void k_kdl_params(const unsigned* __restrict__ lo, const unsigned* __restrict__ hi, uint32_t nodes,
+                             float4* par) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    const float l0 = ord2f(lo[3 * i]), l1 = ord2f(lo[3 * i + 1]), l2 = ord2f(lo[3 * i + 2]);
+    const float e0 = ord2f(hi[3 * i]) - l0, e1 = ord2f(hi[3 * i + 1]) - l1, e2 = ord2f(hi[3 * i + 2]) - l2;
+    int axis;
+    float l, e;
+    if (e0 >= e1 && e0 >= e2) { axis = 0; l = l0; e = e0; }
+    else if (e1 >= e2) { axis = 1; l = l1; e = e1; }
+    else { axis = 2; l = l2; e = e2; }
+    if (!(e > 0.f)) axis = -1;
+    par[i] = make_float4(__int_as_float(axis), l, axis >= 0 ? 65535.f / e : 0.f, 0.f);
+}
+
+ALB_DEVICE uint32_t kd_quant16(float4 p, LevelNodes nb, uint32_t path) {
+    const float4 np = nb.par[path];
+    const int axis = __float_as_int(np.x);
+    if (axis < 0) return 0u;
+    const float v = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+    return (uint32_t)fminf(fmaxf((v - np.y) * np.z, 0.f), 65535.f);
 }
 
 // warp-aggregated atomicAdd of 1 on cnt[key]; returns this lane's ticket
@@ -616,7 +629,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
             int r;
             kd_node_path(i / 32, L, d, a, c, path, r);
             if (r == d && c > 1) {
-                const uint32_t q = kd_quant16(X[i], nb.lo, nb.hi, path);
+                const uint32_t q = kd_quant16(X[i], nb, path);
                 if (PASS == 1) {
                     act = true;
                     h = q >> 8;
@@ -783,7 +796,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     moves = true;
                     left = 1ull << (63 - __clzll((long long)(c - 1)));
                     const uint2 ct = cut[path[t]];
-                    const uint32_t q = kd_quant16(p[t], nb.lo, nb.hi, path[t]);
+                    const uint32_t q = kd_quant16(p[t], nb, path[t]);
                     if (q < ct.x) side = 0;
                     else if (q > ct.x) side = 1;
                     else side = (atomicAdd(ties + path[t], 1u) < ct.y) ? 0u : 1u;
@@ -1103,7 +1116,8 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         unsigned* hi = ws.take_u32(maxnodes * 6);
         unsigned* clo = ws.take_u32(maxnodes * 6);  // children boxes
         unsigned* chi = ws.take_u32(maxnodes * 6);
-        if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi) {
+        float4* par = (float4*)ws.take_bytes(maxnodes * 16);
+        if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi || !par) {
             ws.release(mark);
             return -1;
         }
@@ -1135,7 +1149,9 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
             cudaMemsetAsync(ties, 0, (size_t)nodes * 4, st);
             cudaMemsetAsync(clo, 0xff, (size_t)nodes * 2 * 12, st);
             cudaMemsetAsync(chi, 0x00, (size_t)nodes * 2 * 12, st);
-            LevelNodes nb{lo, hi};
+            k_kdl_params<<<(nodes + 255) / 256, 256, 0, st>>>(lo, hi, nodes, par);
+            note_launch();
+            LevelNodes nb{par};
             k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, nullptr, hist1, per);
             note_launch();
             k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
@@ -1375,7 +1391,8 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     }
     if (rec.id) m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, n);
     if (!m.b || (rec.fwi && (!m.fwi || !m.sfi)) || (rec.id && !m.id)) return -1;
-    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 16384);
+    // one record per thread: the gathers are random, so many loads in flight matter
+    const unsigned blocks = (unsigned)((n + 255) / 256);
     k_finalize<<<blocks, 256, 0, st>>>(m.a, m.b, rec.fwi ? m.fwi : nullptr, rec.fwi ? m.sfi : nullptr,
                                        rec.id ? m.id : nullptr, rec, n);
     note_launch();
