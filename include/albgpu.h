@@ -76,6 +76,23 @@ typedef struct AlbLayer {
     const double* phase_cdf;      /* ALB_PHASE_DIVISIONS normalised CDF values */
     const double* phase_slope;    /* ALB_PHASE_DIVISIONS-1 interpolation slopes d theta/d cdf */
     const double* scatter_weight; /* ALB_PHASE_DIVISIONS CDF mass per angular bin */
+    /* Depth profile (TurbidityLayerModel, alb_sim/physics/models/water.py:85-101,190-245).
+     * profiled == 0: the constants above hold in the whole layer. Otherwise, at a local
+     * depth z below the layer top, per integration step: speed = float32(c / n(z)),
+     * attenuation = float32(interp(float32(z), lut_z, lut_alpha)), albedo =
+     * float32((interp - a(z)) / interp). Profiles: kind 0 constant (start), 1 linear in
+     * float32 (LinearParameter), 2 exponential in float64 (ExponentialParameter), at the
+     * fraction z / height. */
+    int32_t profiled;
+    int32_t lut_n;                /* attenuation LUT entries (num_sublayers) */
+    const float* lut_z;           /* linspace(0, height, lut_n) in float32 */
+    const double* lut_alpha;      /* attenuation at lut_z */
+    int32_t n_kind;               /* refractive index profile kind */
+    int32_t a_kind;               /* absorption profile kind */
+    double n_start, n_end;
+    double a_start, a_end;
+    double height;                /* layer thickness, m */
+    double top32;                 /* depth of the layer top, rounded to float32 */
 } AlbLayer;
 
 /* Scene constants derived on the host from SimulationConfig. */

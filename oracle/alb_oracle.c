@@ -151,6 +151,77 @@ static int layer_of(const Model* m, double y) {
 
 static double norm3(double x, double y, double z) { return sqrt((x * x + y * y) + z * z); }
 
+/* Depth-profiled layers (alb_sim/physics/models/water.py:85-101,190-245,306-308;
+ * utils/parameter_profile.py:46-99): local depth below the layer top (float32 offset),
+ * LinearParameter in float32 at t = float32(z / h), ExponentialParameter in float64, the
+ * attenuation by numpy.interp on the float32-depth LUT at float32(z). */
+static double profile_value(int kind, double p0, double p1, double z, double h) {
+    if (kind == 1) {
+        float t = (float)(z / h);
+        float d = (float)(p1 - p0);
+        float prod = t * d;
+        return (double)((float)p0 + prod);
+    }
+    if (kind == 2) {
+        double l0 = log(p0), l1 = log(p1);
+        return exp(l0 + (z / h) * (l1 - l0));
+    }
+    return p0;
+}
+
+static double local_depth(const Model* m, int L, double y) {
+    return -(y - m->p->surface_y) - m->p->layers[L].top32;
+}
+
+static double lut_alpha(const AlbLayer* L, double z) {
+    const float* xp = L->lut_z;
+    const double* fp = L->lut_alpha;
+    int n = L->lut_n;
+    double x = (double)(float)z;
+    if (!(x >= (double)xp[0])) return fp[0];
+    if (x >= (double)xp[n - 1]) return fp[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) / 2;
+        if ((double)xp[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    if (x == (double)xp[lo]) return fp[lo];
+    double slope = (fp[lo + 1] - fp[lo]) / ((double)xp[lo + 1] - (double)xp[lo]);
+    double prod = slope * (x - (double)xp[lo]);
+    return prod + fp[lo];
+}
+
+/* speed of a water step starting at height y */
+static double water_speed(const Model* m, double y) {
+    int L = layer_of(m, y);
+    const AlbLayer* A = &m->p->layers[L];
+    if (!A->profiled) return A->speed;
+    double n = profile_value(A->n_kind, A->n_start, A->n_end, local_depth(m, L, y), A->height);
+    if (A->n_kind == 1) {
+        float q = 299800000.0f / (float)n;
+        return (double)q;
+    }
+    return (double)(float)(299800000.0 / n);
+}
+
+static float water_alpha(const Model* m, double y) {
+    int L = layer_of(m, y);
+    const AlbLayer* A = &m->p->layers[L];
+    if (!A->profiled) return A->alpha;
+    return (float)lut_alpha(A, local_depth(m, L, y));
+}
+
+static float water_ssa(const Model* m, double y) {
+    int L = layer_of(m, y);
+    const AlbLayer* A = &m->p->layers[L];
+    if (!A->profiled) return A->ssa;
+    double z = local_depth(m, L, y);
+    double al = lut_alpha(A, z);
+    double a = profile_value(A->a_kind, A->a_start, A->a_end, z, A->height);
+    return (float)((al - a) / al);
+}
+
 static double schlick(double f0, double c) { return f0 + (1.0 - f0) * pow(1.0 - c, 5.0); }
 
 /* numpy.interp(u, cdf, theta) */
@@ -282,7 +353,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
     const AlbSceneParams* P = m->p;
     const double ys = P->surface_y, yf = P->floor_y, dt = P->dt;
     for (int64_t step = 0; step < m->S; ++step) {
-        double v = (ph->p[1] > ys) ? P->speed_air : P->layers[layer_of(m, ph->p[1])].speed;
+        double v = (ph->p[1] > ys) ? P->speed_air : water_speed(m, ph->p[1]);
         double nx[3];
         for (int i = 0; i < 3; ++i) nx[i] = ph->p[i] + (ph->d[i] * v) * dt;
         double y = ph->p[1], yn = nx[1];
@@ -298,7 +369,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
         double sv[3] = {nx[0] - ph->p[0], nx[1] - ph->p[1], nx[2] - ph->p[2]};
         double len = norm3(sv[0], sv[1], sv[2]);
         if (st == 2) {
-            float a = P->layers[layer_of(m, ph->p[1])].alpha;
+            float a = water_alpha(m, ph->p[1]);
             ph->tau = (float)((double)ph->tau + (double)a * len);
             int scatter = ph->tau >= ph->taut;
             for (int i = 0; i < 3; ++i) ph->p[i] = nx[i];
@@ -322,7 +393,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
                 double nd[3];
                 rot_apply(ph->d, lv, nd);
                 for (int i = 0; i < 3; ++i) ph->d[i] = nd[i];
-                ph->E = ph->E * P->layers[L].ssa;
+                ph->E = ph->E * water_ssa(m, ph->p[1]);
                 ph->tau = ph->tau - ph->taut;
                 ph->taut = nt;
             }
@@ -367,7 +438,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
             }
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
             if (reflect) {
-                float a = P->layers[layer_of(m, ph->p[1])].alpha;
+                float a = water_alpha(m, ph->p[1]);
                 ph->tau = (float)((double)ph->tau + (double)a * len);
             }
         } else { /* seafloor */
@@ -407,7 +478,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
             double hn = norm3(h[0], h[1], h[2]);
             for (int i = 0; i < 3; ++i) ph->d[i] = h[i] / hn;
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
-            float a = P->layers[layer_of(m, ph->p[1])].alpha;
+            float a = water_alpha(m, ph->p[1]);
             ph->tau = (float)((double)ph->tau + (double)a * len);
             ph->E = ph->E * m->alb32;
         }

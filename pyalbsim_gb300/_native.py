@@ -48,6 +48,18 @@ class AlbLayer(C.Structure):
         ("phase_cdf", C.POINTER(C.c_double)),
         ("phase_slope", C.POINTER(C.c_double)),
         ("scatter_weight", C.POINTER(C.c_double)),
+        ("profiled", C.c_int32),
+        ("lut_n", C.c_int32),
+        ("lut_z", C.POINTER(C.c_float)),
+        ("lut_alpha", C.POINTER(C.c_double)),
+        ("n_kind", C.c_int32),
+        ("a_kind", C.c_int32),
+        ("n_start", C.c_double),
+        ("n_end", C.c_double),
+        ("a_start", C.c_double),
+        ("a_end", C.c_double),
+        ("height", C.c_double),
+        ("top32", C.c_double),
     ]
 
 
@@ -202,8 +214,6 @@ def scene_struct(scene: SceneModel):
     p.aperture_radius = scene.aperture_radius
     p.pulse_sigma = scene.pulse_sigma
     p.effective_rate = scene.effective_rate
-    if not scene.all_constant:
-        raise ValueError("depth-profiled layers are not supported by the GPU engine yet")
     if len(scene.layers) > MAX_LAYERS:
         raise ValueError(f"at most {MAX_LAYERS} water layers are supported")
     p.n_layers = len(scene.layers)
@@ -229,6 +239,18 @@ def scene_struct(scene: SceneModel):
         L.phase_cdf = cdf.ctypes.data_as(C.POINTER(C.c_double))
         L.phase_slope = sl.ctypes.data_as(C.POINTER(C.c_double))
         L.scatter_weight = w.ctypes.data_as(C.POINTER(C.c_double))
+        L.height = layer.height
+        L.top32 = layer.top32
+        L.profiled = int(not layer.constant)
+        if not layer.constant:
+            lz = np.ascontiguousarray(layer.lut_z, dtype=np.float32)
+            la = np.ascontiguousarray(layer.lut_alpha, dtype=np.float64)
+            keep += [lz, la]
+            L.lut_n = len(lz)
+            L.lut_z = lz.ctypes.data_as(C.POINTER(C.c_float))
+            L.lut_alpha = la.ctypes.data_as(C.POINTER(C.c_double))
+            L.n_kind, L.n_start, L.n_end = layer.n_profile
+            L.a_kind, L.a_start, L.a_end = layer.a_profile
     return p, keep
 
 

@@ -267,6 +267,36 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         s.layer_alpha[l] = L.alpha;
         s.layer_ssa[l] = L.ssa;
         s.layer_binw[l] = (float)L.bin_width;
+        s.layer_h[l] = L.height;
+        s.layer_top32[l] = L.top32;
+        s.layer_prof[l] = L.profiled ? 1 : 0;
+        s.layer_lut_n[l] = 0;
+        s.layer_lut_z[l] = nullptr;
+        s.layer_lut_a[l] = nullptr;
+        s.layer_nkind[l] = s.layer_akind[l] = 0;
+        s.layer_n0[l] = s.layer_n1[l] = s.layer_a0[l] = s.layer_a1[l] = 0.0;
+        if (L.profiled) {
+            if (!L.lut_z || !L.lut_alpha || L.lut_n < 2) return bad("profiled layer without an attenuation table");
+            if (!(L.height > 0.0)) return bad("profiled layer needs a positive height");
+            if (L.n_kind < 0 || L.n_kind > 2 || L.a_kind < 0 || L.a_kind > 2) return bad("unknown profile kind");
+            float* lz;
+            double* la;
+            if (cudaMalloc(&lz, L.lut_n * sizeof(float)) != cudaSuccess ||
+                cudaMalloc(&la, L.lut_n * sizeof(double)) != cudaSuccess)
+                return bad("table allocation failed");
+            ctx->tables.insert(ctx->tables.end(), {lz, la});
+            cudaMemcpy(lz, L.lut_z, L.lut_n * sizeof(float), cudaMemcpyHostToDevice);
+            cudaMemcpy(la, L.lut_alpha, L.lut_n * sizeof(double), cudaMemcpyHostToDevice);
+            s.layer_lut_n[l] = L.lut_n;
+            s.layer_lut_z[l] = lz;
+            s.layer_lut_a[l] = la;
+            s.layer_nkind[l] = L.n_kind;
+            s.layer_akind[l] = L.a_kind;
+            s.layer_n0[l] = L.n_start;
+            s.layer_n1[l] = L.n_end;
+            s.layer_a0[l] = L.a_start;
+            s.layer_a1[l] = L.a_end;
+        }
         double *th, *cdf, *sl;
         float* w;
         if (cudaMalloc(&th, N * sizeof(double)) != cudaSuccess || cudaMalloc(&cdf, N * sizeof(double)) != cudaSuccess ||

@@ -47,6 +47,16 @@ struct SceneDev {
     const double* layer_cdf[ALB_MAX_LAYERS];
     const double* layer_slope[ALB_MAX_LAYERS];
     const float* layer_weight[ALB_MAX_LAYERS];
+    // depth-profiled layers (layer_prof != 0): per-step speed, attenuation and albedo
+    int32_t layer_prof[ALB_MAX_LAYERS];
+    int32_t layer_lut_n[ALB_MAX_LAYERS];
+    const float* layer_lut_z[ALB_MAX_LAYERS];
+    const double* layer_lut_a[ALB_MAX_LAYERS];
+    int32_t layer_nkind[ALB_MAX_LAYERS];
+    int32_t layer_akind[ALB_MAX_LAYERS];
+    double layer_n0[ALB_MAX_LAYERS], layer_n1[ALB_MAX_LAYERS];
+    double layer_a0[ALB_MAX_LAYERS], layer_a1[ALB_MAX_LAYERS];
+    double layer_h[ALB_MAX_LAYERS], layer_top32[ALB_MAX_LAYERS];
 };
 
 // ---------------------------------------------------------------------------------------

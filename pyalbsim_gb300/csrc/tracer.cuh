@@ -172,6 +172,75 @@ ALB_DEVICE int layer_of(const SceneDev& sc, double y) {
     return i < sc.n_layers ? i : sc.n_layers - 1;
 }
 
+// ----------------------------------------------------------------------------------------
+// Depth-profiled layers (alb_sim/physics/models/water.py:85-101,190-245 and
+// utils/parameter_profile.py:46-99), evaluated per integration step at the local depth z
+// below the layer top (depth - float32 layer offset, water.py:306-308).
+// ----------------------------------------------------------------------------------------
+
+// Profile value at local depth z of a layer of height h: kind 1 is LinearParameter
+// (float32: t = f32(z / h), f32(start) + t * f32(end - start)), kind 2 ExponentialParameter
+// (float64), kind 0 the constant `p0`.
+ALB_DEVICE double profile_value(int kind, double p0, double p1, double z, double h) {
+    if (kind == 1) {
+        const float t = __double2float_rn(z / h);
+        return (double)__fadd_rn(__double2float_rn(p0), __fmul_rn(t, __double2float_rn(p1 - p0)));
+    }
+    if (kind == 2) {
+        const double l0 = log(p0), l1 = log(p1);
+        return exp(l0 + (z / h) * (l1 - l0));
+    }
+    return p0;
+}
+
+// numpy.interp(f32(z), lut_z, lut_alpha) (clamped at both ends), in float64
+ALB_DEVICE double profile_alpha64(const SceneDev& sc, int L, double z) {
+    const float* xp = sc.layer_lut_z[L];
+    const double* fp = sc.layer_lut_a[L];
+    const int n = sc.layer_lut_n[L];
+    const double x = (double)__double2float_rn(z);
+    if (!(x >= (double)xp[0])) return fp[0];
+    if (x >= (double)xp[n - 1]) return fp[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((double)xp[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    if (x == (double)xp[lo]) return fp[lo];
+    const double slope = __ddiv_rn(__dsub_rn(fp[lo + 1], fp[lo]), __dsub_rn((double)xp[lo + 1], (double)xp[lo]));
+    return __dadd_rn(__dmul_rn(slope, __dsub_rn(x, (double)xp[lo])), fp[lo]);
+}
+
+ALB_DEVICE double local_depth(const SceneDev& sc, int L, double y) { return -(y - sc.ys) - sc.layer_top32[L]; }
+
+// speed of the integration step that starts at height y in water layer L: f32(c / n(z))
+ALB_DEVICE double water_speed(const SceneDev& sc, int L, double y) {
+    if (!sc.layer_prof[L]) return sc.layer_speed[L];
+    const double z = local_depth(sc, L, y);
+    const int kind = sc.layer_nkind[L];
+    const double n = profile_value(kind, sc.layer_n0[L], sc.layer_n1[L], z, sc.layer_h[L]);
+    if (kind == 1) return (double)__fdiv_rn(299800000.0f, (float)n);  // float32 profile
+    return (double)__double2float_rn(299800000.0 / n);
+}
+
+// attenuation (float32) at height y in water
+ALB_DEVICE float water_alpha(const SceneDev& sc, double y) {
+    const int L = layer_of(sc, y);
+    if (!sc.layer_prof[L]) return sc.layer_alpha[L];
+    return __double2float_rn(profile_alpha64(sc, L, local_depth(sc, L, y)));
+}
+
+// single-scattering albedo (float32) at height y: (alpha - a) / alpha with the LUT alpha
+ALB_DEVICE float water_ssa(const SceneDev& sc, double y) {
+    const int L = layer_of(sc, y);
+    if (!sc.layer_prof[L]) return sc.layer_ssa[L];
+    const double z = local_depth(sc, L, y);
+    const double al = profile_alpha64(sc, L, z);
+    const double a = profile_value(sc.layer_akind[L], sc.layer_a0[L], sc.layer_a1[L], z, sc.layer_h[L]);
+    return __double2float_rn(__ddiv_rn(__dsub_rn(al, a), al));
+}
+
 ALB_DEVICE double norm3(double x, double y, double z) {
     return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
 }
@@ -445,7 +514,7 @@ ALB_DEVICE void handle_exit(const SceneDev& sc, const TraceOut& out, Ph& ph, Src
     double rem = (1.0 - f) * len;
     ph.px = xs + ph.dx * rem; ph.py = ys + ph.dy * rem; ph.pz = zs + ph.dz * rem;
     if (reflect) {
-        float a = sc.layer_alpha[layer_of(sc, ph.py)];
+        float a = water_alpha(sc, ph.py);
         ph.tau = __double2float_rn(__dadd_rn((double)ph.tau, (double)a * len));
     }
 }
@@ -481,7 +550,7 @@ ALB_DEVICE void handle_floor(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
     double len = norm3(stx, sty, stz);
     double rem = (1.0 - f) * len;
     ph.px = xb + ph.dx * rem; ph.py = yb + ph.dy * rem; ph.pz = zb + ph.dz * rem;
-    float a = sc.layer_alpha[layer_of(sc, ph.py)];
+    float a = water_alpha(sc, ph.py);
     ph.tau = __double2float_rn(__dadd_rn((double)ph.tau, (double)a * len));
     ph.E = __fmul_rn(ph.E, sc.floor_albedo32);
 }
@@ -502,7 +571,7 @@ ALB_DEVICE void handle_scatter(const SceneDev& sc, const TraceOut& out, Ph& ph, 
     double ox, oy, oz;
     rotate_from_z(ph.dx, ph.dy, ph.dz, l0, l1, l2, ox, oy, oz);
     ph.dx = ox; ph.dy = oy; ph.dz = oz;
-    ph.E = __fmul_rn(ph.E, sc.layer_ssa[L]);
+    ph.E = __fmul_rn(ph.E, water_ssa(sc, ph.py));
     ph.tau = __fsub_rn(ph.tau, ph.taut);
     ph.taut = new_target;
 }
@@ -580,6 +649,40 @@ ALB_DEVICE void trace_photon(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
             handle_enter<PASS>(sc, out, ph, src, svx, svy, svz, pid);
             ph.s += 1;
             ++events;
+        } else if (sc.layer_prof[layer_of(sc, ph.py)]) {
+            // depth-profiled layer: one integration step, speed and attenuation at its start
+            --guard;  // bounded by the step count, not an event
+            const int L = layer_of(sc, ph.py);
+            const double v = water_speed(sc, L, ph.py);
+            const double svx = (ph.dx * v) * sc.dt, svy = (ph.dy * v) * sc.dt, svz = (ph.dz * v) * sc.dt;
+            const double ny = ph.py + svy;
+            if (ny > sc.ys) {
+                handle_exit<PASS>(sc, out, ph, src, svx, svy, svz, pid);
+                ph.s += 1;
+                ++events;
+                ++guard;
+                continue;
+            }
+            if (ny <= sc.yf) {
+                handle_floor<PASS>(sc, out, ph, src, svx, svy, svz, pid);
+                ph.s += 1;
+                ++events;
+                ++guard;
+                continue;
+            }
+            const double len = norm3(svx, svy, svz);
+            const float a = __double2float_rn(profile_alpha64(sc, L, local_depth(sc, L, ph.py)));
+            ph.tau = __double2float_rn(__dadd_rn((double)ph.tau, (double)a * len));
+            ph.px = ph.px + svx;
+            ph.py = ny;
+            ph.pz = ph.pz + svz;
+            const int64_t step = ph.s;
+            ph.s += 1;
+            if (ph.tau >= ph.taut) {
+                handle_scatter<PASS>(sc, out, ph, src, step, pid);
+                ++events;
+                ++guard;
+            }
         } else {
             int L = layer_of(sc, ph.py);
             double v = sc.layer_speed[L];

@@ -101,6 +101,12 @@ ALB_DEVICE int first_layer_change_f(const SceneDev& sc, int layer, float y0, flo
     return first_above_f(y0, sy, lim, nmax);
 }
 
+// attenuation at height y (float32 layer lookup; profiled layers through the exact table)
+ALB_DEVICE float water_alpha_f(const SceneDev& sc, float y) {
+    const int L = layer_of_f(sc, y);
+    return sc.layer_prof[L] ? water_alpha(sc, (double)y) : sc.layer_alpha[L];
+}
+
 template <int PASS>
 ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const TraceOut& out, PhF& ph,
                                   PhiloxSrc& src, uint32_t pid, unsigned long long& events) {
@@ -147,15 +153,19 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             continue;
         }
         int L = layer_of_f(sc, ph.py);
-        float v = (float)sc.layer_speed[L] * dt;
+        // a depth-profiled layer is crossed one integration step at a time (speed and
+        // attenuation at the step's start depth); those steps are not events for the cap
+        const bool prof = sc.layer_prof[L] != 0;
+        if (prof) --guard;
+        float v = (prof ? (float)water_speed(sc, L, (double)ph.py) : (float)sc.layer_speed[L]) * dt;
         float svx = ph.dx * v, svy = ph.dy * v, svz = ph.dz * v;
         float len = sqrtf(fmaf(svx, svx, fmaf(svy, svy, svz * svz)));
         int n_plane = left + 1;
         if (svy > 0.f) n_plane = first_above_f(ph.py, svy, ys, left) - 1;
         else if (svy < 0.f) n_plane = first_at_or_below_f(ph.py, svy, yf, left) - 1;
-        int n_layer = first_layer_change_f(sc, L, ph.py, svy, left);
+        int n_layer = prof ? 1 : first_layer_change_f(sc, L, ph.py, svy, left);
         int nseg = min(min(n_plane, n_layer), left);
-        float inc = sc.layer_alpha[L] * len;
+        float inc = (prof ? water_alpha(sc, (double)ph.py) : sc.layer_alpha[L]) * len;
         int m = 0;
         if (nseg > 0 && inc > 0.f) {
             float need = (ph.taut - ph.tau) / inc;
@@ -188,11 +198,12 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.dx = fmaf(ctt, ph.dx, st * ux);
             ph.dy = fmaf(ctt, ph.dy, st * uy);
             ph.dz = fmaf(ctt, ph.dz, st * uz);
-            ph.E *= sc.layer_ssa[L2];
+            ph.E *= sc.layer_prof[L2] ? water_ssa(sc, (double)ph.py) : sc.layer_ssa[L2];
             ph.tau = fmaxf(ph.tau - ph.taut, 0.f);
             ph.taut = -__logf(uf(b.z));
             ph.s = step + 1;
             ++events;
+            if (prof) ++guard;
             continue;
         }
         float k = (float)nseg;
@@ -200,7 +211,8 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
         ph.tau = fmaf(k, inc, ph.tau);
         ph.s += nseg;
         if (ph.s >= S) break;
-        if (nseg != n_plane) continue;  // layer change only
+        if (nseg != n_plane) continue;  // layer change (or one profiled step) only
+        if (prof) ++guard;
         if (svy > 0.f) {
             // handle_exit
             float f = fminf(fmaxf((ys - ph.py) / svy, 0.f), 1.f);
@@ -220,7 +232,7 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             }
             float rem = (1.f - f) * len;
             ph.px = fmaf(ph.dx, rem, xs); ph.py = fmaf(ph.dy, rem, yss); ph.pz = fmaf(ph.dz, rem, zs);
-            if (reflect) ph.tau = fmaf(sc.layer_alpha[layer_of_f(sc, ph.py)], len, ph.tau);
+            if (reflect) ph.tau = fmaf(water_alpha_f(sc, ph.py), len, ph.tau);
         } else {
             // handle_seafloor
             float f = fminf(fmaxf((yf - ph.py) / svy, 0.f), 1.f);
@@ -246,7 +258,7 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.dx = hx * hn; ph.dy = hy * hn; ph.dz = hz * hn;
             float rem = (1.f - f) * len;
             ph.px = fmaf(ph.dx, rem, xb); ph.py = fmaf(ph.dy, rem, yb); ph.pz = fmaf(ph.dz, rem, zb);
-            ph.tau = fmaf(sc.layer_alpha[layer_of_f(sc, ph.py)], len, ph.tau);
+            ph.tau = fmaf(water_alpha_f(sc, ph.py), len, ph.tau);
             ph.E *= sc.floor_albedo32;
         }
         ph.s += 1;

@@ -23,7 +23,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
-from typing import List
+from typing import List, Optional, Tuple
 
 import numpy as np
 
@@ -137,6 +137,33 @@ def _value_at(value, z_local, height):
     return value.at(z_local / height)
 
 
+def _profile_code(value):
+    """(kind, start, end) of a layer property: 0 constant, 1 linear, 2 exponential."""
+    if isinstance(value, float):
+        return (0, float(value), float(value))
+    name = type(value).__name__
+    if name == "LinearParameter":
+        return (1, float(value.start), float(value.end))
+    if name == "ExponentialParameter":
+        return (2, float(value.start), float(value.end))
+    raise ValueError(f"unsupported depth profile {name}: LinearParameter or ExponentialParameter expected")
+
+
+def attenuation_lut(layer, wavelength, flying_height, divergence, bb_frac):
+    """The reference's attenuation LUT of a profiled layer
+    (TurbidityLayerModel._build_lidar_attenuation_lut, water.py:85-101): the Churnside
+    coefficient at num_sublayers float32 local depths, profiles evaluated at z / height with
+    the profiles' own float32 / float64 arithmetic."""
+    z = np.linspace(0.0, layer.height, int(layer.num_sublayers), dtype=np.float32)
+    a = _value_at(layer.absorption_coefficient, z, layer.height)
+    b = _value_at(layer.scattering_coefficient, z, layer.height)
+    s = _value_at(layer.salinity, z, layer.height)
+    # the reference's backscatter fraction is a NumPy float64 scalar, which (unlike a Python
+    # float) promotes float32 profile arrays to float64 in the formula
+    alpha = churnside_alpha(a, b, s, wavelength, flying_height, divergence, np.float64(bb_frac))
+    return z, np.asarray(alpha)
+
+
 @dataclass
 class LayerModel:
     height: float
@@ -154,6 +181,13 @@ class LayerModel:
     backscatter: float
     scatter_weight: np.ndarray
     bin_width32: float
+    top32: float = 0.0  # depth of the layer top, float32 (the reference's layer offset z0)
+    # depth profiles (profiled layers only): attenuation LUT on float32 local depths and
+    # the (kind, start, end) of the refractive index and absorption profiles
+    lut_z: Optional[np.ndarray] = None
+    lut_alpha: Optional[np.ndarray] = None
+    n_profile: Tuple[int, float, float] = (0, 0.0, 0.0)
+    a_profile: Tuple[int, float, float] = (0, 0.0, 0.0)
 
 
 @dataclass
@@ -241,6 +275,13 @@ def build_scene(cfg) -> SceneModel:
         with np.errstate(divide="ignore", invalid="ignore"):
             slope = np.diff(th) / np.diff(cdf)
         weight, width32 = scatter_weight_table(th, cdf)
+        top32 = float(np.float32(depth_acc))
+        constant = _is_constant(layer)
+        lut_z = lut_alpha = None
+        if not constant:
+            lut_z, lut_alpha = attenuation_lut(
+                layer, laser.wavelength, cfg.scene.flying_height, laser.divergence_angle, bb
+            )
         depth_acc = depth_acc + float(layer.height)
         layers.append(
             LayerModel(
@@ -259,6 +300,11 @@ def build_scene(cfg) -> SceneModel:
                 backscatter=bb,
                 scatter_weight=weight,
                 bin_width32=float(width32),
+                top32=top32,
+                lut_z=lut_z,
+                lut_alpha=lut_alpha,
+                n_profile=_profile_code(layer.refractive_index),
+                a_profile=_profile_code(layer.absorption_coefficient),
             )
         )
     depth = layers[-1].bottom_depth

@@ -18,6 +18,7 @@ from pyalbsim_gb300.config import (
     WaterConfig,
 )
 from pyalbsim_gb300.config.water import FournierForandConfig
+from pyalbsim_gb300.utils.parameter_profile import ExponentialParameter, LinearParameter
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -29,19 +30,29 @@ def load(name):
 def config_from_fixture(d) -> SimulationConfig:
     """Rebuild the SimulationConfig a golden fixture was recorded with."""
     f = lambda k: d[k].item() if np.ndim(d[k]) == 0 else d[k]  # noqa: E731
+    nl = len(d["cfg_layer_height"])
+    prof = d.get("cfg_layer_prof")
+    nsub = d.get("cfg_layer_nsub")
+
+    def prop(i, j, plain):
+        if prof is None or int(prof[i][j][0]) == 0:
+            return float(plain)
+        kind, start, end = prof[i][j]
+        return (LinearParameter if int(kind) == 1 else ExponentialParameter)(float(start), float(end))
+
     layers = tuple(
         TurbidityLayerConfig(
-            height=float(h),
-            absorption_coefficient=float(a),
-            scattering_coefficient=float(b),
-            salinity=float(s),
-            refractive_index=float(n),
-            fournier_forand_parameters=FournierForandConfig(refractive_index_ratio=float(nr), junge_slope=float(j)),
+            height=float(d["cfg_layer_height"][i]),
+            absorption_coefficient=prop(i, 0, d["cfg_layer_a"][i]),
+            scattering_coefficient=prop(i, 1, d["cfg_layer_b"][i]),
+            salinity=prop(i, 2, d["cfg_layer_salinity"][i]),
+            refractive_index=prop(i, 3, d["cfg_layer_n"][i]),
+            fournier_forand_parameters=FournierForandConfig(
+                refractive_index_ratio=float(d["cfg_layer_nratio"][i]), junge_slope=float(d["cfg_layer_junge"][i])
+            ),
+            **({"num_sublayers": int(nsub[i])} if nsub is not None else {}),
         )
-        for h, a, b, s, n, j, nr in zip(
-            d["cfg_layer_height"], d["cfg_layer_a"], d["cfg_layer_b"], d["cfg_layer_salinity"],
-            d["cfg_layer_n"], d["cfg_layer_junge"], d["cfg_layer_nratio"],
-        )
+        for i in range(nl)
     )
     return SimulationConfig(
         sample_multiplier=int(f("cfg_sample_multiplier")),

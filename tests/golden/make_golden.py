@@ -52,6 +52,7 @@ from alb_sim.photon_mapping.build_photon_map_data import build_photon_map_data  
 from alb_sim.photon_mapping.photon_map_index import PhotonMapIndex  # noqa: E402
 from alb_sim.photon_mapping.photon_type import PhotonType  # noqa: E402
 from alb_sim.utils.photon_wrapper import PhotonWrapper  # noqa: E402
+from alb_sim.utils.parameter_profile import ExponentialParameter, LinearParameter  # noqa: E402
 
 TYPES = list(PhotonType)  # channel order: BOTTOM, SCATTER, SURFACE_REFLECTION, TRANSMISSION_UP
 
@@ -288,8 +289,23 @@ def _state_arrays(prefix, w):
     }
 
 
+def _prof(v):
+    """(kind, start, end) of a layer property: 0 constant, 1 linear, 2 exponential."""
+    if isinstance(v, float):
+        return (0.0, v, v)
+    if isinstance(v, LinearParameter):
+        return (1.0, float(v.start), float(v.end))
+    if isinstance(v, ExponentialParameter):
+        return (2.0, float(v.start), float(v.end))
+    raise TypeError(type(v))
+
+
+def _start(v):
+    return v if isinstance(v, float) else float(v.start)
+
+
 def config_fields(cfg):
-    """Flatten a SimulationConfig (constant layers only) into npz scalars."""
+    """Flatten a SimulationConfig into npz scalars (layer properties may be profiles)."""
     out = {
         "cfg_sample_multiplier": cfg.sample_multiplier,
         "cfg_k": cfg.photon_mapping_k,
@@ -312,10 +328,15 @@ def config_fields(cfg):
     }
     layers = cfg.water.layers
     out["cfg_layer_height"] = np.array([l.height for l in layers], np.float64)
-    out["cfg_layer_a"] = np.array([l.absorption_coefficient for l in layers], np.float64)
-    out["cfg_layer_b"] = np.array([l.scattering_coefficient for l in layers], np.float64)
-    out["cfg_layer_salinity"] = np.array([l.salinity for l in layers], np.float64)
-    out["cfg_layer_n"] = np.array([l.refractive_index for l in layers], np.float64)
+    out["cfg_layer_a"] = np.array([_start(l.absorption_coefficient) for l in layers], np.float64)
+    out["cfg_layer_b"] = np.array([_start(l.scattering_coefficient) for l in layers], np.float64)
+    out["cfg_layer_salinity"] = np.array([_start(l.salinity) for l in layers], np.float64)
+    out["cfg_layer_n"] = np.array([_start(l.refractive_index) for l in layers], np.float64)
+    # [layer, (a, b, salinity, n), (kind, start, end)] and the LUT size
+    out["cfg_layer_prof"] = np.array(
+        [[_prof(l.absorption_coefficient), _prof(l.scattering_coefficient), _prof(l.salinity),
+          _prof(l.refractive_index)] for l in layers], np.float64)
+    out["cfg_layer_nsub"] = np.array([l.num_sublayers for l in layers], np.int64)
     out["cfg_layer_junge"] = np.array(
         [l.fournier_forand_parameters.junge_slope for l in layers], np.float64
     )
@@ -376,6 +397,10 @@ def run_recorded(cfg, n_fwd, n_bwd, seed):
             with np.errstate(divide="ignore"):
                 out[f"{p}_stream_tau"] = -np.log(s.astype(np.float32))
         out.update(config_fields(cfg))
+        for i, layer in enumerate(sim.model.water.layers):
+            if hasattr(layer, "_z_lut"):  # profiled layer: the reference's attenuation LUT
+                out[f"lut{i}_z"] = layer._z_lut
+                out[f"lut{i}_alpha"] = layer._lidar_alpha_lut
         return out
     finally:
         core_sim.PhotonWrapper = PhotonWrapper
@@ -456,12 +481,46 @@ def config0_geometry():
     )
 
 
-def make_replay():
+def profiled_config():
+    """Two depth-profiled layers: linear IOPs and index, then exponential ones with a
+    linear salinity profile (TurbidityLayerModel's attenuation LUT, per-step speed)."""
+    return SimulationConfig(
+        photon_mapping_k=32,
+        scene=SceneConfig(flying_height=10.0),
+        water=WaterConfig(
+            layers=(
+                TurbidityLayerConfig(
+                    height=1.0,
+                    absorption_coefficient=LinearParameter(0.05, 0.3),
+                    scattering_coefficient=LinearParameter(0.5, 1.5),
+                    refractive_index=LinearParameter(1.33, 1.35),
+                ),
+                TurbidityLayerConfig(
+                    height=1.5,
+                    absorption_coefficient=ExponentialParameter(0.1, 0.4),
+                    scattering_coefficient=0.8,
+                    refractive_index=ExponentialParameter(1.34, 1.36),
+                    salinity=LinearParameter(30.0, 38.0),
+                ),
+            )
+        ),
+        laser=LaserConfig(divergence_angle=5e-3, nadir_angle=10.0, azimuth_angle=30.0, pulse_fwhm=3e-9),
+        sensor=SensorConfig(aperture_radius=0.1, field_of_view=50e-3, sample_rate=int(1e9)),
+        sea_floor=SeaFloorConfig(albedo=0.2),
+        sea_surface=SeaSurfaceConfig(albedo=0.1, roughness=float(np.sqrt(0.05))),
+        heatmap=HeatmapConfig(enabled=False),
+    )
+
+
+def make_replay(only=None):
     jobs = [
         ("small", small_config(), 1500, 400, 11),
         ("twolayer", two_layer_config(), 800, 200, 12),
         ("cfg0", config0_geometry(), 300, 60, 0),
+        ("profiled", profiled_config(), 1200, 300, 13),
     ]
+    if only:
+        jobs = [j for j in jobs if j[0] in only]
     for name, cfg, nf, nb, seed in jobs:
         t = time.time()
         out = run_recorded(cfg, nf, nb, seed)
@@ -635,5 +694,7 @@ if __name__ == "__main__":
         make_knn()
     if what in ("replay", "all"):
         make_replay()
+    if what == "replay_profiled":
+        make_replay(only=("profiled",))
     if what in ("stats", "all"):
         make_stats()

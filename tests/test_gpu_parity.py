@@ -12,7 +12,7 @@ from pyalbsim_gb300.scene import build_scene
 
 pytestmark = pytest.mark.gpu
 
-REPLAYS = ["small", "twolayer", "cfg0"]
+REPLAYS = ["small", "twolayer", "cfg0", "profiled"]
 # Tolerances: FP32 arithmetic on the device vs float64 in the reference.
 REL_WAVEFORM_L1 = 1e-5
 

@@ -9,7 +9,7 @@ from fixtures import assert_statistically_equal, config_from_fixture, load, repl
 from oracle.oracle import Oracle, oracle_run
 from pyalbsim_gb300.scene import build_scene
 
-REPLAYS = ["small", "twolayer", "cfg0"]
+REPLAYS = ["small", "twolayer", "cfg0", "profiled"]
 
 
 @pytest.fixture(scope="module", params=REPLAYS)
@@ -26,6 +26,18 @@ def test_steps_match(replayed):
     assert scene.steps == int(d["steps"])
 
 
+def _assert_energy(d, mine, ref):
+    """Energies are bit-exact for constant layers. In depth-profiled layers the albedo
+    depends continuously on the float64 position, whose last bits differ from NumPy's
+    vectorised kernels (norms, exp/log); a flipped float32 rounding of the albedo then
+    shows as a one-ulp energy difference, so there the bar is the 1e-5 parity tolerance."""
+    prof = d.get("cfg_layer_prof")
+    if prof is not None and np.any(prof[:, :, 0] != 0):
+        np.testing.assert_allclose(mine, ref, rtol=1e-5, atol=0)
+    else:
+        np.testing.assert_array_equal(mine, ref)
+
+
 def test_photon_maps_record_by_record(replayed):
     """Same records (photon, step) per type; energies and times exact; geometry to 1e-6."""
     _, d, _, r = replayed
@@ -38,7 +50,7 @@ def test_photon_maps_record_by_record(replayed):
         ib = np.lexsort((d[f"map{c}_time"], d[f"map{c}_ids"]))
         np.testing.assert_array_equal(mp["photon"][ia], d[f"map{c}_ids"][ib])
         np.testing.assert_array_equal(mp["time"][ia], d[f"map{c}_time"][ib])
-        np.testing.assert_array_equal(mp["energy"][ia], d[f"map{c}_energy"][ib])
+        _assert_energy(d, mp["energy"][ia], d[f"map{c}_energy"][ib])
         np.testing.assert_allclose(mp["pos"][ia], d[f"map{c}_pos"][ib], rtol=1e-6, atol=1e-5)
         np.testing.assert_allclose(mp["dir"][ia], d[f"map{c}_dir"][ib], rtol=0, atol=1e-6)
         fa, fb = mp["fwi"][ia], d[f"map{c}_fwi"][ib]
@@ -50,7 +62,7 @@ def test_exit_states(replayed):
     _, d, _, r = replayed
     for p in ("fwd", "bwd"):
         ex = r[f"{p}_exit"]
-        np.testing.assert_array_equal(ex["energy"], d[f"{p}_final_energy"])
+        _assert_energy(d, ex["energy"], d[f"{p}_final_energy"])
         np.testing.assert_array_equal(ex["tau_target"], d[f"{p}_final_tau_target"])
         np.testing.assert_array_equal(ex["time"], d[f"{p}_final_time"])
         np.testing.assert_allclose(ex["tau"], d[f"{p}_final_tau"], rtol=1e-5, atol=1e-6)
@@ -98,7 +110,7 @@ def test_queries(replayed):
         np.testing.assert_array_equal(mine["photon"][ia], ref[ib, 1].astype(np.int64))
         np.testing.assert_array_equal(mine["time"][ia], ref[ib, 9].astype(np.float32))
         np.testing.assert_allclose(mine["pos"][ia], ref[ib, 2:5], rtol=1e-6, atol=1e-5)
-        np.testing.assert_array_equal(mine["energy"][ia], ref[ib, 8].astype(np.float32))
+        _assert_energy(d, mine["energy"][ia], ref[ib, 8].astype(np.float32))
 
 
 def test_heatmaps(replayed):

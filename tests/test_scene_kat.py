@@ -4,7 +4,7 @@ against values the reference's own functions returned (tests/golden/kat_physics.
 import numpy as np
 import pytest
 
-from fixtures import load
+from fixtures import config_from_fixture, load
 from pyalbsim_gb300.config import (
     HeatmapConfig, LaserConfig, SceneConfig, SeaFloorConfig, SeaSurfaceConfig, SensorConfig,
     SimulationConfig, TurbidityLayerConfig, WaterConfig,
@@ -131,3 +131,21 @@ def test_scene_struct_packs(mk):
     assert p.n_layers == len(s.layers)
     assert p.steps == s.steps and p.k == s.k
     assert abs(p.layers[p.n_layers - 1].bottom_depth - s.depth) < 1e-12
+
+
+def test_profiled_attenuation_lut_matches_reference():
+    """Depth-profiled layers: the attenuation LUT (float32 depths, float64 values) equals the
+    reference's TurbidityLayerModel LUT bit for bit (linear and exponential IOPs, a linear
+    salinity profile)."""
+    d = load("replay_profiled.npz")
+    scene = build_scene(config_from_fixture(d))
+    n = 0
+    for i, layer in enumerate(scene.layers):
+        if f"lut{i}_z" not in d:
+            assert layer.constant
+            continue
+        n += 1
+        assert not layer.constant
+        np.testing.assert_array_equal(layer.lut_z, d[f"lut{i}_z"])
+        np.testing.assert_array_equal(layer.lut_alpha, d[f"lut{i}_alpha"])
+    assert n == 2
