@@ -266,6 +266,35 @@ def test_fast_and_precise_agree_in_distribution(gpu_available):
     assert np.all(np.abs(a.mean(0) - b.mean(0)) < 4 * se + 1e-30), (a.mean(0), b.mean(0), se)
 
 
+def test_fast_and_precise_agree_in_distribution_profiled(gpu_available):
+    """Depth-profiled layers: the float32 tracer (one step at a time in profiled layers)
+    against the float64-geometry tracer, channel totals within 4 combined standard errors
+    over 8 seeds each."""
+    cfg = config_from_fixture(load("replay_profiled.npz"))
+    nf, nb = 40000, 10000
+    tot = {}
+    for precise in (True, False):
+        tot[precise] = np.stack(
+            [_philox_run(cfg, nf, nb, 700 + r, ids=False, precise=precise)[2].sum(1) / (nf * nb) for r in range(8)]
+        )
+    a, b = tot[True], tot[False]
+    se = np.sqrt(a.var(0, ddof=1) / 8 + b.var(0, ddof=1) / 8)
+    assert np.all(np.abs(a.mean(0) - b.mean(0)) < 4 * se + 1e-30), (a.mean(0), b.mean(0), se)
+
+
+def test_philox_profiled_matches_oracle(gpu_available):
+    """Same Philox streams, profiled layers: the precise tracer and the oracle agree on the
+    waveform within the parity tolerance."""
+    cfg = config_from_fixture(load("replay_profiled.npz"))
+    nf, nb = 3000, 800
+    wf = _philox_run(cfg, nf, nb, 41, ids=False, precise=True)[2]
+    orc = oracle_run(build_scene(cfg), nf, nb, seed=41)
+    for c in range(4):
+        den = np.abs(orc["waveform"][c]).sum()
+        if den:
+            assert np.abs(wf[c] - orc["waveform"][c]).sum() / den < REL_WAVEFORM_L1, c
+
+
 def test_too_few_photons_raises_index_error(gpu_available):
     """Reference quirk: a gather on a map with fewer than k records raises IndexError."""
     cfg = config_from_fixture(load("replay_small.npz"))
