@@ -125,6 +125,9 @@ typedef struct AlbSceneParams {
     double water_center[3];
     double floor_center[3];
     AlbLayer layers[ALB_MAX_LAYERS];
+    /* Extension (no counterpart in the reference): > 0 selects the fixed-radius gather, every
+     * record within this distance (m) with norm 1/(pi R^2) or 1/(4/3 pi R^3); 0 is k-NN. */
+    double gather_radius;
 } AlbSceneParams;
 
 /* Caller-supplied variates (replay mode): photon i consumes values[offsets[i] ..

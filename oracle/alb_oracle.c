@@ -706,7 +706,8 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                   double* rk_out, double* heat_w, double* heat_f, int threads) {
     int k = p->k;
     int64_t nb = 2 * p->steps;
-    if (nq > 0 && m < k) return ALB_ERR_TOO_FEW;
+    const double R = p->gather_radius;  /* extension: > 0 selects the fixed-radius gather */
+    if (nq > 0 && R <= 0.0 && m < k) return ALB_ERR_TOO_FEW;
     int nthreads = 1;
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
@@ -726,15 +727,36 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
         double* wf = priv + (size_t)tid * (nb + 2 * hb);
         double* hw = wf + nb;
         double* hf = hw + hb;
-        Cand* c = (Cand*)malloc((size_t)k * sizeof(Cand));
+        int64_t ccap = R > 0.0 ? 64 : k;
+        Cand* c = (Cand*)malloc((size_t)ccap * sizeof(Cand));
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 8)
 #endif
         for (int64_t q = 0; q < nq; ++q) {
             const double* x = qpos + 3 * q;
             const double* ds = qdir + 3 * q;
-            knn_brute(mpos, m, x, k, c);
-            double r = sqrt(c[k - 1].d2);
+            int64_t cnt = k;
+            double r;
+            if (R > 0.0) {
+                /* every record with float64 squared distance <= R^2 */
+                cnt = 0;
+                for (int64_t j = 0; j < m; ++j) {
+                    double dx = (double)mpos[3 * j] - x[0], dy = (double)mpos[3 * j + 1] - x[1],
+                           dz = (double)mpos[3 * j + 2] - x[2];
+                    if ((dx * dx + dy * dy) + dz * dz <= R * R) {
+                        if (cnt == ccap) {
+                            ccap *= 2;
+                            c = (Cand*)realloc(c, (size_t)ccap * sizeof(Cand));
+                        }
+                        c[cnt].i = (int32_t)j;
+                        ++cnt;
+                    }
+                }
+                r = R;
+            } else {
+                knn_brute(mpos, m, x, k, c);
+                r = sqrt(c[k - 1].d2);
+            }
             if (rk_out) rk_out[q] = r;
             double ks = (channel == ALB_SCATTER) ? (4.0 / 3.0) * PI * pow(r, 3.0) : PI * (r * r);
             double norm = 1.0 / ks;
@@ -745,7 +767,7 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                 while (L < p->n_layers && !(p->layers[L].bottom_depth > depth)) ++L;
                 if (L >= p->n_layers) L = p->n_layers - 1;
             }
-            for (int j = 0; j < k; ++j) {
+            for (int64_t j = 0; j < cnt; ++j) {
                 int32_t id = c[j].i;
                 double w;
                 const float* df = mdir + 3 * id;

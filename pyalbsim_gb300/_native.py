@@ -93,6 +93,7 @@ class AlbSceneParams(C.Structure):
         ("water_center", C.c_double * 3),
         ("floor_center", C.c_double * 3),
         ("layers", AlbLayer * MAX_LAYERS),
+        ("gather_radius", C.c_double),
     ]
 
 
@@ -217,6 +218,7 @@ def scene_struct(scene: SceneModel):
     if len(scene.layers) > MAX_LAYERS:
         raise ValueError(f"at most {MAX_LAYERS} water layers are supported")
     p.n_layers = len(scene.layers)
+    p.gather_radius = float(scene.gather_radius or 0.0)
     p.heatmap_enabled = int(scene.heatmap_enabled)
     p.heatmap_bins = scene.heatmap_bins
     p.heatmap_water_extent = scene.heatmap_water_extent

@@ -1,6 +1,7 @@
 """Top-level simulation settings; fields and defaults as ``alb_sim/config/simulation.py:12-60``."""
 
 from dataclasses import dataclass, field
+from typing import Optional
 
 from pyalbsim_gb300.config.heatmap import HeatmapConfig
 from pyalbsim_gb300.config.laser import LaserConfig
@@ -26,3 +27,12 @@ class SimulationConfig:
     sea_floor: SeaFloorConfig = field(default_factory=SeaFloorConfig)
     sea_surface: SeaSurfaceConfig = field(default_factory=SeaSurfaceConfig)
     heatmap: HeatmapConfig = field(default_factory=HeatmapConfig)
+    # Extension (no counterpart in the reference): density estimates over every photon-map
+    # record within this radius (m) instead of the k nearest; None keeps the k-NN gather.
+    gather_radius: Optional[float] = field(
+        default=None, metadata={"unit": "m", "description": "Fixed gather radius; None: k nearest"}
+    )
+
+    def __post_init__(self):
+        if self.gather_radius is not None and not self.gather_radius > 0:
+            raise ValueError("gather_radius must be positive (None selects the k-NN gather)")

@@ -51,8 +51,16 @@ class TurbidityLayerConfig:
     num_sublayers: Optional[int] = field(
         default=None, metadata={"description": "Number of sub-layers of the depth LUT"}
     )
+    # Extension (no counterpart in the reference): Henyey-Greenstein scattering with this
+    # asymmetry parameter in place of the Fournier-Forand phase function (None: FF).
+    henyey_greenstein_g: Optional[float] = field(
+        default=None, metadata={"description": "HG asymmetry g in (-1, 1); None selects Fournier-Forand"}
+    )
 
     def __post_init__(self):
+        g = self.henyey_greenstein_g
+        if g is not None and (not -1.0 < float(g) < 1.0 or g == 0.0):
+            raise ValueError("henyey_greenstein_g must lie in (-1, 1) and be non-zero")
         if self.height <= 0:
             raise ValueError("Layer height must be positive")
         for name in (

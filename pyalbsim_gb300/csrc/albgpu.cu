@@ -248,6 +248,8 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
     s.rayleigh_sigma = p->divergence / 3.0;
     s.rayleigh_mass = -std::expm1(-(p->divergence * p->divergence) / (2.0 * s.rayleigh_sigma * s.rayleigh_sigma));
     s.n_layers = p->n_layers;
+    if (!(p->gather_radius >= 0.0)) return bad("gather_radius must be >= 0 (0 selects the k-NN gather)");
+    s.radius = p->gather_radius;
     s.heatmap = p->heatmap_enabled;
     s.hm_bins = p->heatmap_bins;
     s.hm_wext = p->heatmap_water_extent;
@@ -655,7 +657,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             for (int k = 0; k < 3; ++k) ctx->q_rate[k] = (double)cnt[k] / (double)nc;
             if (attempt == 2) return fail(ctx, ALB_ERR_CAPACITY, "query capacity could not be established");
         }
-        int rc = check_map_sizes(ctx);
+        int rc = ctx->sc.radius > 0.0 ? ALB_OK : check_map_sizes(ctx);  // k-NN needs k records
         if (rc) return rc;
         static const int kinds[4] = {kQueryBottom, kQueryScatter, kQuerySurface, kQuerySurface};
         static const int chans[4] = {ALB_BOTTOM_REFLECTION, ALB_SCATTER, ALB_SURFACE_REFLECTION,

@@ -665,6 +665,88 @@ ALB_DEVICE void bin_add(BinCache& bc, const Accum& acc, int channel, int bin, co
     }
 }
 
+// Extension (no counterpart in the reference): every record within the fixed radius R of
+// the query, visited in any order. Screening as in the k-NN search; points within the
+// float32 error band of R are decided on their float64 distance. visit(record) runs on the
+// lanes holding admitted records.
+template <class F>
+ALB_DEVICE void warp_radius_visit(const MapDev& m, WarpSmem& s, double qx, double qy, double qz, float fx, float fy,
+                                  float fz, float lx, float ly, float lz, double R, F&& visit, KnnResult& res) {
+    const int l = lane_id();
+    const double R2 = R * R;
+    const float thr = __double2float_ru(R2) * (1.0f + 2.0f * kRelMargin);
+    const float lo_band = __double2float_rd(R2) * (1.0f - 2.0f * kRelMargin);
+    res.leaves = res.nodes = res.selects = res.clipped = 0;
+    res.rk2 = R2;
+    res.rkf = (float)R;
+    if (m.nlevels <= 0) return;  // an empty map contributes nothing
+    int sp = 0;
+    {
+        const int top = m.nlevels - 1;
+        bool ok = false;
+        if ((uint64_t)l < m.lvl_cnt[top])
+            ok = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[top] + l], m.box_hi[m.lvl_off[top] + l]) <= thr;
+        const unsigned b = __ballot_sync(0xffffffffu, ok);
+        if (ok) s.stk[sp + __popc(b & lanemask_lt())] = ((uint32_t)top << 29) | (uint32_t)l;
+        sp += __popc(b);
+        __syncwarp();
+    }
+    // every box is pushed at most once, so the box count bounds the loop
+    const uint64_t boxes = m.lvl_off[m.nlevels - 1] + m.lvl_cnt[m.nlevels - 1];
+    uint64_t guard = 0;
+    while (sp > 0) {
+        if (++guard > boxes) {
+            res.clipped = 1;
+            break;
+        }
+        --sp;
+        const uint32_t e = s.stk[sp];
+        __syncwarp();
+        const int lev = (int)(e >> 29);
+        const uint32_t node = e & 0x1fffffffu;
+        if (lev == 0) {
+            ++res.leaves;
+            const uint64_t r = (uint64_t)node * 32 + l;
+            bool in = false;
+            if (r < m.n) {
+                const float4 p = m.a[r];
+                const float d = point_dist2(fx, fy, fz, lx, ly, lz, p);
+                in = d < lo_band || (d <= thr && point_dist2_f64(qx, qy, qz, p) <= R2);
+            }
+            if (in) visit((uint32_t)r);
+        } else {
+            ++res.nodes;
+            const int cl = lev - 1;
+            const uint64_t c = (uint64_t)node * 32 + l;
+            bool ok = false;
+            if (c < m.lvl_cnt[cl])
+                ok = box_dist2(fx, fy, fz, lx, ly, lz, m.box_lo[m.lvl_off[cl] + c], m.box_hi[m.lvl_off[cl] + c]) <= thr;
+            const unsigned b = __ballot_sync(0xffffffffu, ok);
+            if (ok) s.stk[sp + __popc(b & lanemask_lt())] = ((uint32_t)cl << 29) | (uint32_t)c;
+            sp += __popc(b);
+            __syncwarp();
+        }
+    }
+}
+
+// accumulate_to_heatmap (alb_sim/math/accumulate_heatmap.py:6-61) for one neighbour
+ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, uint32_t idx, float c) {
+    const float4 fw = m.fwi[idx], sf = m.sfi[idx];
+    const Fix128 f = f32_to_fix(c);
+    if (fw.x == fw.x) {
+        long long xi = (long long)(((double)fw.x - sc.wc[0] + sc.hm_wext) / sc.hm_wbin);
+        long long zi = (long long)(((double)fw.z - sc.wc[2] + sc.hm_wext) / sc.hm_wbin);
+        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+            fix_atomic_add(acc.hw_lo + xi * sc.hm_bins + zi, acc.hw_hi + xi * sc.hm_bins + zi, f);
+    }
+    if (sf.x == sf.x) {
+        long long xi = (long long)(((double)sf.x - sc.fc[0] + sc.hm_fext) / sc.hm_fbin);
+        long long zi = (long long)(((double)sf.z - sc.fc[2] + sc.hm_fext) / sc.hm_fbin);
+        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
+            fix_atomic_add(acc.hf_lo + xi * sc.hm_bins + zi, acc.hf_hi + xi * sc.hm_bins + zi, f);
+    }
+}
+
 template <int CHANNEL>
 __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
@@ -689,6 +771,41 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             uint64_t src = q.perm ? q.perm[qi] : qi;
             float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
             double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
+            if (sc.radius > 0.0) {
+                // extension: every record within the fixed radius contributes at once
+                KnnResult r;
+                const float Es = qa.w, ts = qb.w;
+                const float R = (float)sc.radius;
+                const float norm = (CHANNEL == ALB_SCATTER) ? 1.0f / ((4.0f / 3.0f) * 3.14159265358979f * R * R * R)
+                                                            : 1.0f / (3.14159265358979f * R * R);
+                const float vinv = rsqrtf(fmaf(qb.x, qb.x, fmaf(qb.y, qb.y, qb.z * qb.z)));
+                const float vx = -qb.x * vinv, vy = -qb.y * vinv, vz = -qb.z * vinv;
+                float wconst = 0.f;
+                if (CHANNEL == ALB_BOTTOM_REFLECTION) wconst = (float)(sc.floor_albedo / kPi) * fmaxf(0.f, -qb.y);
+                if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
+                const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
+                warp_radius_visit(m, s, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, sc.radius,
+                    [&](uint32_t idx) {
+                        const float4 pb = m.b[idx];
+                        float w;
+                        if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
+                        else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
+                        else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+                        const float c = ((Es * m.a[idx].w) * norm) * w;
+                        const int bin = (int)((ts + pb.w) / (float)sc.mult);
+                        if (bin >= 0 && bin < acc.nbins) bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                        else atomicCAS(err, 0, ALB_ERR_CAPACITY);
+                        if (acc.hw_lo && m.fwi) heat_add(sc, m, acc, idx, c);
+                    },
+                    r);
+                st_leaves += r.leaves;
+                st_nodes += r.nodes;
+                st_inexact += r.clipped;
+                ++st_queries;
+                if (q.rk_out && l == 0) q.rk_out[src] = sc.radius;
+                __syncwarp();
+                continue;
+            }
             float thr0 = FLT_MAX;
             if (have_prev) {
                 // the float32 screening error (below 2^-21) is far inside the 2^-14 inflation
@@ -753,21 +870,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                     if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
                     else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
                     else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
-                    const float c = ((Es * m.a[idx].w) * norm) * w;
-                    float4 fw = m.fwi[idx], sf = m.sfi[idx];
-                    Fix128 f = f32_to_fix(c);
-                    if (fw.x == fw.x) {
-                        long long xi = (long long)(((double)fw.x - sc.wc[0] + sc.hm_wext) / sc.hm_wbin);
-                        long long zi = (long long)(((double)fw.z - sc.wc[2] + sc.hm_wext) / sc.hm_wbin);
-                        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
-                            fix_atomic_add(acc.hw_lo + xi * sc.hm_bins + zi, acc.hw_hi + xi * sc.hm_bins + zi, f);
-                    }
-                    if (sf.x == sf.x) {
-                        long long xi = (long long)(((double)sf.x - sc.fc[0] + sc.hm_fext) / sc.hm_fbin);
-                        long long zi = (long long)(((double)sf.z - sc.fc[2] + sc.hm_fext) / sc.hm_fbin);
-                        if (xi >= 0 && xi < sc.hm_bins && zi >= 0 && zi < sc.hm_bins)
-                            fix_atomic_add(acc.hf_lo + xi * sc.hm_bins + zi, acc.hf_hi + xi * sc.hm_bins + zi, f);
-                    }
+                    heat_add(sc, m, acc, idx, ((Es * m.a[idx].w) * norm) * w);
                 }
             }
             __syncwarp();

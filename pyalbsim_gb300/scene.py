@@ -61,6 +61,22 @@ def fournier_forand_table(junge_slope: float, n_ratio: float):
     return theta, pf, cdf
 
 
+def henyey_greenstein_table(g: float):
+    """Henyey-Greenstein p(theta) = (1 - g^2) / (4 pi (1 + g^2 - 2 g cos theta)^1.5) on the FF
+    angle grid, with the CDF formed the same way (running sum of p sin theta, normalised), so
+    the sampling tables and the gather's bin weights follow the phase-table path unchanged."""
+    theta = np.linspace(1e-6, np.pi, SCATTER_DIVISIONS, dtype=np.float64)
+    pf = (1.0 - g * g) / (4.0 * np.pi * (1.0 + g * g - 2.0 * g * np.cos(theta)) ** 1.5)
+    cdf = np.cumsum(pf * np.sin(theta))
+    cdf /= cdf[-1]
+    return theta, pf, cdf
+
+
+def henyey_greenstein_backscatter(g: float) -> np.float64:
+    """Backward-hemisphere fraction of HG: (1 - g) / (2 g) ((1 + g) / sqrt(1 + g^2) - 1)."""
+    return np.float64((1.0 - g) / (2.0 * g) * ((1.0 + g) / np.sqrt(1.0 + g * g) - 1.0))
+
+
 def fournier_forand_backscatter(junge_slope: float, n_ratio: float) -> float:
     """Fraction of FF scattering into the backward hemisphere (closed form at 90 deg)."""
     nu = (3.0 - junge_slope) / 2.0
@@ -218,6 +234,7 @@ class SceneModel:
     flying_height: float
     layers: List[LayerModel] = field(default_factory=list)
     heatmap_enabled: bool = False
+    gather_radius: Optional[float] = None  # extension: fixed-radius gather (m), None = k-NN
     heatmap_bins: int = 200
     heatmap_water_extent: float = 1.0
     heatmap_seafloor_extent: float = 10.0
@@ -258,9 +275,14 @@ def build_scene(cfg) -> SceneModel:
     layers: List[LayerModel] = []
     depth_acc = 0.0
     for layer in cfg.water.layers:
-        ff = layer.fournier_forand_parameters
-        th, _, cdf = fournier_forand_table(ff.junge_slope, ff.refractive_index_ratio)
-        bb = fournier_forand_backscatter(ff.junge_slope, ff.refractive_index_ratio)
+        hg = getattr(layer, "henyey_greenstein_g", None)
+        if hg is None:
+            ff = layer.fournier_forand_parameters
+            th, _, cdf = fournier_forand_table(ff.junge_slope, ff.refractive_index_ratio)
+            bb = fournier_forand_backscatter(ff.junge_slope, ff.refractive_index_ratio)
+        else:
+            th, _, cdf = henyey_greenstein_table(float(hg))
+            bb = henyey_greenstein_backscatter(float(hg))
         a0 = _value_at(layer.absorption_coefficient, 0.0, layer.height)
         b0 = _value_at(layer.scattering_coefficient, 0.0, layer.height)
         s0 = _value_at(layer.salinity, 0.0, layer.height)
@@ -351,6 +373,7 @@ def build_scene(cfg) -> SceneModel:
         flying_height=float(cfg.scene.flying_height),
         layers=layers,
         heatmap_enabled=bool(hm.enabled),
+        gather_radius=(float(getattr(cfg, "gather_radius")) if getattr(cfg, "gather_radius", None) else None),
         heatmap_bins=int(hm.bins),
         heatmap_water_extent=float(hm.water_extent),
         heatmap_seafloor_extent=float(hm.seafloor_extent),
