@@ -63,6 +63,9 @@ extern "C" {
 #define ALB_OPT_MAP_CAPACITY 4     /* records per channel to pre-allocate (0 = automatic) */
 #define ALB_OPT_SORT_QUERIES 5     /* 1: sort gather queries spatially before the gather */
 #define ALB_OPT_STREAM 6           /* cudaStream_t (as integer) used for every launch */
+#define ALB_OPT_ADJOINT 7          /* 1: track path scores and accumulate d waveform / d theta
+                                      (extension; set before the first forward trace of a
+                                      simulation; constant layers only) */
 
 /* One homogeneous water layer. The tables are host pointers read once by alb_create. */
 typedef struct AlbLayer {
@@ -93,6 +96,14 @@ typedef struct AlbLayer {
     double a_start, a_end;
     double height;                /* layer thickness, m */
     double top32;                 /* depth of the layer top, rounded to float32 */
+    /* Adjoint (extension, no counterpart in the reference). d ln(alpha)/d theta and
+     * d ln(ssa)/d theta for theta = (a, b, g) of this layer, g the Henyey-Greenstein
+     * asymmetry; hg_g != 0 marks an HG layer (its phase sampling and gather weight depend
+     * on g); dlog_weight_g (ALB_PHASE_DIVISIONS, nullable) = d ln(scatter_weight)/dg. */
+    double dlog_alpha[3];
+    double dlog_ssa[3];
+    double hg_g;
+    const double* dlog_weight_g;
 } AlbLayer;
 
 /* Scene constants derived on the host from SimulationConfig. */
@@ -211,6 +222,24 @@ int alb_knn(AlbCtx* ctx, const float* points, uint64_t m, const double* queries,
 #define ALB_NOALLOC_MAX_POINTS 4096
 int alb_knn_noalloc(const float* points_dev, uint64_t m, const double* queries_dev, uint64_t q, int k,
                     int32_t* idx_dev, double* dist_dev, void* stream);
+
+/* Adjoint (extension, no counterpart in the reference), enabled by ALB_OPT_ADJOINT.
+ * Parameters: 0 water depth, 1 absorption a, 2 scattering b, 3 HG asymmetry g, 4 seafloor
+ * albedo, 5 surface roughness (a, b and g move every layer together). Every record and
+ * query carries the score d ln(p E)/d theta of its path prefix (theta = a, b, g, albedo);
+ * the gather adds c (s_query + s_record + d ln w/d theta) per neighbour into a Jacobian
+ * held like the waveform (128-bit fixed point). The depth moves the seafloor plane and
+ * with it the discrete return step, which has no score form; the host forms that column by
+ * a central difference with common random numbers, so parameter 0 is rejected here.
+ * alb_get_jacobian: d waveform[channel] / d theta[param] (float64 [nbins]).
+ * alb_adjoint: grad[p] = sum over channels and bins of dL_dw[c][b] * J[p][c][b] for
+ * p = 1..5 (dL_dw is float64 [ALB_CHANNELS][nbins]); grad[0] is set to NaN.
+ * alb_export_map_scores: the per-record scores (float[4n]: a, b, g, albedo), in the order
+ * of alb_export_map. */
+#define ALB_ADJ_PARAMS 6
+int alb_get_jacobian(AlbCtx* ctx, int param, int channel, double* out, size_t nbins);
+int alb_adjoint(AlbCtx* ctx, const double* dL_dw, size_t nbins, double* grad);
+int alb_export_map_scores(AlbCtx* ctx, int channel, float* scores, size_t n);
 
 /* Device-side counters of the last trace / gather (events, records, queries, launches). */
 int alb_stats(AlbCtx* ctx, int64_t* out, int n);

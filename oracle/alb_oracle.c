@@ -56,6 +56,7 @@ typedef struct {
     float time;
     float fwi[3];
     float sfi[3];
+    float score[4]; /* adjoint path score d ln(p E)/d (a, b, g, albedo) of the prefix */
 } OrRecord;
 
 typedef struct {
@@ -276,7 +277,21 @@ typedef struct {
     double p[3], d[3];
     float E, tau, taut, t0;
     float fwi[3], sfi[3];
+    double sc[4]; /* adjoint path score (extension) */
 } Ph;
+
+/* Adjoint scores (extension, no counterpart in the reference). The scatter process is
+ * Poisson in the optical depth tau: each increment dtau in layer L multiplies the path
+ * density by e^(-dtau), each scatter by alpha_L, so d ln p / d theta gains
+ * -dtau d ln(alpha_L)/d theta per increment and +d ln(alpha_L)/d theta per scatter; the
+ * energy gains d ln(ssa_L)/d theta per scatter and 1/albedo per seafloor reflection; an
+ * HG layer's direction sampling adds d ln p_HG(mu)/dg. */
+static void score_tau(const AlbSceneParams* P, Ph* ph, int L, double dtau) {
+    for (int i = 0; i < 3; ++i) ph->sc[i] -= dtau * P->layers[L].dlog_alpha[i];
+}
+static double hg_dlogp(double g, double mu) {
+    return -2.0 * g / (1.0 - g * g) - 3.0 * (g - mu) / (1.0 + g * g - 2.0 * g * mu);
+}
 
 static void emit(const Model* m, int pass, Src* s, Ph* ph) {
     const float* Rf = m->p->laser_rot;
@@ -286,6 +301,7 @@ static void emit(const Model* m, int pass, Src* s, Ph* ph) {
     ph->E = 1.0f;
     ph->tau = 0.0f;
     ph->taut = INFINITY;
+    for (int i = 0; i < 4; ++i) ph->sc[i] = 0.0;
     ph->fwi[0] = ph->fwi[1] = ph->fwi[2] = NAN;
     ph->sfi[0] = ph->sfi[1] = ph->sfi[2] = NAN;
     if (pass == ALB_FORWARD) {
@@ -346,6 +362,7 @@ static void record(OrBuf* out, int channel, int photon, int64_t step, const doub
     }
     r.energy = ph->E;
     r.time = ph->t0 + (float)step;
+    for (int i = 0; i < 4; ++i) r.score[i] = (float)ph->sc[i];
     buf_push(out, &r);
 }
 
@@ -370,12 +387,14 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
         double len = norm3(sv[0], sv[1], sv[2]);
         if (st == 2) {
             float a = water_alpha(m, ph->p[1]);
+            score_tau(P, ph, layer_of(m, ph->p[1]), (double)a * len);
             ph->tau = (float)((double)ph->tau + (double)a * len);
             int scatter = ph->tau >= ph->taut;
             for (int i = 0; i < 3; ++i) ph->p[i] = nx[i];
             if (scatter) {
-                record(out, pass == ALB_FORWARD ? ALB_SCATTER : 1, photon, step, ph->p, ph);
                 int L = layer_of(m, ph->p[1]);
+                for (int i = 0; i < 3; ++i) ph->sc[i] += P->layers[L].dlog_alpha[i];
+                record(out, pass == ALB_FORWARD ? ALB_SCATTER : 1, photon, step, ph->p, ph);
                 double uth, phi;
                 float nt;
                 if (s->replay) {
@@ -393,6 +412,8 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
                 double nd[3];
                 rot_apply(ph->d, lv, nd);
                 for (int i = 0; i < 3; ++i) ph->d[i] = nd[i];
+                for (int i = 0; i < 3; ++i) ph->sc[i] += P->layers[L].dlog_ssa[i];
+                if (P->layers[L].hg_g != 0.0) ph->sc[2] += hg_dlogp(P->layers[L].hg_g, cos(th));
                 ph->E = ph->E * water_ssa(m, ph->p[1]);
                 ph->tau = ph->tau - ph->taut;
                 ph->taut = nt;
@@ -439,6 +460,7 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
             if (reflect) {
                 float a = water_alpha(m, ph->p[1]);
+                score_tau(P, ph, layer_of(m, ph->p[1]), (double)a * len);
                 ph->tau = (float)((double)ph->tau + (double)a * len);
             }
         } else { /* seafloor */
@@ -479,6 +501,8 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
             for (int i = 0; i < 3; ++i) ph->d[i] = h[i] / hn;
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
             float a = water_alpha(m, ph->p[1]);
+            score_tau(P, ph, layer_of(m, ph->p[1]), (double)a * len);
+            if (P->seafloor_albedo > 0.0) ph->sc[3] += 1.0 / P->seafloor_albedo;
             ph->tau = (float)((double)ph->tau + (double)a * len);
             ph->E = ph->E * m->alb32;
         }
@@ -679,8 +703,33 @@ static double ggx(double rough, double f0, const double wi_in[3], const double w
     return (double)(float)spec;
 }
 
+/* adjoint (extension): d ln(ggx)/d(alpha^2) of the same vectors, alpha^2 = roughness^4 */
+static double ggx_dlog_da2(double rough, const double wi_in[3], const double wo_in[3]) {
+    double wn = norm3(wi_in[0], wi_in[1], wi_in[2]);
+    double wi[3] = {wi_in[0] / wn, wi_in[1] / wn, wi_in[2] / wn};
+    double on = norm3(wo_in[0], wo_in[1], wo_in[2]);
+    double wo[3] = {wo_in[0] / on, wo_in[1] / on, wo_in[2] / on};
+    double h[3] = {wi[0] + wo[0], wi[1] + wo[1], wi[2] + wo[2]};
+    double hn = norm3(h[0], h[1], h[2]);
+    if (hn == 0.0) hn = 1.0;
+    for (int i = 0; i < 3; ++i) h[i] /= hn;
+    double a = rough * rough, a2 = a * a;
+    double n_wi = wi[1] < 0 ? 0 : (wi[1] > 1 ? 1 : wi[1]);
+    double n_wo = wo[1] < 0 ? 0 : (wo[1] > 1 ? 1 : wo[1]);
+    double nh = h[1] < 0 ? 0 : (h[1] > 1 ? 1 : h[1]);
+    if (!(n_wi > 0 && n_wo > 0)) return 0.0;
+    double den = (a2 - 1.0) * nh * nh + 1.0;
+    double si = sqrt(a2 + (1 - a2) * (n_wi * n_wi)), so = sqrt(a2 + (1 - a2) * (n_wo * n_wo));
+    return 1.0 / a2 - 2.0 * nh * nh / den - (1.0 - n_wi * n_wi) / (2.0 * si * (n_wi + si)) -
+           (1.0 - n_wo * n_wo) / (2.0 * so * (n_wo + so));
+}
+
 /* the map directions are float32 and normalised in float32; the view is float64 */
+static long long scatter_bin(const AlbLayer* L, const float pd_in[3], const double view_in[3]);
 static double scatter_bin_energy(const AlbLayer* L, const float pd_in[3], const double view_in[3]) {
+    return L->scatter_weight[scatter_bin(L, pd_in, view_in)];
+}
+static long long scatter_bin(const AlbLayer* L, const float pd_in[3], const double view_in[3]) {
     volatile float pq = (pd_in[0] * pd_in[0] + pd_in[1] * pd_in[1]) + pd_in[2] * pd_in[2];
     float pn = sqrtf(pq);
     float pd[3] = {pd_in[0] / pn, pd_in[1] / pn, pd_in[2] / pn};
@@ -693,17 +742,22 @@ static double scatter_bin_energy(const AlbLayer* L, const float pd_in[3], const 
     long long i = (long long)((th - (double)EPS32) / width);
     if (i < 0) i = 0;
     if (i > NDIV - 1) i = NDIV - 1;
-    return L->scatter_weight[i];
+    return i;
 }
 
 /* Gather queries of one kind against one map and add into waveform[nbins] (float64).
  * map: pos float[3m], dir float[3m], energy/time float[m], fwi/sfi float[3m] (nullable);
  * queries: pos/dir double[3q], energy/time float[q]. rk_out (nullable) gets r_k per query.
- * heat_w/heat_f (nullable, bins*bins) receive the sampled heatmaps. */
+ * heat_w/heat_f (nullable, bins*bins) receive the sampled heatmaps.
+ * Adjoint (extension): with mscore/qscore (float[4m] / float[4q]: a, b, g, albedo) and jac
+ * (float64 [5][nbins]: a, b, g, albedo, roughness) non-null, every neighbour adds
+ * c (s_query + s_record + d ln w/d theta) to jac. */
 int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const float* mdir, const float* menergy,
                   const float* mtime, const float* mfwi, const float* msfi, int64_t m, const double* qpos,
                   const double* qdir, const float* qenergy, const float* qtime, int64_t nq, double* waveform,
-                  double* rk_out, double* heat_w, double* heat_f, int threads) {
+                  double* rk_out, double* heat_w, double* heat_f, const float* mscore, const float* qscore,
+                  double* jac, int threads) {
+    const int nj = (mscore && qscore && jac) ? 5 : 0;
     int k = p->k;
     int64_t nb = 2 * p->steps;
     const double R = p->gather_radius;  /* extension: > 0 selects the fixed-radius gather */
@@ -714,7 +768,8 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
     nthreads = omp_get_max_threads();
 #endif
     int hb = p->heatmap_enabled ? p->heatmap_bins * p->heatmap_bins : 0;
-    double* priv = (double*)calloc((size_t)nthreads * (nb + 2 * hb), sizeof(double));
+    const size_t stride = (size_t)nb + 2 * hb + (size_t)nj * nb;
+    double* priv = (double*)calloc((size_t)nthreads * stride, sizeof(double));
     int err = 0;
 #ifdef _OPENMP
 #pragma omp parallel
@@ -724,9 +779,10 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
 #ifdef _OPENMP
         tid = omp_get_thread_num();
 #endif
-        double* wf = priv + (size_t)tid * (nb + 2 * hb);
+        double* wf = priv + (size_t)tid * stride;
         double* hw = wf + nb;
         double* hf = hw + hb;
+        double* jp = hf + hb;
         int64_t ccap = R > 0.0 ? 64 : k;
         Cand* c = (Cand*)malloc((size_t)ccap * sizeof(Cand));
 #ifdef _OPENMP
@@ -791,6 +847,21 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                     continue;
                 }
                 wf[bin] += contrib;
+                if (nj) {
+                    const float* sq = qscore + 4 * q;
+                    const float* sp = mscore + 4 * (int64_t)id;
+                    double d[5] = {(double)sq[0] + sp[0], (double)sq[1] + sp[1], (double)sq[2] + sp[2],
+                                   (double)sq[3] + sp[3], 0.0};
+                    if (channel == ALB_SCATTER && p->layers[L].dlog_weight_g)
+                        d[2] += p->layers[L].dlog_weight_g[scatter_bin(&p->layers[L], df, view)];
+                    if (channel == ALB_BOTTOM_REFLECTION && p->seafloor_albedo > 0.0) d[3] += 1.0 / p->seafloor_albedo;
+                    if (channel == ALB_SURFACE_REFLECTION) {
+                        double wi[3] = {-(double)df[0], -(double)df[1], -(double)df[2]};
+                        double r = p->roughness;
+                        d[4] = 4.0 * r * r * r * ggx_dlog_da2(r, wi, view);
+                    }
+                    for (int t = 0; t < 5; ++t) jp[(int64_t)t * nb + bin] += contrib * d[t];
+                }
                 if (hb && mfwi) {
                     const float* fw = mfwi + 3 * id;
                     const float* sf = msfi + 3 * id;
@@ -814,8 +885,9 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
         free(c);
     }
     for (int t = 0; t < nthreads; ++t) {
-        const double* wf = priv + (size_t)t * (nb + 2 * hb);
+        const double* wf = priv + (size_t)t * stride;
         for (int64_t b = 0; b < nb; ++b) waveform[b] += wf[b];
+        for (int64_t b = 0; b < (int64_t)nj * nb; ++b) jac[b] += wf[nb + 2 * hb + b];
         if (hb && heat_w)
             for (int b = 0; b < hb; ++b) {
                 heat_w[b] += wf[nb + b];

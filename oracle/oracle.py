@@ -51,6 +51,7 @@ class _Rec(C.Structure):
         ("time", C.c_float),
         ("fwi", C.c_float * 3),
         ("sfi", C.c_float * 3),
+        ("score", C.c_float * 4),
     ]
 
 
@@ -65,6 +66,7 @@ _REC_DTYPE = np.dtype(
         ("time", np.float32),
         ("fwi", np.float32, 3),
         ("sfi", np.float32, 3),
+        ("score", np.float32, 4),
     ],
     align=True,
 )
@@ -92,7 +94,9 @@ def _load():
         lib.oracle_free.argtypes = [C.POINTER(_Trace)]
         lib.oracle_record_size.restype = C.c_int
         lib.oracle_knn.argtypes = [P, C.c_int64, P, C.c_int64, C.c_int, P, P, C.c_int]
-        lib.oracle_gather.argtypes = [P, C.c_int, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P, P, C.c_int]
+        lib.oracle_gather.argtypes = [
+            P, C.c_int, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P, P, P, P, P, C.c_int
+        ]
         if lib.oracle_record_size() != _REC_DTYPE.itemsize:
             raise RuntimeError("oracle record layout mismatch")
         _lib = lib
@@ -157,8 +161,10 @@ class Oracle:
             raise IndexError("fewer map points than k")
         return dist, idx
 
-    def gather(self, channel, m, q, waveform, heat_w=None, heat_f=None):
-        """m: dict pos/dir/energy/time/fwi/sfi (float32); q: dict pos/dir (float64), energy/time."""
+    def gather(self, channel, m, q, waveform, heat_w=None, heat_f=None, jac=None):
+        """m: dict pos/dir/energy/time/fwi/sfi (float32); q: dict pos/dir (float64), energy/time.
+        jac (float64 [5, nbins], nullable) receives d waveform / d (a, b, g, albedo,
+        roughness) from the "score" entries of m and q (float32 [n, 4])."""
         n = len(m["energy"])
         nq = len(q["energy"])
         rk = np.empty(nq, np.float64)
@@ -167,10 +173,14 @@ class Oracle:
         qd = np.ascontiguousarray(q["dir"], np.float64)
         qe = np.ascontiguousarray(q["energy"], np.float32)
         qt = np.ascontiguousarray(q["time"], np.float32)
+        ms = qs = None
+        if jac is not None:
+            ms = np.ascontiguousarray(m["score"], np.float32)
+            qs = np.ascontiguousarray(q["score"], np.float32)
         rc = self.lib.oracle_gather(
             C.byref(self.params), channel, _p(arr["pos"]), _p(arr["dir"]), _p(arr["energy"]), _p(arr["time"]),
             _p(arr.get("fwi")), _p(arr.get("sfi")), n, _p(qp), _p(qd), _p(qe), _p(qt), nq, _p(waveform), _p(rk),
-            _p(heat_w), _p(heat_f), self.threads,
+            _p(heat_w), _p(heat_f), _p(ms), _p(qs), _p(jac), self.threads,
         )
         if rc == -2:
             raise IndexError(f"photon map of channel {channel} holds {n} records, fewer than k")
@@ -191,6 +201,7 @@ def maps_from_records(recs, channels=4):
             time=r["time"].astype(np.float32),
             fwi=r["fwi"].astype(np.float32),
             sfi=r["sfi"].astype(np.float32),
+            score=r["score"].astype(np.float32),
             photon=r["photon"],
             step=r["step"],
         )
@@ -201,12 +212,15 @@ def queries_from_records(recs):
     out = {}
     for kind in range(3):
         r = recs[recs["channel"] == kind]
-        out[kind] = dict(pos=r["pos"], dir=r["dir"], energy=r["energy"], time=r["time"], photon=r["photon"])
+        out[kind] = dict(pos=r["pos"], dir=r["dir"], energy=r["energy"], time=r["time"], photon=r["photon"],
+                         score=r["score"].astype(np.float32))
     return out
 
 
-def oracle_run(scene, n_fwd, n_bwd, seed=0, replay_fwd=None, replay_bwd=None, threads=0):
-    """Forward + maps + backward + gathers; returns dict with waveforms (float64 [4, nbins])."""
+def oracle_run(scene, n_fwd, n_bwd, seed=0, replay_fwd=None, replay_bwd=None, threads=0, adjoint=False):
+    """Forward + maps + backward + gathers; returns dict with waveforms (float64 [4, nbins])
+    and, with adjoint=True, "jacobian" (float64 [5, 4, nbins]: d waveform / d (a, b, g,
+    albedo, roughness))."""
     orc = Oracle(scene, threads=threads)
     frec, fexit = orc.trace(True, n_fwd, seed=seed, replay=replay_fwd)
     maps = maps_from_records(frec)
@@ -218,13 +232,16 @@ def oracle_run(scene, n_fwd, n_bwd, seed=0, replay_fwd=None, replay_bwd=None, th
     heat_w = np.zeros(hb, np.float64) if scene.heatmap_enabled else None
     heat_f = np.zeros(hb, np.float64) if scene.heatmap_enabled else None
     rks = {}
+    jac = np.zeros((4, 5, nb), np.float64) if adjoint else None
     for ch, kind in ((0, 0), (1, 1), (2, 2), (3, 2)):
         if len(qs[kind]["energy"]) == 0:
             continue
-        rks[ch] = orc.gather(ch, maps[ch], qs[kind], wf[ch], heat_w, heat_f)
+        rks[ch] = orc.gather(ch, maps[ch], qs[kind], wf[ch], heat_w, heat_f,
+                             jac=jac[ch] if adjoint else None)
     return dict(
         waveform=wf, maps=maps, queries=qs, fwd_exit=fexit, bwd_exit=bexit, rk=rks,
         heat_water=heat_w, heat_floor=heat_f, heat_radius=orc.hm_radius,
+        jacobian=jac.transpose(1, 0, 2).copy() if adjoint else None,
     )
 
 

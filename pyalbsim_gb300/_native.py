@@ -32,6 +32,8 @@ ALB_OPT_PRECISE = 3
 ALB_OPT_MAP_CAPACITY = 4
 ALB_OPT_SORT_QUERIES = 5
 ALB_OPT_STREAM = 6
+ALB_OPT_ADJOINT = 7
+ALB_ADJ_PARAMS = 6  # depth, a, b, g, albedo, roughness
 
 PHASE_DIVISIONS = 18000
 
@@ -60,6 +62,10 @@ class AlbLayer(C.Structure):
         ("a_end", C.c_double),
         ("height", C.c_double),
         ("top32", C.c_double),
+        ("dlog_alpha", C.c_double * 3),
+        ("dlog_ssa", C.c_double * 3),
+        ("hg_g", C.c_double),
+        ("dlog_weight_g", C.POINTER(C.c_double)),
     ]
 
 
@@ -107,6 +113,9 @@ class AlbReplay(C.Structure):
 
 
 EXPORTED = [
+    "alb_adjoint",
+    "alb_export_map_scores",
+    "alb_get_jacobian",
     "alb_create",
     "alb_destroy",
     "alb_last_error",
@@ -169,6 +178,9 @@ def load_library(path: str = LIB_PATH):
     lib.alb_phase_times.argtypes = [_P, _P, _P, _P, C.c_int]
     lib.alb_reset.argtypes = [_P]
     lib.alb_knn_noalloc.argtypes = [_P, C.c_uint64, _P, C.c_uint64, C.c_int, _P, _P, _P]
+    lib.alb_get_jacobian.argtypes = [_P, C.c_int, C.c_int, _P, C.c_size_t]
+    lib.alb_adjoint.argtypes = [_P, _P, C.c_size_t, _P]
+    lib.alb_export_map_scores.argtypes = [_P, C.c_int, _P, C.c_size_t]
     _lib = lib
     return lib
 
@@ -253,6 +265,14 @@ def scene_struct(scene: SceneModel):
             L.lut_alpha = la.ctypes.data_as(C.POINTER(C.c_double))
             L.n_kind, L.n_start, L.n_end = layer.n_profile
             L.a_kind, L.a_start, L.a_end = layer.a_profile
+        for j in range(3):
+            L.dlog_alpha[j] = float(layer.dlog_alpha[j])
+            L.dlog_ssa[j] = float(layer.dlog_ssa[j])
+        L.hg_g = float(layer.hg_g)
+        if layer.dlog_weight_g is not None:
+            dw = np.ascontiguousarray(layer.dlog_weight_g, dtype=np.float64)
+            keep.append(dw)
+            L.dlog_weight_g = dw.ctypes.data_as(C.POINTER(C.c_double))
     return p, keep
 
 
@@ -390,6 +410,30 @@ class NativeContext:
             )
         )
         return dict(pos=pos, dir=d, energy=e, time=t, id=pid, rk=rk, rk2=rk2)
+
+    def jacobian(self) -> np.ndarray:
+        """d waveform / d (a, b, g, albedo, roughness): float64 [5, channels, nbins]."""
+        nb = self.scene.n_bins
+        out = np.zeros((ALB_ADJ_PARAMS - 1, 4, nb), np.float64)
+        for p in range(1, ALB_ADJ_PARAMS):
+            for c in range(4):
+                self._check(self.lib.alb_get_jacobian(self.h, p, c, _ptr(out[p - 1, c]), nb))
+        return out
+
+    def adjoint(self, dL_dw: np.ndarray) -> np.ndarray:
+        """grad[1:] = sum dL_dw * J for (a, b, g, albedo, roughness); grad[0] (depth) is NaN."""
+        d = np.ascontiguousarray(dL_dw, np.float64)
+        if d.shape != (4, self.scene.n_bins):
+            raise ValueError("dL_dw must have shape (channels, nbins)")
+        g = np.empty(ALB_ADJ_PARAMS, np.float64)
+        self._check(self.lib.alb_adjoint(self.h, _ptr(d), self.scene.n_bins, _ptr(g)))
+        return g
+
+    def export_map_scores(self, channel: int) -> np.ndarray:
+        n = self.map_size(channel)
+        out = np.empty((n, 4), np.float32)
+        self._check(self.lib.alb_export_map_scores(self.h, channel, _ptr(out), n))
+        return out
 
     def knn(self, points: np.ndarray, queries: np.ndarray, k: int):
         pts = np.ascontiguousarray(points, dtype=np.float32)

@@ -1,0 +1,158 @@
+"""Differentiable waveform (extension: the reference has no derivatives).
+
+Parameters, in this order: water depth, absorption a, scattering b, Henyey-Greenstein
+asymmetry g, seafloor albedo, surface roughness. a, b and g are set on every water layer
+(constant layers only); the depth is the sum of the layer heights and moves the lowest
+layer's floor.
+
+Columns a, b, g, albedo and roughness come from the device adjoint (path scores carried by
+every record and query, accumulated in the same gather as the waveform). The depth moves
+the seafloor plane and with it the discrete integrator step at which a photon returns, so
+its column is a central difference with common random numbers: the same Philox streams
+traced at depth +- h.
+
+``WaveformFunction`` wraps one simulation as a ``torch.autograd.Function``: forward returns
+the float64 waveform [channels, nbins]; backward contracts the incoming gradient with the
+Jacobian.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+from pyalbsim_gb300.config.gpu import GpuRunOptions
+from pyalbsim_gb300.engine import GpuEngine
+
+PARAMS = ("depth", "absorption", "scattering", "asymmetry", "seafloor_albedo", "roughness")
+
+
+def parameters_of(cfg) -> np.ndarray:
+    """The six parameters of a configuration (g = 0 for a Fournier-Forand water column)."""
+    layers = cfg.water.layers
+    top = layers[0]
+    g = getattr(top, "henyey_greenstein_g", None)
+    return np.array([
+        float(sum(float(L.height) for L in layers)),
+        float(top.absorption_coefficient),
+        float(top.scattering_coefficient),
+        0.0 if g is None else float(g),
+        float(cfg.sea_floor.albedo),
+        float(cfg.sea_surface.roughness),
+    ])
+
+
+def with_parameters(cfg, params: Sequence[float]):
+    """A copy of ``cfg`` with the six parameters applied (g only on HG layers)."""
+    depth, a, b, g, albedo, rough = (float(x) for x in params)
+    layers = list(cfg.water.layers)
+    above = sum(float(L.height) for L in layers[:-1])
+    if not depth > above:
+        raise ValueError("depth must exceed the height of the layers above the lowest one")
+    out = []
+    for i, L in enumerate(layers):
+        kw = dict(absorption_coefficient=a, scattering_coefficient=b)
+        if getattr(L, "henyey_greenstein_g", None) is not None:
+            kw["henyey_greenstein_g"] = g
+        if i == len(layers) - 1:
+            kw["height"] = depth - above
+        out.append(dataclasses.replace(L, **kw))
+    return dataclasses.replace(
+        cfg,
+        water=dataclasses.replace(cfg.water, layers=tuple(out)),
+        sea_floor=dataclasses.replace(cfg.sea_floor, albedo=albedo),
+        sea_surface=dataclasses.replace(cfg.sea_surface, roughness=rough),
+    )
+
+
+def _run(cfg, n_fwd: int, n_bwd: int, seed: int, options: GpuRunOptions, adjoint: bool):
+    eng = GpuEngine(cfg, dataclasses.replace(options, adjoint=adjoint))
+    try:
+        eng.forward(n_fwd, seed)
+        eng.build_maps()
+        eng.backward(n_bwd, seed)
+        w = eng.waveform_array(f64=True)
+        j = eng.jacobian() if adjoint else None
+    finally:
+        eng.close()
+    return w, j
+
+
+def simulate_with_jacobian(
+    cfg,
+    n_fwd: int,
+    n_bwd: int,
+    seed: int,
+    options: Optional[GpuRunOptions] = None,
+    depth_step: Optional[float] = None,
+    with_depth: bool = True,
+) -> Tuple[np.ndarray, np.ndarray]:
+    """One simulation: (waveform float64 [4, nbins], Jacobian float64 [6, 4, nbins]).
+
+    depth_step (m): half-width of the depth difference, default max(1% of the depth, 1 cm).
+    with_depth=False leaves the depth column at zero and skips its two extra runs."""
+    options = options or GpuRunOptions()
+    w, j5 = _run(cfg, n_fwd, n_bwd, seed, options, adjoint=True)
+    jac = np.zeros((6,) + w.shape)
+    jac[1:] = j5
+    if with_depth:
+        p = parameters_of(cfg)
+        h = depth_step if depth_step is not None else max(0.01 * p[0], 0.01)
+        plus, minus = p.copy(), p.copy()
+        plus[0] += h
+        minus[0] -= h
+        wp, _ = _run(with_parameters(cfg, plus), n_fwd, n_bwd, seed, options, adjoint=False)
+        wm, _ = _run(with_parameters(cfg, minus), n_fwd, n_bwd, seed, options, adjoint=False)
+        # the simulated time span follows the depth; bins share t = 0 and their width, so
+        # the shifted runs are cut or zero-padded to this run's bins
+        jac[0] = (_fit(wp, w.shape[1]) - _fit(wm, w.shape[1])) / (2.0 * h)
+    return w, jac
+
+
+def _fit(w: np.ndarray, nbins: int) -> np.ndarray:
+    out = np.zeros((w.shape[0], nbins))
+    n = min(nbins, w.shape[1])
+    out[:, :n] = w[:, :n]
+    return out
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class WaveformFunction:
+    """``WaveformFunction.apply(params, cfg, n_fwd, n_bwd, seed, options)`` -> waveform.
+
+    params: float64 tensor [6] (PARAMS order). The depth column is formed only when the
+    depth needs a gradient."""
+
+    _impl = None
+
+    @classmethod
+    def apply(cls, params, cfg, n_fwd, n_bwd, seed, options=None):
+        if cls._impl is None:
+            torch = _torch()
+
+            class _Fn(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, p, cfg_, nf, nb, sd, opts):
+                    vals = p.detach().cpu().double().numpy()
+                    run_cfg = with_parameters(cfg_, vals)
+                    w, jac = simulate_with_jacobian(
+                        run_cfg, nf, nb, sd, opts, with_depth=bool(ctx.needs_input_grad[0])
+                    )
+                    ctx.save_for_backward(torch.from_numpy(jac))
+                    return torch.from_numpy(w).to(p.device)
+
+                @staticmethod
+                def backward(ctx, g):
+                    (jac,) = ctx.saved_tensors
+                    grad = torch.einsum("pcb,cb->p", jac.to(g.device), g.double())
+                    return grad, None, None, None, None, None
+
+            cls._impl = _Fn
+        return cls._impl.apply(params, cfg, n_fwd, n_bwd, seed, options)

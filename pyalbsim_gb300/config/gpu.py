@@ -24,3 +24,6 @@ class GpuRunOptions:
     # rounding (per-photon reproducible against the CPU restatement); precise=False: the
     # float32 tracer, equal in distribution. Replayed variates always use the precise one.
     precise: bool = False
+    # adjoint=True (extension): every record and query carries its path score and the
+    # gather accumulates d waveform / d (a, b, g, albedo, roughness) beside the waveform
+    adjoint: bool = False

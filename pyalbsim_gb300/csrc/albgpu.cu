@@ -106,6 +106,7 @@ struct AlbCtx {
     float4* qb[3] = {nullptr, nullptr, nullptr};
     float4* qc[3] = {nullptr, nullptr, nullptr};
     uint32_t* qid[3] = {nullptr, nullptr, nullptr};
+    float4* qs[3] = {nullptr, nullptr, nullptr};  // adjoint query scores
     uint32_t* qperm[3] = {nullptr, nullptr, nullptr};
     double* qrk[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     uint64_t qcap[3] = {0, 0, 0}, qcap_b[3] = {0}, qcap_c[3] = {0}, qid_cap[3] = {0}, qperm_cap[3] = {0};
@@ -117,6 +118,8 @@ struct AlbCtx {
     unsigned long long* wf = nullptr;  // lo words then hi words, [2][channels][nbins]
     unsigned long long* hm = nullptr;  // sampled heatmaps, [2 maps][2 words][bins*bins]
     unsigned* hm_radius = nullptr;
+    // adjoint Jacobian: lo words then hi words, [2][kJacParams][channels][nbins]
+    unsigned long long* jac = nullptr;
     // exit states
     double* ex_pos = nullptr;
     double* ex_dir = nullptr;
@@ -260,10 +263,28 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         s.wc[i] = p->water_center[i];
         s.fc[i] = p->floor_center[i];
     }
+    s.adjoint = 0;
+    s.inv_albedo = p->seafloor_albedo > 0.0 ? (float)(1.0 / p->seafloor_albedo) : 0.f;
+    s.dla2_drough = (float)(4.0 * p->roughness * p->roughness * p->roughness);
     const int N = ALB_PHASE_DIVISIONS;
     for (int l = 0; l < p->n_layers; ++l) {
         const AlbLayer& L = p->layers[l];
         if (!L.phase_theta || !L.phase_cdf || !L.phase_slope || !L.scatter_weight) return bad("missing layer table");
+        for (int i = 0; i < 3; ++i) {
+            s.adj_dla[l][i] = (float)L.dlog_alpha[i];
+            s.adj_dls[l][i] = (float)L.dlog_ssa[i];
+        }
+        s.layer_hg_g[l] = (float)L.hg_g;
+        s.layer_dlw_g[l] = nullptr;
+        if (L.dlog_weight_g) {
+            std::vector<float> d(N);
+            for (int i = 0; i < N; ++i) d[i] = (float)L.dlog_weight_g[i];
+            float* dd;
+            if (cudaMalloc(&dd, N * sizeof(float)) != cudaSuccess) return bad("table allocation failed");
+            ctx->tables.push_back(dd);
+            cudaMemcpy(dd, d.data(), N * sizeof(float), cudaMemcpyHostToDevice);
+            s.layer_dlw_g[l] = dd;
+        }
         s.layer_bottom[l] = L.bottom_depth;
         s.layer_speed[l] = L.speed;
         s.layer_alpha[l] = L.alpha;
@@ -370,15 +391,16 @@ extern "C" void alb_destroy(AlbCtx* ctx) {
     for (void* p : ctx->tables) cudaFree(p);
     for (int c = 0; c < ALB_CHANNELS; ++c) {
         cudaFree(ctx->rec[c].a); cudaFree(ctx->rec[c].b); cudaFree(ctx->rec[c].fwi); cudaFree(ctx->rec[c].sfi);
-        cudaFree(ctx->rec[c].id);
+        cudaFree(ctx->rec[c].id); cudaFree(ctx->rec[c].sco);
         MapIndex& m = ctx->map[c];
-        cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id); cudaFree(m.box_lo); cudaFree(m.box_hi);
+        cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id); cudaFree(m.sco);
+        cudaFree(m.box_lo); cudaFree(m.box_hi);
     }
     for (int k = 0; k < 3; ++k) {
         cudaFree(ctx->qa[k]); cudaFree(ctx->qb[k]); cudaFree(ctx->qc[k]); cudaFree(ctx->qid[k]); cudaFree(ctx->qperm[k]);
-        cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]);
+        cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]); cudaFree(ctx->qs[k]);
     }
-    cudaFree(ctx->wf); cudaFree(ctx->hm); cudaFree(ctx->hm_radius);
+    cudaFree(ctx->wf); cudaFree(ctx->hm); cudaFree(ctx->hm_radius); cudaFree(ctx->jac);
     cudaFree(ctx->ex_pos); cudaFree(ctx->ex_dir); cudaFree(ctx->ex_f);
     cudaFree(ctx->d_rec_count); cudaFree(ctx->d_q_count); cudaFree(ctx->d_err); cudaFree(ctx->d_stats);
     if (ctx->ev_ready)
@@ -398,6 +420,21 @@ extern "C" int alb_set_option(AlbCtx* ctx, int key, int64_t v) {
             ctx->st = (cudaStream_t)(intptr_t)v;
             ctx->ws.set_stream(ctx->st);
             break;
+        case ALB_OPT_ADJOINT: {
+            for (int c = 0; c < ALB_CHANNELS; ++c)
+                if (ctx->h_rec_count[c]) return fail(ctx, ALB_ERR_STATE, "set ALB_OPT_ADJOINT before the first forward trace");
+            if (v) {
+                for (int l = 0; l < ctx->sc.n_layers; ++l)
+                    if (ctx->sc.layer_prof[l]) return fail(ctx, ALB_ERR_INVALID, "the adjoint needs constant layers");
+                if (!ctx->jac) {
+                    const size_t words = (size_t)2 * kJacParams * ALB_CHANNELS * ctx->sc.nbins;
+                    CK(cudaMalloc(&ctx->jac, words * 8));
+                    CK(cudaMemset(ctx->jac, 0, words * 8));
+                }
+            }
+            ctx->sc.adjoint = v ? 1 : 0;
+            break;
+        }
         default: return fail(ctx, ALB_ERR_INVALID, "unknown option");
     }
     return ALB_OK;
@@ -411,9 +448,10 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
     RecordStore& r = ctx->rec[c];
     bool want_hm = ctx->sc.heatmap != 0;
     bool want_id = ctx->keep_ids != 0;
-    if (r.cap >= need && (!want_id || r.id) && (!want_hm || r.fwi)) return ALB_OK;
+    bool want_sco = ctx->sc.adjoint != 0;
+    if (r.cap >= need && (!want_id || r.id) && (!want_hm || r.fwi) && (!want_sco || r.sco)) return ALB_OK;
     uint64_t cap = std::max<uint64_t>(need + need / 16, 1024);
-    float4 *a, *b, *fwi = nullptr, *sfi = nullptr;
+    float4 *a, *b, *fwi = nullptr, *sfi = nullptr, *sco = nullptr;
     uint32_t* id = nullptr;
     CK(cudaMalloc(&a, cap * 16));
     CK(cudaMalloc(&b, cap * 16));
@@ -422,6 +460,7 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
         CK(cudaMalloc(&sfi, cap * 16));
     }
     if (want_id) CK(cudaMalloc(&id, cap * 4));
+    if (want_sco) CK(cudaMalloc(&sco, cap * 16));
     if (keep) {
         CK(cudaMemcpyAsync(a, r.a, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
         CK(cudaMemcpyAsync(b, r.b, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
@@ -430,16 +469,17 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
             CK(cudaMemcpyAsync(sfi, r.sfi, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
         }
         if (want_id && r.id) CK(cudaMemcpyAsync(id, r.id, keep * 4, cudaMemcpyDeviceToDevice, ctx->st));
+        if (want_sco && r.sco) CK(cudaMemcpyAsync(sco, r.sco, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
     }
     CK(cudaStreamSynchronize(ctx->st));
-    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id);
-    r.a = a; r.b = b; r.fwi = fwi; r.sfi = sfi; r.id = id; r.cap = cap;
+    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
+    r.a = a; r.b = b; r.fwi = fwi; r.sfi = sfi; r.id = id; r.sco = sco; r.cap = cap;
     return ALB_OK;
 }
 
 static void release_records(AlbCtx* ctx, int c) {
     RecordStore& r = ctx->rec[c];
-    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id);
+    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
     r = RecordStore{};
 }
 
@@ -459,6 +499,7 @@ static int restore_records(AlbCtx* ctx, int c, uint64_t need) {
             CK(cudaMemcpyAsync(r.sfi, m.sfi, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
         }
         if (r.id && m.id) CK(cudaMemcpyAsync(r.id, m.id, n * 4, cudaMemcpyDeviceToDevice, ctx->st));
+        if (r.sco && m.sco) CK(cudaMemcpyAsync(r.sco, m.sco, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
     }
     ctx->rec_released[c] = false;
@@ -466,11 +507,11 @@ static int restore_records(AlbCtx* ctx, int c, uint64_t need) {
 }
 
 static int ensure_queries(AlbCtx* ctx, int k, uint64_t need) {
-    if (ctx->qcap[k] >= need && (!ctx->keep_ids || ctx->qid[k])) return ALB_OK;
+    if (ctx->qcap[k] >= need && (!ctx->keep_ids || ctx->qid[k]) && (!ctx->sc.adjoint || ctx->qs[k])) return ALB_OK;
     uint64_t cap = std::max<uint64_t>(need + need / 4, 1024);
     cudaFree(ctx->qa[k]); cudaFree(ctx->qb[k]); cudaFree(ctx->qc[k]); cudaFree(ctx->qid[k]); cudaFree(ctx->qperm[k]);
-    cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]);
-    ctx->qid[k] = nullptr; ctx->qrk[k][0] = ctx->qrk[k][1] = nullptr;
+    cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]); cudaFree(ctx->qs[k]);
+    ctx->qid[k] = nullptr; ctx->qrk[k][0] = ctx->qrk[k][1] = nullptr; ctx->qs[k] = nullptr;
     CK(cudaMalloc(&ctx->qa[k], cap * 16));
     CK(cudaMalloc(&ctx->qb[k], cap * 16));
     CK(cudaMalloc(&ctx->qc[k], cap * 16));
@@ -480,6 +521,7 @@ static int ensure_queries(AlbCtx* ctx, int k, uint64_t need) {
         CK(cudaMalloc(&ctx->qrk[k][0], cap * 8));
         CK(cudaMalloc(&ctx->qrk[k][1], cap * 8));
     }
+    if (ctx->sc.adjoint) CK(cudaMalloc(&ctx->qs[k], cap * 16));
     ctx->qcap[k] = cap;
     return ALB_OK;
 }
@@ -492,6 +534,7 @@ static TraceOut make_out(AlbCtx* ctx) {
         o.rec_fwi[c] = ctx->rec[c].fwi;
         o.rec_sfi[c] = ctx->rec[c].sfi;
         o.rec_id[c] = ctx->rec[c].id;
+        o.rec_sco[c] = ctx->sc.adjoint ? ctx->rec[c].sco : nullptr;
         o.rec_cap[c] = ctx->rec[c].cap;
     }
     o.rec_count = ctx->d_rec_count;
@@ -500,6 +543,7 @@ static TraceOut make_out(AlbCtx* ctx) {
         o.q_b[k] = ctx->qb[k];
         o.q_c[k] = ctx->qc[k];
         o.q_id[k] = ctx->qid[k];
+        o.q_s[k] = ctx->sc.adjoint ? ctx->qs[k] : nullptr;
         o.q_cap[k] = ctx->qcap[k];
     }
     o.q_count = ctx->d_q_count;
@@ -620,6 +664,10 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
     acc.wf_lo = ctx->wf;
     acc.wf_hi = ctx->wf + (size_t)ALB_CHANNELS * ctx->sc.nbins;
     acc.nbins = ctx->sc.nbins;
+    if (ctx->sc.adjoint) {
+        acc.jac_lo = ctx->jac;
+        acc.jac_hi = ctx->jac + (size_t)kJacParams * ALB_CHANNELS * ctx->sc.nbins;
+    }
     if (ctx->sc.heatmap) {
         size_t hb = (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins;
         acc.hw_lo = ctx->hm;
@@ -670,6 +718,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             q.a = ctx->qa[k];
             q.b = ctx->qb[k];
             q.c = ctx->qc[k];
+            q.s = ctx->sc.adjoint ? ctx->qs[k] : nullptr;
             q.n = nq;
             q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
             q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
@@ -817,10 +866,59 @@ extern "C" int alb_get_waveform_f64(AlbCtx* ctx, int c, double* out, size_t nbin
     return ALB_OK;
 }
 
+extern "C" int alb_get_jacobian(AlbCtx* ctx, int param, int c, double* out, size_t nbins) {
+    if (!ctx || !out || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    if (param == 0)
+        return fail(ctx, ALB_ERR_INVALID, "the depth column is a host-side central difference (no score form)");
+    if (param < 1 || param >= ALB_ADJ_PARAMS) return fail(ctx, ALB_ERR_INVALID, "unknown adjoint parameter");
+    if (!ctx->jac) return fail(ctx, ALB_ERR_STATE, "ALB_OPT_ADJOINT is not enabled");
+    const int64_t nb = ctx->sc.nbins;
+    if (nbins < (size_t)nb) return fail(ctx, ALB_ERR_INVALID, "jacobian buffer too small");
+    const size_t off = ((size_t)(param - 1) * ALB_CHANNELS + c) * nb;
+    const size_t half = (size_t)kJacParams * ALB_CHANNELS * nb;
+    std::vector<unsigned long long> lo(nb), hi(nb);
+    CK(cudaMemcpy(lo.data(), ctx->jac + off, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hi.data(), ctx->jac + half + off, nb * 8, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < nb; ++i) out[i] = fix_to_double(lo[i], (long long)hi[i]);
+    return ALB_OK;
+}
+
+extern "C" int alb_adjoint(AlbCtx* ctx, const double* dL_dw, size_t nbins, double* grad) {
+    if (!ctx || !dL_dw || !grad) return ALB_ERR_INVALID;
+    const int64_t nb = ctx->sc.nbins;
+    if (nbins != (size_t)nb) return fail(ctx, ALB_ERR_INVALID, "dL_dw must hold channels * nbins values");
+    grad[0] = std::nan("");
+    std::vector<double> j(nb);
+    for (int p = 1; p < ALB_ADJ_PARAMS; ++p) {
+        double acc = 0.0;
+        for (int c = 0; c < ALB_CHANNELS; ++c) {
+            int rc = alb_get_jacobian(ctx, p, c, j.data(), nb);
+            if (rc) return rc;
+            for (int64_t i = 0; i < nb; ++i) acc += dL_dw[(size_t)c * nb + i] * j[i];
+        }
+        grad[p] = acc;
+    }
+    return ALB_OK;
+}
+
+extern "C" int alb_export_map_scores(AlbCtx* ctx, int c, float* scores, size_t n) {
+    if (!ctx || !scores || c < 0 || c >= ALB_CHANNELS) return ALB_ERR_INVALID;
+    if (!ctx->sc.adjoint) return fail(ctx, ALB_ERR_STATE, "ALB_OPT_ADJOINT is not enabled");
+    const uint64_t m = ctx->h_rec_count[c];
+    if (n < m) return fail(ctx, ALB_ERR_INVALID, "export buffer smaller than the map");
+    if (m == 0) return ALB_OK;
+    const float4* s = ctx->rec_released[c] ? ctx->map[c].sco : ctx->rec[c].sco;
+    if (!s) return fail(ctx, ALB_ERR_STATE, "records carry no scores");
+    CK(cudaMemcpy(scores, s, m * 16, cudaMemcpyDeviceToHost));
+    return ALB_OK;
+}
+
 extern "C" int alb_reset_waveform(AlbCtx* ctx) {
     if (!ctx) return ALB_ERR_INVALID;
     CK(cudaMemsetAsync(ctx->wf, 0, (size_t)2 * ALB_CHANNELS * ctx->sc.nbins * 8, ctx->st));
     if (ctx->hm) CK(cudaMemsetAsync(ctx->hm, 0, (size_t)4 * ctx->sc.hm_bins * ctx->sc.hm_bins * 8, ctx->st));
+    if (ctx->jac)
+        CK(cudaMemsetAsync(ctx->jac, 0, (size_t)2 * kJacParams * ALB_CHANNELS * ctx->sc.nbins * 8, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return ALB_OK;
 }

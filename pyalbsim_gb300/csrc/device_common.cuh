@@ -58,7 +58,26 @@ struct SceneDev {
     double layer_n0[ALB_MAX_LAYERS], layer_n1[ALB_MAX_LAYERS];
     double layer_a0[ALB_MAX_LAYERS], layer_a1[ALB_MAX_LAYERS];
     double layer_h[ALB_MAX_LAYERS], layer_top32[ALB_MAX_LAYERS];
+    // adjoint (extension): path scores for theta = (a, b, g) and the seafloor albedo
+    int32_t adjoint;
+    int32_t pad1;
+    float adj_dla[ALB_MAX_LAYERS][3];  // d ln(alpha) / d theta
+    float adj_dls[ALB_MAX_LAYERS][3];  // d ln(ssa) / d theta
+    float layer_hg_g[ALB_MAX_LAYERS];  // HG asymmetry (0: not an HG layer)
+    const float* layer_dlw_g[ALB_MAX_LAYERS];  // d ln(scatter weight) / dg per bin
+    float inv_albedo;                  // 1 / seafloor albedo (0 when the albedo is 0)
+    float dla2_drough;                 // d (GGX alpha^2) / d roughness = 4 roughness^3
 };
+
+// Path score of one photon for theta = (a, b, g, seafloor albedo).
+struct Score {
+    float a, b, g, l;
+};
+
+// d ln p_HG(mu) / dg for p_HG(mu) = (1 - g^2) / (4 pi (1 + g^2 - 2 g mu)^1.5)
+ALB_HOST_DEVICE float hg_dlogp_dg(float g, float mu) {
+    return -2.f * g / (1.f - g * g) - 3.f * (g - mu) / (1.f + g * g - 2.f * g * mu);
+}
 
 // ---------------------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3", SC'11).

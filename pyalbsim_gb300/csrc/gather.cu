@@ -598,14 +598,39 @@ ALB_DEVICE float ggx_weight(float a2, float f0, float wix, float wiy, float wiz,
 
 // Scatter weight: CDF mass of the angular bin of theta = acos(d_map . view),
 // alb_sim/physics/scatter/energy.py:8-52 (view = normalize(-d_query)).
-ALB_DEVICE float scatter_weight(const SceneDev& sc, int layer, float dx, float dy, float dz, float vx, float vy, float vz) {
+ALB_DEVICE int scatter_bin(const SceneDev& sc, int layer, float dx, float dy, float dz, float vx, float vy, float vz) {
     float n = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
     float c = fmaf(dx, vx, fmaf(dy, vy, dz * vz)) * n;
     c = fminf(fmaxf(c, -1.f), 1.f);
     float th = acosf(c);
     int i = (int)((th - kEps32) / sc.layer_binw[layer]);
-    i = min(max(i, 0), ALB_PHASE_DIVISIONS - 1);
-    return __ldg(sc.layer_weight[layer] + i);
+    return min(max(i, 0), ALB_PHASE_DIVISIONS - 1);
+}
+ALB_DEVICE float scatter_weight(const SceneDev& sc, int layer, float dx, float dy, float dz, float vx, float vy, float vz) {
+    return __ldg(sc.layer_weight[layer] + scatter_bin(sc, layer, dx, dy, dz, vx, vy, vz));
+}
+
+// Adjoint (extension): d ln(ggx_weight) / d(alpha^2), the same vectors as ggx_weight:
+// 1/a2 - 2 Hy^2 / (|H|^2 den) from the distribution term and -(1 - n^2) / (2 s (n + s)),
+// s = sqrt((1 - a2) n^2 + a2), from each Smith G1 factor; the Fresnel term has no a2.
+ALB_DEVICE float ggx_dlog_da2(float a2, float wix, float wiy, float wiz, float wox, float woy, float woz) {
+    float ni = rsqrtf(fmaf(wix, wix, fmaf(wiy, wiy, wiz * wiz)));
+    wix *= ni; wiy *= ni; wiz *= ni;
+    float n_wi = fminf(fmaxf(wiy, 0.f), 1.f);
+    float n_wo = fminf(fmaxf(woy, 0.f), 1.f);
+    if (!(n_wi > 0.f && n_wo > 0.f)) return 0.f;
+    float Hx = wix + wox, Hy = wiy + woy, Hz = wiz + woz;
+    float t = fmaf(Hx, Hx, Hz * Hz);
+    float H2 = fmaf(Hy, Hy, t);
+    float d = 1.f / a2;
+    if (H2 > 0.f && Hy > 0.f) {
+        float den = fmaf(a2 * Hy, Hy, t) / H2;
+        d -= 2.f * (Hy * Hy / H2) / den;
+    }
+    float si = sqrtf(fmaf(1.f - a2, n_wi * n_wi, a2)), so = sqrtf(fmaf(1.f - a2, n_wo * n_wo, a2));
+    d -= (1.f - n_wi * n_wi) / (2.f * si * (n_wi + si));
+    d -= (1.f - n_wo * n_wo) / (2.f * so * (n_wo + so));
+    return d;
 }
 
 // float32 -> 128-bit fixed point (64 fractional bits), integer ops only.
@@ -729,6 +754,32 @@ ALB_DEVICE void warp_radius_visit(const MapDev& m, WarpSmem& s, double qx, doubl
     }
 }
 
+// Adjoint (extension): one neighbour's c (s_query + s_record + d ln w / d theta) into the
+// Jacobian for theta = a, b, g, albedo, roughness (128-bit fixed point, global atomics).
+template <int CHANNEL>
+ALB_DEVICE void jac_add(const SceneDev& sc, const MapDev& m, const Accum& acc, int layer, int bin, uint32_t idx,
+                        float c, float4 sq, float4 pb, float vx, float vy, float vz) {
+    const float4 sp = m.sco ? m.sco[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float d[kJacParams];
+    d[0] = sq.x + sp.x;
+    d[1] = sq.y + sp.y;
+    d[2] = sq.z + sp.z;
+    d[3] = sq.w + sp.w;
+    d[4] = 0.f;
+    if (CHANNEL == ALB_SCATTER && sc.layer_dlw_g[layer])
+        d[2] += __ldg(sc.layer_dlw_g[layer] + scatter_bin(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz));
+    if (CHANNEL == ALB_BOTTOM_REFLECTION) d[3] += sc.inv_albedo;
+    if (CHANNEL == ALB_SURFACE_REFLECTION) d[4] = sc.dla2_drough * ggx_dlog_da2(sc.ggx_a2, -pb.x, -pb.y, -pb.z, vx, vy, vz);
+#pragma unroll
+    for (int p = 0; p < kJacParams; ++p) {
+        const float v = c * d[p];
+        if (v != 0.f) {
+            const uint64_t o = ((uint64_t)p * ALB_CHANNELS + CHANNEL) * acc.nbins + bin;
+            fix_atomic_add(acc.jac_lo + o, acc.jac_hi + o, f32_to_fix(v));
+        }
+    }
+}
+
 // accumulate_to_heatmap (alb_sim/math/accumulate_heatmap.py:6-61) for one neighbour
 ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, uint32_t idx, float c) {
     const float4 fw = m.fwi[idx], sf = m.sfi[idx];
@@ -784,6 +835,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 if (CHANNEL == ALB_BOTTOM_REFLECTION) wconst = (float)(sc.floor_albedo / kPi) * fmaxf(0.f, -qb.y);
                 if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
                 const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
+                const float4 sq = q.s ? q.s[src] : make_float4(0.f, 0.f, 0.f, 0.f);
                 warp_radius_visit(m, s, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, sc.radius,
                     [&](uint32_t idx) {
                         const float4 pb = m.b[idx];
@@ -793,8 +845,12 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                         else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
                         const float c = ((Es * m.a[idx].w) * norm) * w;
                         const int bin = (int)((ts + pb.w) / (float)sc.mult);
-                        if (bin >= 0 && bin < acc.nbins) bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-                        else atomicCAS(err, 0, ALB_ERR_CAPACITY);
+                        if (bin >= 0 && bin < acc.nbins) {
+                            bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                            if (acc.jac_lo) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
+                        } else {
+                            atomicCAS(err, 0, ALB_ERR_CAPACITY);
+                        }
                         if (acc.hw_lo && m.fwi) heat_add(sc, m, acc, idx, c);
                     },
                     r);
@@ -844,6 +900,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
             // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
             const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
+            const float4 sq = q.s ? q.s[src] : make_float4(0.f, 0.f, 0.f, 0.f);
             for (int j = l; j < k; j += 32) {
                 const uint32_t idx = s.ci[j];
                 const float4 pb = m.b[idx];
@@ -855,6 +912,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 const int bin = (int)((ts + pb.w) / (float)sc.mult);
                 if (bin >= 0 && bin < acc.nbins) {
                     bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
+                    if (acc.jac_lo) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
                 } else {
                     atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }

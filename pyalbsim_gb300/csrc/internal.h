@@ -14,6 +14,9 @@
 namespace alb {
 
 constexpr int kMaxLevels = 8;
+// Jacobian columns formed on the device: a, b, g, albedo, roughness (the depth column is a
+// host-side difference)
+constexpr int kJacParams = ALB_ADJ_PARAMS - 1;
 
 // Number of kernels this library has launched (all contexts); read by alb_stats.
 long long launches_total();
@@ -35,6 +38,7 @@ struct RecordStore {
     float4* fwi = nullptr;  // optional
     float4* sfi = nullptr;
     uint32_t* id = nullptr; // optional
+    float4* sco = nullptr;  // adjoint path scores (a, b, g, albedo), optional
     uint64_t cap = 0;
 };
 
@@ -47,7 +51,8 @@ struct MapIndex {
     float4* fwi = nullptr;
     float4* sfi = nullptr;
     uint32_t* id = nullptr;
-    uint64_t a_cap = 0, b_cap = 0, fwi_cap = 0, sfi_cap = 0, id_cap = 0;
+    float4* sco = nullptr;
+    uint64_t a_cap = 0, b_cap = 0, fwi_cap = 0, sfi_cap = 0, id_cap = 0, sco_cap = 0;
     KeyGrid grid{};
     float4* box_lo = nullptr;
     float4* box_hi = nullptr;
@@ -63,6 +68,7 @@ struct MapDev {
     const float4* b;
     const float4* fwi;
     const float4* sfi;
+    const float4* sco;  // adjoint path scores (nullable)
     const float4* box_lo;
     const float4* box_hi;
     uint64_t n;
@@ -77,6 +83,7 @@ struct QueryDev {
     const float4* a;   // x_hi, y_hi, z_hi, energy
     const float4* b;   // dx, dy, dz, time
     const float4* c;   // x_lo, y_lo, z_lo
+    const float4* s;   // adjoint path scores (a, b, g, albedo), nullable
     const uint32_t* perm;  // optional processing order
     uint64_t n;
     double* rk_out;    // optional per-query k-th neighbour distance
@@ -93,6 +100,8 @@ struct Accum {
     unsigned long long* hf_lo;  // sampled seafloor heatmap
     unsigned long long* hf_hi;
     int64_t nbins;
+    unsigned long long* jac_lo;  // adjoint [5 params][channels][nbins] (nullable)
+    unsigned long long* jac_hi;
 };
 
 // Stream-ordered device memory: temporaries come from cudaMallocAsync and are released in
@@ -148,6 +157,7 @@ inline MapDev map_dev(const MapIndex& m) {
     d.b = m.b;
     d.fwi = m.fwi;
     d.sfi = m.sfi;
+    d.sco = m.sco;
     d.box_lo = m.box_lo;
     d.box_hi = m.box_hi;
     d.n = m.n;

@@ -1345,7 +1345,7 @@ int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float 
 // a[i] holds (position, record id) in index order: gather every record field into index
 // order, a last (in place: each thread reads its id before overwriting the entry).
 __global__ void k_finalize(float4* a, float4* __restrict__ b, float4* __restrict__ fwi, float4* __restrict__ sfi,
-                           uint32_t* __restrict__ id, RecordStore rec, uint64_t n) {
+                           uint32_t* __restrict__ id, float4* __restrict__ sco, RecordStore rec, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t r = __float_as_uint(a[i].w);
         b[i] = rec.b[r];
@@ -1354,15 +1354,16 @@ __global__ void k_finalize(float4* a, float4* __restrict__ b, float4* __restrict
             sfi[i] = rec.sfi[r];
         }
         if (id) id[i] = rec.id[r];
+        if (sco) sco[i] = rec.sco[r];
         a[i] = rec.a[r];
     }
 }
 
 void release_map_index(MapIndex& m) {
-    cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id);
-    m.a = m.b = m.fwi = m.sfi = nullptr;
+    cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id); cudaFree(m.sco);
+    m.a = m.b = m.fwi = m.sfi = m.sco = nullptr;
     m.id = nullptr;
-    m.a_cap = m.b_cap = m.fwi_cap = m.sfi_cap = m.id_cap = 0;
+    m.a_cap = m.b_cap = m.fwi_cap = m.sfi_cap = m.id_cap = m.sco_cap = 0;
 }
 
 // Build the k-d index of one channel's n records: records in exact left-balanced k-d order
@@ -1390,11 +1391,12 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
         m.sfi = (float4*)ws.alloc_persistent(m.sfi, m.sfi_cap, n);
     }
     if (rec.id) m.id = (uint32_t*)ws.alloc_persistent_u32(m.id, m.id_cap, n);
-    if (!m.b || (rec.fwi && (!m.fwi || !m.sfi)) || (rec.id && !m.id)) return -1;
+    if (rec.sco) m.sco = (float4*)ws.alloc_persistent(m.sco, m.sco_cap, n);
+    if (!m.b || (rec.fwi && (!m.fwi || !m.sfi)) || (rec.id && !m.id) || (rec.sco && !m.sco)) return -1;
     // one record per thread: the gathers are random, so many loads in flight matter
     const unsigned blocks = (unsigned)((n + 255) / 256);
     k_finalize<<<blocks, 256, 0, st>>>(m.a, m.b, rec.fwi ? m.fwi : nullptr, rec.fwi ? m.sfi : nullptr,
-                                       rec.id ? m.id : nullptr, rec, n);
+                                       rec.id ? m.id : nullptr, rec.sco ? m.sco : nullptr, rec, n);
     note_launch();
     build_box_tree(ws, m, st);
     return 0;

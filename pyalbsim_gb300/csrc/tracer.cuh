@@ -28,6 +28,7 @@ struct TraceOut {
     float4* rec_fwi[ALB_CHANNELS];  // nullable: first-water / seafloor interaction points
     float4* rec_sfi[ALB_CHANNELS];
     uint32_t* rec_id[ALB_CHANNELS];  // nullable
+    float4* rec_sco[ALB_CHANNELS];   // adjoint path scores (nullable)
     unsigned long long* rec_count;   // [ALB_CHANNELS], cumulative over forward calls
     unsigned long long rec_cap[ALB_CHANNELS];
     // backward gather queries, per kind (bottom, scatter, surface)
@@ -35,6 +36,7 @@ struct TraceOut {
     float4* q_b[3];  // dx, dy, dz, time
     float4* q_c[3];  // x_lo, y_lo, z_lo, 0   (x = x_hi + x_lo to ~1e-14)
     uint32_t* q_id[3];
+    float4* q_s[3];  // adjoint path scores (nullable)
     unsigned long long* q_count;  // [3]
     unsigned long long q_cap[3];
     // per-photon final states (nullable)
@@ -53,7 +55,31 @@ struct Ph {
     float E, tau, taut, t0;
     float fwi[3], sfi[3];
     int64_t s;
+    Score sc;  // adjoint: d ln(p E) / d (a, b, g, albedo) of the path so far
 };
+
+// Adjoint score updates (extension). Free paths: tau grows by alpha |step| per step and a
+// scatter happens where it reaches an Exp(1) target, so the path density carries
+// alpha e^(-tau) per scatter and e^(-tau) per survival: an optical-depth increment dtau in
+// layer L adds -dtau d ln(alpha_L)/d theta; a scatter adds +d ln(alpha_L)/d theta for its
+// density and d ln(ssa_L)/d theta for its energy factor; HG sampling adds
+// d ln p_HG(mu)/dg; a seafloor reflection adds 1/albedo.
+ALB_DEVICE void score_tau(const SceneDev& sc, Score& s, int L, float dtau) {
+    s.a = fmaf(-dtau, sc.adj_dla[L][0], s.a);
+    s.b = fmaf(-dtau, sc.adj_dla[L][1], s.b);
+    s.g = fmaf(-dtau, sc.adj_dla[L][2], s.g);
+}
+ALB_DEVICE void score_scatter_density(const SceneDev& sc, Score& s, int L) {
+    s.a += sc.adj_dla[L][0];
+    s.b += sc.adj_dla[L][1];
+    s.g += sc.adj_dla[L][2];
+}
+ALB_DEVICE void score_scatter_after(const SceneDev& sc, Score& s, int L, float mu) {
+    s.a += sc.adj_dls[L][0];
+    s.b += sc.adj_dls[L][1];
+    s.g += sc.adj_dls[L][2];
+    if (sc.layer_hg_g[L] != 0.f) s.g += hg_dlogp_dg(sc.layer_hg_g[L], mu);
+}
 
 ALB_DEVICE void set_err(int* err, int code) { atomicCAS(err, 0, code); }
 
@@ -440,10 +466,12 @@ ALB_DEVICE void emit_event(const TraceOut& out, int channel, int qkind, const Ph
                 out.rec_sfi[channel][slot] = make_float4(ph.sfi[0], ph.sfi[1], ph.sfi[2], 0.f);
             }
             if (out.rec_id[channel]) out.rec_id[channel][slot] = pid;
+            if (out.rec_sco[channel]) out.rec_sco[channel][slot] = make_float4(ph.sc.a, ph.sc.b, ph.sc.g, ph.sc.l);
         }
     } else {
         unsigned long long slot = warp_append(out.q_count, qkind);
         if (slot < out.q_cap[qkind]) {
+            if (out.q_s[qkind]) out.q_s[qkind][slot] = make_float4(ph.sc.a, ph.sc.b, ph.sc.g, ph.sc.l);
             float xh = (float)x, yh = (float)y, zh = (float)z;
             out.q_a[qkind][slot] = make_float4(xh, yh, zh, ph.E);
             out.q_b[qkind][slot] = make_float4((float)ph.dx, (float)ph.dy, (float)ph.dz, t);
@@ -515,6 +543,7 @@ ALB_DEVICE void handle_exit(const SceneDev& sc, const TraceOut& out, Ph& ph, Src
     ph.px = xs + ph.dx * rem; ph.py = ys + ph.dy * rem; ph.pz = zs + ph.dz * rem;
     if (reflect) {
         float a = water_alpha(sc, ph.py);
+        if (sc.adjoint) score_tau(sc, ph.sc, layer_of(sc, ph.py), (float)((double)a * len));
         ph.tau = __double2float_rn(__dadd_rn((double)ph.tau, (double)a * len));
     }
 }
@@ -551,6 +580,10 @@ ALB_DEVICE void handle_floor(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
     double rem = (1.0 - f) * len;
     ph.px = xb + ph.dx * rem; ph.py = yb + ph.dy * rem; ph.pz = zb + ph.dz * rem;
     float a = water_alpha(sc, ph.py);
+    if (sc.adjoint) {
+        score_tau(sc, ph.sc, layer_of(sc, ph.py), (float)((double)a * len));
+        ph.sc.l += sc.inv_albedo;
+    }
     ph.tau = __double2float_rn(__dadd_rn((double)ph.tau, (double)a * len));
     ph.E = __fmul_rn(ph.E, sc.floor_albedo32);
 }
@@ -558,8 +591,9 @@ ALB_DEVICE void handle_floor(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
 template <int PASS, class Src>
 ALB_DEVICE void handle_scatter(const SceneDev& sc, const TraceOut& out, Ph& ph, Src& src,
                                int64_t step, uint32_t pid) {
-    emit_event<PASS>(out, ALB_SCATTER, kQueryScatter, ph, ph.px, ph.py, ph.pz, step, pid);
     int L = layer_of(sc, ph.py);
+    if (sc.adjoint) score_scatter_density(sc, ph.sc, L);
+    emit_event<PASS>(out, ALB_SCATTER, kQueryScatter, ph, ph.px, ph.py, ph.pz, step, pid);
     double uth, phi;
     float new_target;
     draw_scatter(src, uth, phi, new_target);
@@ -571,6 +605,7 @@ ALB_DEVICE void handle_scatter(const SceneDev& sc, const TraceOut& out, Ph& ph, 
     double ox, oy, oz;
     rotate_from_z(ph.dx, ph.dy, ph.dz, l0, l1, l2, ox, oy, oz);
     ph.dx = ox; ph.dy = oy; ph.dz = oz;
+    if (sc.adjoint) score_scatter_after(sc, ph.sc, L, (float)ct);
     ph.E = __fmul_rn(ph.E, water_ssa(sc, ph.py));
     ph.tau = __fsub_rn(ph.tau, ph.taut);
     ph.taut = new_target;
@@ -585,6 +620,7 @@ ALB_DEVICE void emit_photon(const SceneDev& sc, Ph& ph, Src& src) {
     const double* R = sc.rot_d;
     ph.px = 0.0; ph.py = 0.0; ph.pz = 0.0;
     ph.E = 1.0f; ph.tau = 0.0f; ph.taut = __int_as_float(0x7f800000); ph.s = 0;
+    ph.sc = Score{0.f, 0.f, 0.f, 0.f};
     float qnan = __int_as_float(0x7fc00000);
     ph.fwi[0] = ph.fwi[1] = ph.fwi[2] = qnan;
     ph.sfi[0] = ph.sfi[1] = ph.sfi[2] = qnan;
@@ -696,6 +732,8 @@ ALB_DEVICE void trace_photon(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
             if (nseg > left) nseg = left;
             double inc = (double)sc.layer_alpha[L] * len;
             int64_t m = (nseg > 0) ? tau_run(ph.tau, inc, ph.taut, nseg) : 0;
+            // optical depth of the run: m steps to the scatter, else the whole segment
+            if (sc.adjoint) score_tau(sc, ph.sc, L, (float)((double)(m > 0 ? m : nseg) * inc));
             if (m > 0) {
                 double k = (double)m;
                 ph.px = fma(k, svx, ph.px); ph.py = fma(k, svy, ph.py); ph.pz = fma(k, svz, ph.pz);

@@ -28,6 +28,7 @@ struct PhF {
     float E, tau, taut, t0;
     float fwi[3], sfi[3];
     int s;
+    Score sc;  // adjoint path score (see score_tau in tracer.cuh)
 };
 
 // (x / 2^9 + 0.5) / 2^23: an exact float strictly inside (0, 1), 2^23 equally spaced values
@@ -54,10 +55,12 @@ ALB_DEVICE void emit_event_f(const TraceOut& out, int channel, int qkind, const 
                 out.rec_sfi[channel][slot] = make_float4(ph.sfi[0], ph.sfi[1], ph.sfi[2], 0.f);
             }
             if (out.rec_id[channel]) out.rec_id[channel][slot] = pid;
+            if (out.rec_sco[channel]) out.rec_sco[channel][slot] = make_float4(ph.sc.a, ph.sc.b, ph.sc.g, ph.sc.l);
         }
     } else {
         unsigned long long slot = warp_append(out.q_count, qkind);
         if (slot < out.q_cap[qkind]) {
+            if (out.q_s[qkind]) out.q_s[qkind][slot] = make_float4(ph.sc.a, ph.sc.b, ph.sc.g, ph.sc.l);
             out.q_a[qkind][slot] = make_float4(x, y, z, ph.E);
             out.q_b[qkind][slot] = make_float4(ph.dx, ph.dy, ph.dz, t);
             out.q_c[qkind][slot] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -178,8 +181,12 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.px = fmaf(k, svx, ph.px); ph.py = fmaf(k, svy, ph.py); ph.pz = fmaf(k, svz, ph.pz);
             ph.tau = fmaf(k, inc, ph.tau);
             int step = ph.s + m - 1;
-            emit_event_f<PASS>(out, ALB_SCATTER, kQueryScatter, ph, ph.px, ph.py, ph.pz, step, pid);
             int L2 = layer_of_f(sc, ph.py);
+            if (sc.adjoint) {
+                score_tau(sc, ph.sc, L, k * inc);
+                score_scatter_density(sc, ph.sc, L2);
+            }
+            emit_event_f<PASS>(out, ALB_SCATTER, kQueryScatter, ph, ph.px, ph.py, ph.pz, step, pid);
             U4 b = src.block();
             float u = uf(b.x) * (float)kInvCdf;
             int j = min((int)u, kInvCdf - 1);
@@ -198,6 +205,7 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.dx = fmaf(ctt, ph.dx, st * ux);
             ph.dy = fmaf(ctt, ph.dy, st * uy);
             ph.dz = fmaf(ctt, ph.dz, st * uz);
+            if (sc.adjoint) score_scatter_after(sc, ph.sc, L2, ctt);
             ph.E *= sc.layer_prof[L2] ? water_ssa(sc, (double)ph.py) : sc.layer_ssa[L2];
             ph.tau = fmaxf(ph.tau - ph.taut, 0.f);
             ph.taut = -__logf(uf(b.z));
@@ -209,6 +217,7 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
         float k = (float)nseg;
         ph.px = fmaf(k, svx, ph.px); ph.py = fmaf(k, svy, ph.py); ph.pz = fmaf(k, svz, ph.pz);
         ph.tau = fmaf(k, inc, ph.tau);
+        if (sc.adjoint && nseg > 0) score_tau(sc, ph.sc, L, k * inc);
         ph.s += nseg;
         if (ph.s >= S) break;
         if (nseg != n_plane) continue;  // layer change (or one profiled step) only
@@ -232,7 +241,11 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             }
             float rem = (1.f - f) * len;
             ph.px = fmaf(ph.dx, rem, xs); ph.py = fmaf(ph.dy, rem, yss); ph.pz = fmaf(ph.dz, rem, zs);
-            if (reflect) ph.tau = fmaf(water_alpha_f(sc, ph.py), len, ph.tau);
+            if (reflect) {
+                const float a = water_alpha_f(sc, ph.py);
+                if (sc.adjoint) score_tau(sc, ph.sc, layer_of_f(sc, ph.py), a * len);
+                ph.tau = fmaf(a, len, ph.tau);
+            }
         } else {
             // handle_seafloor
             float f = fminf(fmaxf((yf - ph.py) / svy, 0.f), 1.f);
@@ -258,7 +271,12 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.dx = hx * hn; ph.dy = hy * hn; ph.dz = hz * hn;
             float rem = (1.f - f) * len;
             ph.px = fmaf(ph.dx, rem, xb); ph.py = fmaf(ph.dy, rem, yb); ph.pz = fmaf(ph.dz, rem, zb);
-            ph.tau = fmaf(water_alpha_f(sc, ph.py), len, ph.tau);
+            const float a = water_alpha_f(sc, ph.py);
+            if (sc.adjoint) {
+                score_tau(sc, ph.sc, layer_of_f(sc, ph.py), a * len);
+                ph.sc.l += sc.inv_albedo;
+            }
+            ph.tau = fmaf(a, len, ph.tau);
             ph.E *= sc.floor_albedo32;
         }
         ph.s += 1;
@@ -274,6 +292,7 @@ ALB_DEVICE void emit_photon_fast(const SceneDev& sc, PhF& ph, PhiloxSrc& src) {
     for (int i = 0; i < 9; ++i) R[i] = (float)Rd[i];
     ph.px = ph.py = ph.pz = 0.f;
     ph.E = 1.f; ph.tau = 0.f; ph.taut = __int_as_float(0x7f800000); ph.s = 0;
+    ph.sc = Score{0.f, 0.f, 0.f, 0.f};
     float qnan = __int_as_float(0x7fc00000);
     ph.fwi[0] = ph.fwi[1] = ph.fwi[2] = qnan;
     ph.sfi[0] = ph.sfi[1] = ph.sfi[2] = qnan;

@@ -13,6 +13,7 @@ from typing import Dict, Optional
 import numpy as np
 
 from pyalbsim_gb300._native import (
+    ALB_OPT_ADJOINT,
     ALB_OPT_KEEP_EXIT_STATES,
     ALB_OPT_KEEP_RECORD_IDS,
     ALB_OPT_PRECISE,
@@ -44,6 +45,8 @@ class GpuEngine:
         self.ctx = NativeContext(self.scene, device=self.options.device)
         self.ctx.set_option(ALB_OPT_SORT_QUERIES, 1 if self.options.sort_queries else 0)
         self.ctx.set_option(ALB_OPT_PRECISE, 1 if self.options.precise else 0)
+        if self.options.adjoint:
+            self.ctx.set_option(ALB_OPT_ADJOINT, 1)
         self.n_forward = 0
         self.n_backward = 0
         self._maps_stale = True
@@ -97,6 +100,11 @@ class GpuEngine:
             seafloor_heatmap=f.reshape(b, b).astype(np.float32),
             scatter_radius_heatmap=r.reshape(b, b),
         )
+
+    def jacobian(self) -> np.ndarray:
+        """d waveform / d (a, b, g, albedo, roughness), float64 [5, channels, nbins]
+        (needs GpuRunOptions(adjoint=True))."""
+        return self.ctx.jacobian()
 
     def keep_exit_states(self, on: bool = True):
         self.ctx.set_option(ALB_OPT_KEEP_EXIT_STATES, int(on))

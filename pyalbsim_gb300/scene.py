@@ -204,6 +204,57 @@ class LayerModel:
     lut_alpha: Optional[np.ndarray] = None
     n_profile: Tuple[int, float, float] = (0, 0.0, 0.0)
     a_profile: Tuple[int, float, float] = (0, 0.0, 0.0)
+    # adjoint (extension): d ln(alpha)/d theta and d ln(ssa)/d theta for theta = (a, b, g),
+    # the HG asymmetry (0: Fournier-Forand layer) and d ln(scatter weight)/dg per bin
+    dlog_alpha: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    dlog_ssa: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    hg_g: float = 0.0
+    dlog_weight_g: Optional[np.ndarray] = None
+
+
+_CSTEP = 1e-30  # complex-step size: f'(x) = Im f(x + i h) / h, exact to rounding
+
+
+def adjoint_layer_terms(a, b, salinity, wavelength, flying_height, divergence, bb_frac, hg_g=None):
+    """d ln(alpha)/d theta and d ln(ssa)/d theta for theta = (a, b, g) of a constant layer,
+    by complex-step differentiation of the Churnside attenuation and ssa = (alpha - a)/alpha;
+    with hg_g set, g moves the backscatter fraction B of an HG layer (for a Fournier-Forand
+    layer the g entries are 0)."""
+
+    def alpha_ssa(da=0.0, db=0.0, dg=0.0):
+        bb = bb_frac if hg_g is None else _hg_backscatter(hg_g + dg)
+        al = churnside_alpha(a + da, b + db, salinity, wavelength, flying_height, divergence, bb)
+        return al, (al - (a + da)) / al
+
+    al0, ssa0 = alpha_ssa()
+    al0, ssa0 = float(np.real(al0)), float(np.real(ssa0))
+    dla, dls = [], []
+    for i in range(3):
+        if i == 2 and hg_g is None:
+            dla.append(0.0)
+            dls.append(0.0)
+            continue
+        kw = {("da", "db", "dg")[i]: 1j * _CSTEP}
+        al, ssa = alpha_ssa(**kw)
+        dla.append(float(np.imag(al)) / _CSTEP / al0)
+        dls.append(float(np.imag(ssa)) / _CSTEP / ssa0)
+    return tuple(dla), tuple(dls)
+
+
+def _hg_backscatter(g):
+    return (1.0 - g) / (2.0 * g) * ((1.0 + g) / np.sqrt(1.0 + g * g) - 1.0)
+
+
+def hg_weight_dlog_g(g: float, weight: np.ndarray) -> np.ndarray:
+    """d ln(scatter weight)/dg per angular bin of an HG layer. The weight is the CDF mass of
+    each bin, linear in the CDF on a fixed angle grid, so its derivative is the same bin
+    mass of dCDF/dg (complex step through the normalised running sum)."""
+    th, _, cdf_c = henyey_greenstein_table(g + 1j * _CSTEP)
+    dcdf = np.imag(cdf_c) / _CSTEP
+    dw, _ = scatter_weight_table(th, dcdf)
+    out = np.zeros_like(weight, dtype=np.float64)
+    np.divide(dw, weight, out=out, where=weight > 0)
+    return out
 
 
 @dataclass
@@ -299,6 +350,12 @@ def build_scene(cfg) -> SceneModel:
         weight, width32 = scatter_weight_table(th, cdf)
         top32 = float(np.float32(depth_acc))
         constant = _is_constant(layer)
+        dla = dls = (0.0, 0.0, 0.0)
+        if constant:
+            dla, dls = adjoint_layer_terms(
+                a0, b0, s0, laser.wavelength, cfg.scene.flying_height, laser.divergence_angle, bb,
+                hg_g=None if hg is None else float(hg),
+            )
         lut_z = lut_alpha = None
         if not constant:
             lut_z, lut_alpha = attenuation_lut(
@@ -327,6 +384,10 @@ def build_scene(cfg) -> SceneModel:
                 lut_alpha=lut_alpha,
                 n_profile=_profile_code(layer.refractive_index),
                 a_profile=_profile_code(layer.absorption_coefficient),
+                dlog_alpha=dla,
+                dlog_ssa=dls,
+                hg_g=0.0 if hg is None else float(hg),
+                dlog_weight_g=None if hg is None else hg_weight_dlog_g(float(hg), weight),
             )
         )
     depth = layers[-1].bottom_depth

@@ -1,0 +1,168 @@
+"""Adjoint (extension) on the CPU: the complex-step attenuation and albedo derivatives
+against finite differences, the HG weight-table derivative, the oracle's Jacobian columns
+whose paths do not depend on the parameter (albedo, roughness) against common-random-number
+differences, the parameter plumbing and the autograd contraction."""
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from fixtures import config_from_fixture, load
+from oracle.oracle import oracle_run
+from pyalbsim_gb300 import adjoint as adj
+from pyalbsim_gb300.scene import (
+    adjoint_layer_terms,
+    build_scene,
+    churnside_alpha,
+    henyey_greenstein_table,
+    hg_weight_dlog_g,
+    scatter_weight_table,
+)
+
+ARGS = dict(salinity=35.0, wavelength=0.532, flying_height=400.0, divergence=1e-3)
+
+
+def _hg_cfg(g=0.9, name="replay_small.npz"):
+    cfg = config_from_fixture(load(name))
+    layers = tuple(dataclasses.replace(L, henyey_greenstein_g=g) for L in cfg.water.layers)
+    return dataclasses.replace(cfg, water=dataclasses.replace(cfg.water, layers=layers))
+
+
+def _hg_b(g):
+    return (1.0 - g) / (2.0 * g) * ((1.0 + g) / np.sqrt(1.0 + g * g) - 1.0)
+
+
+@pytest.mark.parametrize("a,b,g", [(0.05, 0.2, 0.9), (0.1, 0.4, 0.92), (0.169, 2.5, 0.5)])
+def test_layer_terms_match_central_differences(a, b, g):
+    dla, dls = adjoint_layer_terms(a, b, ARGS["salinity"], ARGS["wavelength"], ARGS["flying_height"],
+                                   ARGS["divergence"], _hg_b(g), hg_g=g)
+
+    def al(da=0.0, db=0.0, dg=0.0):
+        return float(churnside_alpha(a + da, b + db, ARGS["salinity"], ARGS["wavelength"],
+                                     ARGS["flying_height"], ARGS["divergence"], _hg_b(g + dg)))
+
+    def ssa(da=0.0, db=0.0, dg=0.0):
+        x = al(da, db, dg)
+        return (x - (a + da)) / x
+
+    h = 1e-6
+    for i, key in enumerate(("da", "db", "dg")):
+        fd_a = (np.log(al(**{key: h})) - np.log(al(**{key: -h}))) / (2 * h)
+        fd_s = (np.log(ssa(**{key: h})) - np.log(ssa(**{key: -h}))) / (2 * h)
+        assert abs(dla[i] - fd_a) < 1e-6 * max(1.0, abs(fd_a)), (key, dla[i], fd_a)
+        assert abs(dls[i] - fd_s) < 1e-6 * max(1.0, abs(fd_s)), (key, dls[i], fd_s)
+
+
+def test_ff_layers_have_no_g_terms():
+    scene = build_scene(config_from_fixture(load("replay_small.npz")))
+    L = scene.layers[0]
+    assert L.dlog_alpha[2] == 0.0 and L.dlog_ssa[2] == 0.0 and L.hg_g == 0.0 and L.dlog_weight_g is None
+
+
+@pytest.mark.parametrize("g", [0.5, 0.9])
+def test_hg_weight_derivative_matches_central_difference(g):
+    th, _, cdf = henyey_greenstein_table(g)
+    w, _ = scatter_weight_table(th, cdf)
+    d = hg_weight_dlog_g(g, w)
+    h = 1e-6
+    wp, _ = scatter_weight_table(*henyey_greenstein_table(g + h)[::2])
+    wm, _ = scatter_weight_table(*henyey_greenstein_table(g - h)[::2])
+    fd = (wp - wm) / (2 * h)
+    ok = w > 1e-12
+    # the difference quotient of CDF masses carries ~1e-16 / h = 1e-10 of cancellation noise
+    np.testing.assert_allclose(d[ok] * w[ok], fd[ok], rtol=1e-5, atol=1e-9)
+
+
+def test_parameters_round_trip():
+    cfg = _hg_cfg(0.9)
+    p = adj.parameters_of(cfg)
+    q = p + np.array([0.5, 0.01, 0.02, 0.01, 0.05, 0.01])
+    cfg2 = adj.with_parameters(cfg, q)
+    np.testing.assert_allclose(adj.parameters_of(cfg2), q, rtol=0, atol=1e-12)
+    scene = build_scene(cfg2)
+    assert abs(scene.depth - q[0]) < 1e-9
+    with pytest.raises(ValueError):
+        adj.with_parameters(cfg, [0.0, *q[1:]])
+
+
+def _oracle_w(cfg, seed=5, nf=1500, nb=400, adjoint=False):
+    return oracle_run(build_scene(cfg), nf, nb, seed=seed, adjoint=adjoint)
+
+
+@pytest.mark.parametrize("name", ["replay_small.npz", "replay_twolayer.npz"])
+def test_oracle_albedo_column_matches_crn_difference(name):
+    """Paths do not depend on the seafloor albedo: with the same streams each contribution
+    scales as albedo^(reflections), so the score column equals the central difference (exact
+    for up to two reflections; the step is large enough that the float32 rounding of the
+    albedo the tracer multiplies by stays below 1e-5 of it)."""
+    cfg = config_from_fixture(load(name))
+    r = _oracle_w(cfg, adjoint=True)
+    alb = cfg.sea_floor.albedo
+    h = 1e-2 * alb
+    wp = _oracle_w(dataclasses.replace(cfg, sea_floor=dataclasses.replace(cfg.sea_floor, albedo=alb + h)))["waveform"]
+    wm = _oracle_w(dataclasses.replace(cfg, sea_floor=dataclasses.replace(cfg.sea_floor, albedo=alb - h)))["waveform"]
+    fd = (wp - wm) / (2 * h)
+    j = r["jacobian"][3]
+    assert np.abs(fd).sum() > 0
+    for c in range(4):
+        den = np.abs(fd[c]).sum()
+        # a channel without seafloor reflections differs only by summation-order rounding
+        if den > 1e-9 * np.abs(r["waveform"][c]).sum():
+            assert np.abs(j[c] - fd[c]).sum() / den < 1e-4, c
+        else:
+            assert not j[c].any(), c
+
+
+def test_oracle_roughness_column_matches_crn_difference():
+    """Only the surface-reflection gather weight depends on the roughness."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    r = _oracle_w(cfg, adjoint=True)
+    rough = cfg.sea_surface.roughness
+    h = 1e-4 * rough
+    ss = cfg.sea_surface
+    wp = _oracle_w(dataclasses.replace(cfg, sea_surface=dataclasses.replace(ss, roughness=rough + h)))["waveform"]
+    wm = _oracle_w(dataclasses.replace(cfg, sea_surface=dataclasses.replace(ss, roughness=rough - h)))["waveform"]
+    fd = (wp - wm) / (2 * h)
+    j = r["jacobian"][4]
+    assert np.abs(fd[2]).sum() > 0
+    assert np.abs(j[2] - fd[2]).sum() / np.abs(fd[2]).sum() < 1e-4
+    for c in (0, 1, 3):  # no roughness dependence: differences are summation-order rounding
+        assert not j[c].any()
+        assert np.abs(fd[c]).sum() < 1e-9 * np.abs(r["waveform"][c]).sum()
+
+
+def test_oracle_scores_follow_the_path():
+    """Record scores: albedo = reflections before the record / albedo; a bottom record made
+    before any seafloor reflection has none."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    r = _oracle_w(cfg, adjoint=True)
+    alb = cfg.sea_floor.albedo
+    m = r["maps"][0]
+    # the first bottom record of a photon precedes its first reflection
+    first = np.unique(m["photon"], return_index=True)[1]
+    np.testing.assert_array_equal(m["score"][first, 3], 0.0)
+    refl = m["score"][:, 3] * alb
+    np.testing.assert_allclose(refl, np.round(refl), atol=1e-4)
+
+
+def test_torch_function_contracts_the_jacobian(monkeypatch):
+    torch = pytest.importorskip("torch")
+    cfg = _hg_cfg(0.9)
+    nb = build_scene(cfg).n_bins
+    rng = np.random.default_rng(0)
+    W = rng.normal(size=(4, nb))
+    J = rng.normal(size=(6, 4, nb))
+    calls = {}
+
+    def fake(run_cfg, nf, nbk, seed, opts, with_depth=True, depth_step=None):
+        calls["with_depth"] = with_depth
+        return W, J
+
+    monkeypatch.setattr(adj, "simulate_with_jacobian", fake)
+    p = torch.tensor(adj.parameters_of(cfg), dtype=torch.float64, requires_grad=True)
+    w = adj.WaveformFunction.apply(p, cfg, 10, 10, 1, None)
+    G = rng.normal(size=(4, nb))
+    (w * torch.from_numpy(G)).sum().backward()
+    np.testing.assert_allclose(p.grad.numpy(), np.einsum("pcb,cb->p", J, G), rtol=1e-12)
+    assert calls["with_depth"] is True
