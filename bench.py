@@ -37,34 +37,9 @@ DRAM_BYTES_PER_SCATTER_QUERY = 846
 
 
 def workload_config(name: str):
-    from pyalbsim_gb300.config import (
-        HeatmapConfig, LaserConfig, SceneConfig, SeaFloorConfig, SeaSurfaceConfig, SensorConfig,
-        SimulationConfig, TurbidityLayerConfig, WaterConfig,
-    )
+    from pyalbsim_gb300.workloads import workload_config as wc
 
-    if name == "large":
-        return SimulationConfig(
-            scene=SceneConfig(flying_height=400.0),
-            water=WaterConfig(layers=(TurbidityLayerConfig(
-                height=20.0, absorption_coefficient=0.10, scattering_coefficient=0.40, refractive_index=1.34),)),
-            laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
-            sensor=SensorConfig(field_of_view=50e-3, sample_rate=int(2e10)),
-            sea_floor=SeaFloorConfig(albedo=0.20),
-            sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.10))),
-            heatmap=HeatmapConfig(enabled=False),
-        )
-    if name == "small":
-        return SimulationConfig(
-            scene=SceneConfig(flying_height=400.0),
-            water=WaterConfig(layers=(TurbidityLayerConfig(
-                height=5.0, absorption_coefficient=0.05, scattering_coefficient=0.20, refractive_index=1.34),)),
-            laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
-            sensor=SensorConfig(field_of_view=20e-3, sample_rate=int(1e10)),
-            sea_floor=SeaFloorConfig(albedo=0.15),
-            sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.05))),
-            heatmap=HeatmapConfig(enabled=False),
-        )
-    raise ValueError(name)
+    return wc(name)
 
 
 class ClockSampler:

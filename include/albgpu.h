@@ -139,6 +139,12 @@ typedef struct AlbSceneParams {
     /* Extension (no counterpart in the reference): > 0 selects the fixed-radius gather, every
      * record within this distance (m) with norm 1/(pi R^2) or 1/(4/3 pi R^3); 0 is k-NN. */
     double gather_radius;
+    /* Extension: gated waveform window. gate_bins > 0 keeps bins [gate_start, gate_start +
+     * gate_bins) of the 2*steps timeline (every waveform and Jacobian array then has
+     * gate_bins entries) and drops contributions outside it; 0 keeps the whole timeline,
+     * where a bin outside it is an error (ALB_ERR_CAPACITY). */
+    int64_t gate_start;
+    int64_t gate_bins;
 } AlbSceneParams;
 
 /* Caller-supplied variates (replay mode): photon i consumes values[offsets[i] ..
@@ -240,6 +246,37 @@ int alb_knn_noalloc(const float* points_dev, uint64_t m, const double* queries_d
 int alb_get_jacobian(AlbCtx* ctx, int param, int channel, double* out, size_t nbins);
 int alb_adjoint(AlbCtx* ctx, const double* dL_dw, size_t nbins, double* grad);
 int alb_export_map_scores(AlbCtx* ctx, int channel, float* scores, size_t n);
+
+/* Batched instances (extension: the reference runs one configuration per process; its
+ * hypercube notebook loops run_parallel over samples). Each instance is a full simulation:
+ * n_forward photons traced into fresh photon maps, the maps indexed, n_backward photons
+ * traced and gathered (Philox streams keyed by seed, photon ids from 0). `streams` host
+ * workers each own a context on its own non-blocking CUDA stream and take instances from a
+ * shared queue, largest (n_forward + n_backward) first, so small instances overlap on the
+ * GPU; a context keeps its device buffers from one instance to the next. Results: the
+ * float64 waveform [ALB_CHANNELS][2*steps] of each instance and, with adjoint set, its
+ * Jacobian [ALB_ADJ_PARAMS-1][ALB_CHANNELS][2*steps] (parameters 1..5; nullable). The
+ * call returns ALB_OK once every instance has run; each instance's own result is in
+ * status (its message in alb_last_error(NULL) when it is the last failure). */
+typedef struct AlbBatchInstance {
+    const AlbSceneParams* scene;
+    uint64_t n_forward;
+    uint64_t n_backward;
+    uint64_t seed;
+    double* waveform;             /* out, caller-owned host memory */
+    double* jacobian;             /* out (adjoint), nullable */
+    int32_t status;               /* out: ALB_OK or the instance's error code */
+    float device_ms;              /* out: CUDA-event time of the instance on its stream */
+} AlbBatchInstance;
+
+typedef struct AlbBatchOptions {
+    int32_t device;
+    int32_t streams;              /* concurrent workers, 1..64 */
+    int32_t precise;              /* 1: float64-geometry tracer, 0: fast float32 tracer */
+    int32_t adjoint;              /* 1: also accumulate the Jacobian */
+} AlbBatchOptions;
+
+int alb_batch_run(AlbBatchInstance* instances, uint64_t n, const AlbBatchOptions* options);
 
 /* Device-side counters of the last trace / gather (events, records, queries, launches). */
 int alb_stats(AlbCtx* ctx, int64_t* out, int n);

@@ -759,7 +759,9 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                   double* jac, int threads) {
     const int nj = (mscore && qscore && jac) ? 5 : 0;
     int k = p->k;
-    int64_t nb = 2 * p->steps;
+    /* extension: a gated window keeps bins [gate_start, gate_start + gate_bins) only */
+    const int gated = p->gate_bins > 0;
+    int64_t nb = gated ? p->gate_bins : 2 * p->steps;
     const double R = p->gather_radius;  /* extension: > 0 selects the fixed-radius gather */
     if (nq > 0 && R <= 0.0 && m < k) return ALB_ERR_TOO_FEW;
     int nthreads = 1;
@@ -841,13 +843,14 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                 float e32 = qenergy[q] * menergy[id];
                 double contrib = ((double)e32 * norm) * w;
                 float tsum = qtime[q] + mtime[id];
-                long long bin = (long long)(tsum / (float)p->sample_multiplier);
-                if (bin < 0 || bin >= nb) {
+                long long bin = (long long)(tsum / (float)p->sample_multiplier) - (gated ? p->gate_start : 0);
+                const int in_window = bin >= 0 && bin < nb;
+                if (!in_window && !gated) {
                     err = ALB_ERR_CAPACITY;
                     continue;
                 }
-                wf[bin] += contrib;
-                if (nj) {
+                if (in_window) wf[bin] += contrib;
+                if (nj && in_window) {
                     const float* sq = qscore + 4 * q;
                     const float* sp = mscore + 4 * (int64_t)id;
                     double d[5] = {(double)sq[0] + sp[0], (double)sq[1] + sp[1], (double)sq[2] + sp[2],

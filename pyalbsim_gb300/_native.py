@@ -100,6 +100,8 @@ class AlbSceneParams(C.Structure):
         ("floor_center", C.c_double * 3),
         ("layers", AlbLayer * MAX_LAYERS),
         ("gather_radius", C.c_double),
+        ("gate_start", C.c_int64),
+        ("gate_bins", C.c_int64),
     ]
 
 
@@ -112,8 +114,31 @@ class AlbReplay(C.Structure):
     ]
 
 
+class AlbBatchInstance(C.Structure):
+    _fields_ = [
+        ("scene", C.POINTER(AlbSceneParams)),
+        ("n_forward", C.c_uint64),
+        ("n_backward", C.c_uint64),
+        ("seed", C.c_uint64),
+        ("waveform", C.POINTER(C.c_double)),
+        ("jacobian", C.POINTER(C.c_double)),
+        ("status", C.c_int32),
+        ("device_ms", C.c_float),
+    ]
+
+
+class AlbBatchOptions(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("streams", C.c_int32),
+        ("precise", C.c_int32),
+        ("adjoint", C.c_int32),
+    ]
+
+
 EXPORTED = [
     "alb_adjoint",
+    "alb_batch_run",
     "alb_export_map_scores",
     "alb_get_jacobian",
     "alb_create",
@@ -181,6 +206,7 @@ def load_library(path: str = LIB_PATH):
     lib.alb_get_jacobian.argtypes = [_P, C.c_int, C.c_int, _P, C.c_size_t]
     lib.alb_adjoint.argtypes = [_P, _P, C.c_size_t, _P]
     lib.alb_export_map_scores.argtypes = [_P, C.c_int, _P, C.c_size_t]
+    lib.alb_batch_run.argtypes = [C.POINTER(AlbBatchInstance), C.c_uint64, C.POINTER(AlbBatchOptions)]
     _lib = lib
     return lib
 
@@ -231,6 +257,8 @@ def scene_struct(scene: SceneModel):
         raise ValueError(f"at most {MAX_LAYERS} water layers are supported")
     p.n_layers = len(scene.layers)
     p.gather_radius = float(scene.gather_radius or 0.0)
+    p.gate_start = int(scene.gate_start)
+    p.gate_bins = int(scene.gate_bins)
     p.heatmap_enabled = int(scene.heatmap_enabled)
     p.heatmap_bins = scene.heatmap_bins
     p.heatmap_water_extent = scene.heatmap_water_extent
@@ -470,3 +498,33 @@ class NativeContext:
 
     def reset(self):
         self._check(self.lib.alb_reset(self.h))
+
+
+def batch_run(scenes, n_forward, n_backward, seeds, streams=4, precise=False, adjoint=False, device=0):
+    """alb_batch_run over SceneModels: returns (waveforms: list of float64 [4, nbins],
+    jacobians: list of float64 [5, 4, nbins] or None, statuses int32 [n], device_ms [n]).
+    Instances that failed keep a zero waveform and a non-zero status."""
+    lib = load_library()
+    n = len(scenes)
+    structs, keep, waves, jacs = [], [], [], []
+    arr = (AlbBatchInstance * max(n, 1))()
+    for i, sc in enumerate(scenes):
+        p, k = scene_struct(sc)
+        structs.append(p)
+        keep.append(k)
+        w = np.zeros((4, sc.n_bins), np.float64)
+        j = np.zeros((5, 4, sc.n_bins), np.float64) if adjoint else None
+        waves.append(w)
+        jacs.append(j)
+        arr[i].scene = C.pointer(p)
+        arr[i].n_forward = int(n_forward[i])
+        arr[i].n_backward = int(n_backward[i])
+        arr[i].seed = int(seeds[i]) & 0xFFFFFFFFFFFFFFFF
+        arr[i].waveform = w.ctypes.data_as(C.POINTER(C.c_double))
+        arr[i].jacobian = j.ctypes.data_as(C.POINTER(C.c_double)) if adjoint else None
+    opt = AlbBatchOptions(device, int(streams), int(bool(precise)), int(bool(adjoint)))
+    rc = lib.alb_batch_run(arr, n, C.byref(opt))
+    raise_for(rc, lib.alb_last_error(None).decode())
+    status = np.array([arr[i].status for i in range(n)], np.int32)
+    ms = np.array([arr[i].device_ms for i in range(n)], np.float64)
+    return waves, (jacs if adjoint else None), status, ms

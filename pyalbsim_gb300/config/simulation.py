@@ -1,7 +1,7 @@
 """Top-level simulation settings; fields and defaults as ``alb_sim/config/simulation.py:12-60``."""
 
 from dataclasses import dataclass, field
-from typing import Optional
+from typing import Optional, Tuple
 
 from pyalbsim_gb300.config.heatmap import HeatmapConfig
 from pyalbsim_gb300.config.laser import LaserConfig
@@ -33,6 +33,16 @@ class SimulationConfig:
         default=None, metadata={"unit": "m", "description": "Fixed gather radius; None: k nearest"}
     )
 
+    # Extension: gated waveform window (start, length) in seconds after emission; the
+    # waveforms then hold only the bins of that window. None keeps the whole timeline.
+    waveform_gate: Optional[Tuple[float, float]] = field(
+        default=None, metadata={"unit": "s", "description": "Waveform window (start, length); None: all"}
+    )
+
     def __post_init__(self):
         if self.gather_radius is not None and not self.gather_radius > 0:
             raise ValueError("gather_radius must be positive (None selects the k-NN gather)")
+        if self.waveform_gate is not None:
+            start, length = (float(x) for x in self.waveform_gate)
+            if start < 0 or not length > 0:
+                raise ValueError("waveform_gate needs start >= 0 and length > 0")

@@ -3,7 +3,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "albgpu.h"
@@ -120,6 +122,12 @@ struct AlbCtx {
     unsigned* hm_radius = nullptr;
     // adjoint Jacobian: lo words then hi words, [2][kJacParams][channels][nbins]
     unsigned long long* jac = nullptr;
+    int64_t wf_bins = 0, jac_bins = 0, hm_cells = 0, hm_radius_cells = 0;  // accumulator capacities
+    // per-layer scene tables (device), reused when the context takes a new scene
+    struct LayerTables {
+        void *th = nullptr, *cdf = nullptr, *sl = nullptr, *w = nullptr, *dlw = nullptr, *inv = nullptr;
+    } lt[ALB_MAX_LAYERS];
+    bool keep_records = false;  // keep the append stores after indexing (batched runs)
     // exit states
     double* ex_pos = nullptr;
     double* ex_dir = nullptr;
@@ -181,9 +189,11 @@ static int check_device(AlbCtx* ctx, const char* where) {
         return fail(ctx, ALB_ERR_CUDA, std::string(where) + ": device allocation failed");
     }
     int h = 0;
-    CK(cudaMemcpy(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     if (h != 0) {
-        CK(cudaMemset(ctx->d_err, 0, sizeof(int)));
+        CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
         const char* what = h == ALB_ERR_ITER_CAP ? "a device loop hit its iteration cap"
                            : h == ALB_ERR_REPLAY ? "a replay stream ran out of variates"
                            : h == ALB_ERR_TOO_FEW ? "a photon map holds fewer records than k"
@@ -203,30 +213,40 @@ void set_global_error(const std::string& msg) { g_create_error = msg; }
 
 extern "C" const char* alb_last_error(const AlbCtx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
-extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
-    if (!p || !out) return ALB_ERR_INVALID;
-    *out = nullptr;
-    AlbCtx* ctx = new AlbCtx();
-    auto bad = [&](const std::string& m) {
-        g_create_error = m;
-        delete ctx;
-        return ALB_ERR_INVALID;
-    };
-    if (!(p->dt > 0) || p->steps <= 0 || p->sample_multiplier <= 0) return bad("bad time step");
-    if (p->k < 1 || p->k > 256) return bad("photon_mapping_k must be in [1, 256]");
-    if (p->n_layers < 1 || p->n_layers > ALB_MAX_LAYERS) return bad("1..8 water layers supported");
-    if (!(p->surface_y > p->floor_y)) return bad("seafloor must lie below the surface");
-    ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess) return bad("cudaSetDevice failed");
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-        uint64_t thr = UINT64_MAX;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+static void* table_buf(void*& slot, size_t bytes) {
+    if (!slot && cudaMalloc(&slot, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        slot = nullptr;
     }
+    return slot;
+}
+
+// Scene constants and tables of p into ctx->sc. The per-layer table buffers belong to the
+// context and are reused by a later scene (batched runs re-scene one context per stream);
+// copies are ordered on the context's stream, drained before the host staging vectors go
+// away. Returns "" or why the scene is invalid.
+static std::string set_scene(AlbCtx* ctx, const AlbSceneParams* p) {
+    if (!(p->dt > 0) || p->steps <= 0 || p->sample_multiplier <= 0) return std::string("bad time step");
+    if (p->k < 1 || p->k > 256) return std::string("photon_mapping_k must be in [1, 256]");
+    if (p->n_layers < 1 || p->n_layers > ALB_MAX_LAYERS) return std::string("1..8 water layers supported");
+    if (!(p->surface_y > p->floor_y)) return std::string("seafloor must lie below the surface");
+    const int32_t adjoint = ctx->sc.adjoint;
+    if (adjoint)
+        for (int l = 0; l < p->n_layers; ++l)
+            if (p->layers[l].profiled) return std::string("the adjoint needs constant layers");
     SceneDev& s = ctx->sc;
     s.dt = p->dt;
     s.total_steps = p->steps * (int64_t)p->sample_multiplier;
     s.nbins = 2 * p->steps;
+    s.gate_lo = 0;
+    s.gated = 0;
+    if (p->gate_bins < 0 || p->gate_start < 0) return std::string("gate_start and gate_bins must be >= 0");
+    if (p->gate_bins > 0) {
+        if (p->gate_start + p->gate_bins > 2 * p->steps) return std::string("the gate must lie inside the timeline");
+        s.nbins = p->gate_bins;
+        s.gate_lo = p->gate_start;
+        s.gated = 1;
+    }
     s.mult = p->sample_multiplier;
     s.k = p->k;
     s.ys = p->surface_y;
@@ -251,7 +271,7 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
     s.rayleigh_sigma = p->divergence / 3.0;
     s.rayleigh_mass = -std::expm1(-(p->divergence * p->divergence) / (2.0 * s.rayleigh_sigma * s.rayleigh_sigma));
     s.n_layers = p->n_layers;
-    if (!(p->gather_radius >= 0.0)) return bad("gather_radius must be >= 0 (0 selects the k-NN gather)");
+    if (!(p->gather_radius >= 0.0)) return std::string("gather_radius must be >= 0 (0 selects the k-NN gather)");
     s.radius = p->gather_radius;
     s.heatmap = p->heatmap_enabled;
     s.hm_bins = p->heatmap_bins;
@@ -263,13 +283,13 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         s.wc[i] = p->water_center[i];
         s.fc[i] = p->floor_center[i];
     }
-    s.adjoint = 0;
+    s.adjoint = adjoint;
     s.inv_albedo = p->seafloor_albedo > 0.0 ? (float)(1.0 / p->seafloor_albedo) : 0.f;
     s.dla2_drough = (float)(4.0 * p->roughness * p->roughness * p->roughness);
     const int N = ALB_PHASE_DIVISIONS;
     for (int l = 0; l < p->n_layers; ++l) {
         const AlbLayer& L = p->layers[l];
-        if (!L.phase_theta || !L.phase_cdf || !L.phase_slope || !L.scatter_weight) return bad("missing layer table");
+        if (!L.phase_theta || !L.phase_cdf || !L.phase_slope || !L.scatter_weight) return std::string("missing layer table");
         for (int i = 0; i < 3; ++i) {
             s.adj_dla[l][i] = (float)L.dlog_alpha[i];
             s.adj_dls[l][i] = (float)L.dlog_ssa[i];
@@ -279,10 +299,10 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         if (L.dlog_weight_g) {
             std::vector<float> d(N);
             for (int i = 0; i < N; ++i) d[i] = (float)L.dlog_weight_g[i];
-            float* dd;
-            if (cudaMalloc(&dd, N * sizeof(float)) != cudaSuccess) return bad("table allocation failed");
-            ctx->tables.push_back(dd);
-            cudaMemcpy(dd, d.data(), N * sizeof(float), cudaMemcpyHostToDevice);
+            float* dd = (float*)table_buf(ctx->lt[l].dlw, N * sizeof(float));
+            if (!dd) return std::string("table allocation failed");
+            cudaMemcpyAsync(dd, d.data(), N * sizeof(float), cudaMemcpyHostToDevice, ctx->st);
+            cudaStreamSynchronize(ctx->st);
             s.layer_dlw_g[l] = dd;
         }
         s.layer_bottom[l] = L.bottom_depth;
@@ -299,17 +319,17 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
         s.layer_nkind[l] = s.layer_akind[l] = 0;
         s.layer_n0[l] = s.layer_n1[l] = s.layer_a0[l] = s.layer_a1[l] = 0.0;
         if (L.profiled) {
-            if (!L.lut_z || !L.lut_alpha || L.lut_n < 2) return bad("profiled layer without an attenuation table");
-            if (!(L.height > 0.0)) return bad("profiled layer needs a positive height");
-            if (L.n_kind < 0 || L.n_kind > 2 || L.a_kind < 0 || L.a_kind > 2) return bad("unknown profile kind");
+            if (!L.lut_z || !L.lut_alpha || L.lut_n < 2) return std::string("profiled layer without an attenuation table");
+            if (!(L.height > 0.0)) return std::string("profiled layer needs a positive height");
+            if (L.n_kind < 0 || L.n_kind > 2 || L.a_kind < 0 || L.a_kind > 2) return std::string("unknown profile kind");
             float* lz;
             double* la;
             if (cudaMalloc(&lz, L.lut_n * sizeof(float)) != cudaSuccess ||
                 cudaMalloc(&la, L.lut_n * sizeof(double)) != cudaSuccess)
-                return bad("table allocation failed");
+                return std::string("table allocation failed");
             ctx->tables.insert(ctx->tables.end(), {lz, la});
-            cudaMemcpy(lz, L.lut_z, L.lut_n * sizeof(float), cudaMemcpyHostToDevice);
-            cudaMemcpy(la, L.lut_alpha, L.lut_n * sizeof(double), cudaMemcpyHostToDevice);
+            cudaMemcpyAsync(lz, L.lut_z, L.lut_n * sizeof(float), cudaMemcpyHostToDevice, ctx->st);
+            cudaMemcpyAsync(la, L.lut_alpha, L.lut_n * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
             s.layer_lut_n[l] = L.lut_n;
             s.layer_lut_z[l] = lz;
             s.layer_lut_a[l] = la;
@@ -320,20 +340,19 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
             s.layer_a0[l] = L.a_start;
             s.layer_a1[l] = L.a_end;
         }
-        double *th, *cdf, *sl;
-        float* w;
-        if (cudaMalloc(&th, N * sizeof(double)) != cudaSuccess || cudaMalloc(&cdf, N * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&sl, N * sizeof(double)) != cudaSuccess || cudaMalloc(&w, N * sizeof(float)) != cudaSuccess)
-            return bad("table allocation failed");
-        ctx->tables.insert(ctx->tables.end(), {th, cdf, sl, w});
+        double* th = (double*)table_buf(ctx->lt[l].th, N * sizeof(double));
+        double* cdf = (double*)table_buf(ctx->lt[l].cdf, N * sizeof(double));
+        double* sl = (double*)table_buf(ctx->lt[l].sl, N * sizeof(double));
+        float* w = (float*)table_buf(ctx->lt[l].w, N * sizeof(float));
+        if (!th || !cdf || !sl || !w) return std::string("table allocation failed");
         std::vector<double> slope(N, 0.0);
         std::memcpy(slope.data(), L.phase_slope, (N - 1) * sizeof(double));
         std::vector<float> wf(N);
         for (int i = 0; i < N; ++i) wf[i] = (float)L.scatter_weight[i];
-        cudaMemcpy(th, L.phase_theta, N * sizeof(double), cudaMemcpyHostToDevice);
-        cudaMemcpy(cdf, L.phase_cdf, N * sizeof(double), cudaMemcpyHostToDevice);
-        cudaMemcpy(sl, slope.data(), N * sizeof(double), cudaMemcpyHostToDevice);
-        cudaMemcpy(w, wf.data(), N * sizeof(float), cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(th, L.phase_theta, N * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+        cudaMemcpyAsync(cdf, L.phase_cdf, N * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+        cudaMemcpyAsync(sl, slope.data(), N * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+        cudaMemcpyAsync(w, wf.data(), N * sizeof(float), cudaMemcpyHostToDevice, ctx->st);
         s.layer_theta[l] = th;
         s.layer_cdf[l] = cdf;
         s.layer_slope[l] = sl;
@@ -355,23 +374,77 @@ extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
             }
             inv[j] = (float)t;
         }
-        float* dinv;
-        if (cudaMalloc(&dinv, (kInvCdf + 1) * sizeof(float)) != cudaSuccess) return bad("table allocation failed");
-        ctx->tables.push_back(dinv);
-        cudaMemcpy(dinv, inv.data(), (kInvCdf + 1) * sizeof(float), cudaMemcpyHostToDevice);
+        float* dinv = (float*)table_buf(ctx->lt[l].inv, (kInvCdf + 1) * sizeof(float));
+        if (!dinv) return std::string("table allocation failed");
+        cudaMemcpyAsync(dinv, inv.data(), (kInvCdf + 1) * sizeof(float), cudaMemcpyHostToDevice, ctx->st);
+        cudaStreamSynchronize(ctx->st);  // the host staging vectors die with this iteration
         ctx->fast.inv_theta[l] = dinv;
     }
-    // accumulators
-    size_t wf_words = (size_t)2 * ALB_CHANNELS * s.nbins;
-    if (cudaMalloc(&ctx->wf, wf_words * 8) != cudaSuccess) return bad("waveform allocation failed");
-    cudaMemset(ctx->wf, 0, wf_words * 8);
+    return std::string();
+}
+
+// Waveform, Jacobian and heatmap accumulators sized for the current scene (grown, never
+// shrunk; a grown buffer is zeroed by the next reset).
+static std::string ensure_accumulators(AlbCtx* ctx) {
+    const SceneDev& s = ctx->sc;
+    auto regrow = [&](unsigned long long*& buf, int64_t& have, int64_t need, size_t words_per) -> bool {
+        if (buf && have >= need) return true;
+        if (buf) {
+            cudaStreamSynchronize(ctx->st);
+            cudaFree(buf);
+            buf = nullptr;
+        }
+        if (cudaMalloc(&buf, (size_t)need * words_per * 8) != cudaSuccess) {
+            cudaGetLastError();
+            buf = nullptr;
+            have = 0;
+            return false;
+        }
+        cudaMemsetAsync(buf, 0, (size_t)need * words_per * 8, ctx->st);
+        have = need;
+        return true;
+    };
+    if (!regrow(ctx->wf, ctx->wf_bins, s.nbins, (size_t)2 * ALB_CHANNELS)) return "waveform allocation failed";
+    if (s.adjoint && !regrow(ctx->jac, ctx->jac_bins, s.nbins, (size_t)2 * kJacParams * ALB_CHANNELS))
+        return "jacobian allocation failed";
     if (s.heatmap) {
-        size_t hb = (size_t)s.hm_bins * s.hm_bins;
-        if (cudaMalloc(&ctx->hm, 4 * hb * 8) != cudaSuccess || cudaMalloc(&ctx->hm_radius, hb * 4) != cudaSuccess)
-            return bad("heatmap allocation failed");
-        cudaMemset(ctx->hm, 0, 4 * hb * 8);
-        cudaMemset(ctx->hm_radius, 0, hb * 4);
+        const int64_t hb = (int64_t)s.hm_bins * s.hm_bins;
+        if (!regrow(ctx->hm, ctx->hm_cells, hb, 4)) return "heatmap allocation failed";
+        if (!ctx->hm_radius || ctx->hm_radius_cells < hb) {
+            if (ctx->hm_radius) {
+                cudaStreamSynchronize(ctx->st);
+                cudaFree(ctx->hm_radius);
+            }
+            if (cudaMalloc(&ctx->hm_radius, hb * 4) != cudaSuccess) {
+                ctx->hm_radius = nullptr;
+                return "heatmap allocation failed";
+            }
+            cudaMemsetAsync(ctx->hm_radius, 0, hb * 4, ctx->st);
+            ctx->hm_radius_cells = hb;
+        }
     }
+    return std::string();
+}
+
+extern "C" int alb_create(const AlbSceneParams* p, int device, AlbCtx** out) {
+    if (!p || !out) return ALB_ERR_INVALID;
+    *out = nullptr;
+    AlbCtx* ctx = new AlbCtx();
+    auto bad = [&](const std::string& m) {
+        g_create_error = m;
+        alb_destroy(ctx);
+        return ALB_ERR_INVALID;
+    };
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) return bad("cudaSetDevice failed");
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    std::string e = set_scene(ctx, p);
+    if (e.empty()) e = ensure_accumulators(ctx);
+    if (!e.empty()) return bad(e);
     if (cudaMalloc(&ctx->d_rec_count, ALB_CHANNELS * 8) != cudaSuccess || cudaMalloc(&ctx->d_q_count, 3 * 8) != cudaSuccess ||
         cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, 32 * 8) != cudaSuccess)
         return bad("counter allocation failed");
@@ -401,6 +474,9 @@ extern "C" void alb_destroy(AlbCtx* ctx) {
         cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]); cudaFree(ctx->qs[k]);
     }
     cudaFree(ctx->wf); cudaFree(ctx->hm); cudaFree(ctx->hm_radius); cudaFree(ctx->jac);
+    for (auto& t : ctx->lt) {
+        cudaFree(t.th); cudaFree(t.cdf); cudaFree(t.sl); cudaFree(t.w); cudaFree(t.dlw); cudaFree(t.inv);
+    }
     cudaFree(ctx->ex_pos); cudaFree(ctx->ex_dir); cudaFree(ctx->ex_f);
     cudaFree(ctx->d_rec_count); cudaFree(ctx->d_q_count); cudaFree(ctx->d_err); cudaFree(ctx->d_stats);
     if (ctx->ev_ready)
@@ -426,13 +502,13 @@ extern "C" int alb_set_option(AlbCtx* ctx, int key, int64_t v) {
             if (v) {
                 for (int l = 0; l < ctx->sc.n_layers; ++l)
                     if (ctx->sc.layer_prof[l]) return fail(ctx, ALB_ERR_INVALID, "the adjoint needs constant layers");
-                if (!ctx->jac) {
-                    const size_t words = (size_t)2 * kJacParams * ALB_CHANNELS * ctx->sc.nbins;
-                    CK(cudaMalloc(&ctx->jac, words * 8));
-                    CK(cudaMemset(ctx->jac, 0, words * 8));
-                }
             }
             ctx->sc.adjoint = v ? 1 : 0;
+            if (v) {
+                std::string e = ensure_accumulators(ctx);
+                if (!e.empty()) return fail(ctx, ALB_ERR_CUDA, e);
+                CK(cudaStreamSynchronize(ctx->st));
+            }
             break;
         }
         default: return fail(ctx, ALB_ERR_INVALID, "unknown option");
@@ -628,7 +704,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             }
             if (hb && attempt == 0) {
                 radius_backup.resize(hb);
-                CK(cudaMemcpy(radius_backup.data(), ctx->hm_radius, hb * 4, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpyAsync(radius_backup.data(), ctx->hm_radius, hb * 4, cudaMemcpyDeviceToHost, ctx->st));
             }
             TraceOut o = make_out(ctx);
             PhaseTimer pt(ctx, 0);
@@ -638,7 +714,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             int rc = check_device(ctx, "forward trace");
             if (rc) return rc;
             unsigned long long cnt[ALB_CHANNELS];
-            CK(cudaMemcpy(cnt, ctx->d_rec_count, sizeof cnt, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(cnt, ctx->d_rec_count, sizeof cnt, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
             bool overflow = false;
             for (int c = 0; c < ALB_CHANNELS; ++c) {
                 uint64_t added = cnt[c] - before[c];
@@ -651,8 +728,9 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
                 return ALB_OK;
             }
             // undo and retry with the measured sizes
-            CK(cudaMemcpy(ctx->d_rec_count, before, sizeof before, cudaMemcpyHostToDevice));
-            if (hb) CK(cudaMemcpy(ctx->hm_radius, radius_backup.data(), hb * 4, cudaMemcpyHostToDevice));
+            CK(cudaMemcpyAsync(ctx->d_rec_count, before, sizeof before, cudaMemcpyHostToDevice, ctx->st));
+            if (hb) CK(cudaMemcpyAsync(ctx->hm_radius, radius_backup.data(), hb * 4, cudaMemcpyHostToDevice, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
             for (int c = 0; c < ALB_CHANNELS; ++c) ctx->rec_rate[c] = (double)(cnt[c] - before[c]) / (double)n;
         }
         return fail(ctx, ALB_ERR_CAPACITY, "photon-map capacity could not be established");
@@ -694,7 +772,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             int rc = check_device(ctx, "backward trace");
             if (rc) return rc;
             unsigned long long cnt[3];
-            CK(cudaMemcpy(cnt, ctx->d_q_count, sizeof cnt, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(cnt, ctx->d_q_count, sizeof cnt, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
             bool overflow = false;
             for (int k = 0; k < 3; ++k) {
                 if (nc > 0) ctx->q_rate[k] = std::max(ctx->q_rate[k] * 0.5, (double)cnt[k] / (double)nc);
@@ -751,6 +830,7 @@ extern "C" int alb_build_maps(AlbCtx* ctx) {
         if (build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st) != 0)
             return fail(ctx, ALB_ERR_CAPACITY, "photon-map index build failed (device memory or partition)");
         CK(cudaStreamSynchronize(ctx->st));
+        if (ctx->keep_records) continue;  // the store stays for the next simulation
         release_records(ctx, c);
         ctx->rec_released[c] = true;
     }
@@ -839,8 +919,10 @@ extern "C" int alb_get_heatmaps(AlbCtx* ctx, double* water, double* seafloor, fl
 static int read_wf(AlbCtx* ctx, int c, std::vector<double>& out) {
     int64_t nb = ctx->sc.nbins;
     std::vector<unsigned long long> lo(nb), hi(nb);
-    CK(cudaMemcpy(lo.data(), ctx->wf + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hi.data(), ctx->wf + (size_t)ALB_CHANNELS * nb + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(lo.data(), ctx->wf + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hi.data(), ctx->wf + (size_t)ALB_CHANNELS * nb + (size_t)c * nb, nb * 8, cudaMemcpyDeviceToHost,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     out.resize(nb);
     for (int64_t i = 0; i < nb; ++i) out[i] = fix_to_double(lo[i], (long long)hi[i]);
     return ALB_OK;
@@ -877,8 +959,9 @@ extern "C" int alb_get_jacobian(AlbCtx* ctx, int param, int c, double* out, size
     const size_t off = ((size_t)(param - 1) * ALB_CHANNELS + c) * nb;
     const size_t half = (size_t)kJacParams * ALB_CHANNELS * nb;
     std::vector<unsigned long long> lo(nb), hi(nb);
-    CK(cudaMemcpy(lo.data(), ctx->jac + off, nb * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hi.data(), ctx->jac + half + off, nb * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(lo.data(), ctx->jac + off, nb * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hi.data(), ctx->jac + half + off, nb * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     for (int64_t i = 0; i < nb; ++i) out[i] = fix_to_double(lo[i], (long long)hi[i]);
     return ALB_OK;
 }
@@ -1074,5 +1157,153 @@ extern "C" int alb_phase_times(AlbCtx* ctx, double* ms, int64_t* calls, int64_t*
         }
         for (int c = 0; c < ALB_CHANNELS; ++c) ctx->gathered[c] = 0;
     }
+    return ALB_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched instances (extension)
+// ------------------------------------------------------------------------------------------
+
+// Empty the context for the next instance without releasing device memory: stream-ordered
+// memsets only, so the other workers' streams keep running.
+static int soft_reset(AlbCtx* ctx) {
+    const size_t nb = (size_t)ctx->sc.nbins;
+    CK(cudaMemsetAsync(ctx->d_rec_count, 0, ALB_CHANNELS * 8, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_q_count, 0, 3 * 8, ctx->st));
+    CK(cudaMemsetAsync(ctx->wf, 0, 2 * ALB_CHANNELS * nb * 8, ctx->st));
+    if (ctx->jac) CK(cudaMemsetAsync(ctx->jac, 0, (size_t)2 * kJacParams * ALB_CHANNELS * nb * 8, ctx->st));
+    if (ctx->sc.heatmap) {
+        const size_t hb = (size_t)ctx->sc.hm_bins * ctx->sc.hm_bins;
+        CK(cudaMemsetAsync(ctx->hm, 0, 4 * hb * 8, ctx->st));
+        CK(cudaMemsetAsync(ctx->hm_radius, 0, hb * 4, ctx->st));
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int c = 0; c < ALB_CHANNELS; ++c) {
+        ctx->h_rec_count[c] = 0;
+        ctx->map[c].n = 0;
+        ctx->map[c].n_real = 0;
+        ctx->map[c].nlevels = 0;
+    }
+    for (int k = 0; k < 3; ++k) ctx->h_q_count[k] = 0;
+    ctx->maps_built = false;
+    ctx->ex_n = 0;
+    return ALB_OK;
+}
+
+static int run_instance(AlbCtx* ctx, AlbBatchInstance& I, int adjoint) {
+    int rc = alb_trace(ctx, ALB_FORWARD, I.n_forward, I.seed, 0, nullptr);
+    if (!rc) rc = alb_build_maps(ctx);
+    if (!rc) rc = alb_trace(ctx, ALB_BACKWARD, I.n_backward, I.seed, 0, nullptr);
+    if (rc) return rc;
+    const int64_t nb = ctx->sc.nbins;
+    std::vector<double> w;
+    for (int c = 0; c < ALB_CHANNELS && !rc; ++c) {
+        rc = read_wf(ctx, c, w);
+        if (!rc && I.waveform) std::memcpy(I.waveform + (size_t)c * nb, w.data(), nb * 8);
+    }
+    if (!rc && adjoint && I.jacobian)
+        for (int p = 1; p < ALB_ADJ_PARAMS && !rc; ++p)
+            for (int c = 0; c < ALB_CHANNELS && !rc; ++c)
+                rc = alb_get_jacobian(ctx, p, c, I.jacobian + ((size_t)(p - 1) * ALB_CHANNELS + c) * nb, nb);
+    return rc;
+}
+
+extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchOptions* opt) {
+    if (!inst || !opt) return ALB_ERR_INVALID;
+    if (opt->streams < 1 || opt->streams > 64) {
+        g_create_error = "streams must be in [1, 64]";
+        return ALB_ERR_INVALID;
+    }
+    for (uint64_t i = 0; i < n; ++i)
+        if (!inst[i].scene) {
+            g_create_error = "instance without a scene";
+            return ALB_ERR_INVALID;
+        }
+    // the work queue: largest instances first, so the uneven tail is short
+    std::vector<uint64_t> order(n);
+    for (uint64_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+        return inst[a].n_forward + inst[a].n_backward > inst[b].n_forward + inst[b].n_backward;
+    });
+    int64_t max_bins = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const AlbSceneParams* sp = inst[i].scene;
+        max_bins = std::max<int64_t>(max_bins, sp->gate_bins > 0 ? sp->gate_bins : 2 * sp->steps);
+    }
+    std::atomic<uint64_t> next{0};
+    std::mutex msg_mu;
+    std::string last_msg;
+    auto worker = [&]() {
+        cudaSetDevice(opt->device);
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) st = nullptr;
+        AlbCtx* ctx = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        for (uint64_t t = next.fetch_add(1); t < n; t = next.fetch_add(1)) {
+            AlbBatchInstance& I = inst[order[t]];
+            I.device_ms = 0.f;
+            int rc = ALB_OK;
+            std::string msg;
+            if (!ctx) {
+                rc = alb_create(I.scene, opt->device, &ctx);
+                if (rc) {
+                    msg = g_create_error;
+                    ctx = nullptr;
+                } else {
+                    alb_set_option(ctx, ALB_OPT_STREAM, (int64_t)(intptr_t)st);
+                    alb_set_option(ctx, ALB_OPT_PRECISE, opt->precise ? 1 : 0);
+                    ctx->keep_records = true;
+                    if (opt->adjoint) rc = alb_set_option(ctx, ALB_OPT_ADJOINT, 1);
+                    if (!rc) {  // accumulators for the longest instance: no regrowth later
+                        const int64_t own = ctx->sc.nbins;
+                        ctx->sc.nbins = max_bins;
+                        std::string e = ensure_accumulators(ctx);
+                        ctx->sc.nbins = own;
+                        if (!e.empty()) rc = fail(ctx, ALB_ERR_CUDA, e);
+                        else if (cudaStreamSynchronize(ctx->st) != cudaSuccess) rc = fail(ctx, ALB_ERR_CUDA, "reserve");
+                    }
+                    if (rc) msg = ctx->err;
+                }
+            } else {
+                std::string e = set_scene(ctx, I.scene);
+                if (e.empty()) e = ensure_accumulators(ctx);
+                if (!e.empty()) {
+                    rc = ALB_ERR_INVALID;
+                    msg = e;
+                } else {
+                    rc = soft_reset(ctx);
+                    if (rc) msg = ctx->err;
+                }
+            }
+            if (!rc && ctx) {
+                cudaEventRecord(e0, ctx->st);
+                rc = run_instance(ctx, I, opt->adjoint);
+                cudaEventRecord(e1, ctx->st);
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&I.device_ms, e0, e1);
+                if (rc) msg = ctx->err;
+            }
+            I.status = rc;
+            if (rc) {
+                std::lock_guard<std::mutex> g(msg_mu);
+                last_msg = msg;
+                if (ctx && (rc == ALB_ERR_CUDA || rc == ALB_ERR_ITER_CAP)) {  // start the next instance clean
+                    alb_destroy(ctx);
+                    ctx = nullptr;
+                }
+            }
+        }
+        if (ctx) alb_destroy(ctx);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st) cudaStreamDestroy(st);
+    };
+    std::vector<std::thread> pool;
+    const int K = (int)std::min<uint64_t>((uint64_t)opt->streams, std::max<uint64_t>(n, 1));
+    for (int w = 0; w < K; ++w) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+    g_create_error = last_msg;
     return ALB_OK;
 }

@@ -21,7 +21,10 @@ constexpr int kMaxEventsPerPhoton = 1 << 22;    // device loop cap -> ALB_ERR_IT
 struct SceneDev {
     double dt;
     int64_t total_steps;      // steps * sample_multiplier
-    int64_t nbins;            // 2 * steps
+    int64_t nbins;            // 2 * steps, or the gate's length
+    int64_t gate_lo;          // first timeline bin of the waveform (gated windows)
+    int32_t gated;            // 1: bins outside the window are dropped, not an error
+    int32_t pad_gate;
     int32_t mult;
     int32_t k;
     double ys, yf, v_air;

@@ -844,11 +844,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                         else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
                         else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
                         const float c = ((Es * m.a[idx].w) * norm) * w;
-                        const int bin = (int)((ts + pb.w) / (float)sc.mult);
+                        const int bin = (int)((ts + pb.w) / (float)sc.mult) - (int)sc.gate_lo;
                         if (bin >= 0 && bin < acc.nbins) {
                             bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
                             if (acc.jac_lo) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
-                        } else {
+                        } else if (!sc.gated) {
                             atomicCAS(err, 0, ALB_ERR_CAPACITY);
                         }
                         if (acc.hw_lo && m.fwi) heat_add(sc, m, acc, idx, c);
@@ -909,11 +909,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
                 else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
                 const float c = ((Es * m.a[idx].w) * norm) * w;
-                const int bin = (int)((ts + pb.w) / (float)sc.mult);
+                const int bin = (int)((ts + pb.w) / (float)sc.mult) - (int)sc.gate_lo;
                 if (bin >= 0 && bin < acc.nbins) {
                     bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
                     if (acc.jac_lo) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
-                } else {
+                } else if (!sc.gated) {
                     atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }
             }

@@ -6,6 +6,7 @@
 // that order as two float4 streams, and cut into buckets of 32 consecutive records. A
 // bucket's bounding box is a leaf; 32 consecutive boxes form the next level up, until 32
 // or fewer boxes remain. The gather walks this implicit 32-ary box tree warp-wide.
+#include <atomic>
 #include <algorithm>
 #include <cstdio>
 
@@ -1182,13 +1183,13 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         cudaMemcpyAsync(dcs, cs.data(), cs.size() * 4, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(dcc, cc.data(), cc.size() * 4, cudaMemcpyHostToDevice, st);
     }
-    static bool attr_set[64] = {false};
+    static std::atomic<bool> attr_set[64];  // batched runs build from several host threads
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
         cudaFuncSetAttribute(k_local_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
         cudaFuncSetAttribute(k_local_kd_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FullCellSmem));
-        attr_set[dev] = true;
+        attr_set[dev].store(true, std::memory_order_release);
     }
     if (!fs.empty()) {
         k_local_kd_full<<<(unsigned)fs.size(), kFullThreads, sizeof(FullCellSmem), st>>>(X, dfs);
@@ -1381,7 +1382,7 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     compute_bbox(ws, rec.a, n, lo, hi, st);
     m.grid = make_key_grid(lo, hi);
     cudaStreamSynchronize(st);
-    release_map_index(m);
+    if (n > m.a_cap) release_map_index(m);  // else every array is reused in place
     m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
     if (!m.a || kd_order_fast(ws, rec.a, n, lo, hi, m.a, st) != 0) return -1;
     cudaStreamSynchronize(st);  // the build temporary is back in the pool
@@ -1410,12 +1411,12 @@ int cell_index_max_points() { return kCellMax; }
 void launch_single_cell_index(const float4* pts, uint32_t n, const uint32_t* perm_in, const unsigned* cell,
                               uint32_t* perm_out, float4* sorted, float4* box_lo, float4* box_hi,
                               const uint64_t* lvl_off, const uint64_t* lvl_cnt, int nlevels, cudaStream_t st) {
-    static bool attr_set[64] = {false};
+    static std::atomic<bool> attr_set[64];  // batched runs build from several host threads
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
         cudaFuncSetAttribute(k_cell_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
-        attr_set[dev] = true;
+        attr_set[dev].store(true, std::memory_order_release);
     }
     const uint32_t P = (n + 31u) & ~31u;
     k_cell_kd<<<1, kCellThreads, cell_smem_bytes(), st>>>(pts, perm_in, cell, cell + 1, cell + 2, perm_out);

@@ -291,10 +291,13 @@ class SceneModel:
     heatmap_seafloor_extent: float = 10.0
     water_center: np.ndarray = None
     floor_center: np.ndarray = None
+    # extension: gated waveform window [gate_start, gate_start + gate_bins) of the timeline
+    gate_start: int = 0
+    gate_bins: int = 0
 
     @property
     def n_bins(self) -> int:
-        return 2 * self.steps
+        return self.gate_bins if self.gate_bins > 0 else 2 * self.steps
 
     @property
     def all_constant(self) -> bool:
@@ -409,6 +412,14 @@ def build_scene(cfg) -> SceneModel:
     floor_center = water_center + (-depth / refr[1]) * refr
 
     hm = cfg.heatmap
+    gate_start = gate_bins = 0
+    gate = getattr(cfg, "waveform_gate", None)
+    if gate is not None:
+        # one waveform bin is one sample period (sample_multiplier integrator steps)
+        gate_start = int(math.floor(float(gate[0]) * sample_rate))
+        gate_bins = max(1, int(round(float(gate[1]) * sample_rate)))
+        if gate_start + gate_bins > 2 * steps:
+            raise ValueError("the waveform gate ends after the simulated time span")
     return SceneModel(
         sample_rate=int(sample_rate),
         sample_multiplier=int(mult),
@@ -440,4 +451,6 @@ def build_scene(cfg) -> SceneModel:
         heatmap_seafloor_extent=float(hm.seafloor_extent),
         water_center=water_center,
         floor_center=floor_center,
+        gate_start=gate_start,
+        gate_bins=gate_bins,
     )

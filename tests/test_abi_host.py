@@ -90,7 +90,7 @@ REF_SRC = "/root/reference/src"
 # None (the reference's behaviour): Henyey-Greenstein phase, fixed-radius gather.
 EXTENSION_FIELDS = {
     "TurbidityLayerConfig": ["henyey_greenstein_g"],
-    "SimulationConfig": ["gather_radius"],
+    "SimulationConfig": ["gather_radius", "waveform_gate"],
 }
 
 _EXT_NAMES = {f for fs in EXTENSION_FIELDS.values() for f in fs}
