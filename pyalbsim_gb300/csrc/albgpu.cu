@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <condition_variable>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -241,11 +242,31 @@ static std::string set_scene(AlbCtx* ctx, const AlbSceneParams* p) {
     s.gate_lo = 0;
     s.gated = 0;
     if (p->gate_bins < 0 || p->gate_start < 0) return std::string("gate_start and gate_bins must be >= 0");
+    s.stop_step[ALB_FORWARD] = s.stop_step[ALB_BACKWARD] = s.total_steps;
     if (p->gate_bins > 0) {
         if (p->gate_start + p->gate_bins > 2 * p->steps) return std::string("the gate must lie inside the timeline");
         s.nbins = p->gate_bins;
         s.gate_lo = p->gate_start;
         s.gated = 1;
+        // With the fixed-radius gather every (query, record) pair contributes on its own. A
+        // contribution lands in bin (t_query + t_record) / multiplier. Every photon starts at
+        // the origin, |surface_y| above the water, and no record or query is made before it
+        // reaches the surface: t >= floor(|surface_y| / (c_air dt)) - 2 steps, less the
+        // forward pulse offset (bounded by 7 sigma / effective rate steps). A photon of one
+        // pass can therefore stop once its steps exceed the gate's end minus the other
+        // pass's earliest time: nothing it would add later can land in the window. (The
+        // k-NN estimate is not pairwise: a late record can still be among a query's k
+        // nearest and set its radius, so k-NN runs trace the whole timeline.)
+        const double step_air = p->speed_air * p->dt;
+        const int64_t t_surface = std::max<int64_t>((int64_t)std::floor(-p->surface_y / step_air) - 2, 0);
+        const int64_t pulse = (int64_t)std::ceil(7.0 * p->pulse_sigma / (double)(float)p->effective_rate) + 1;
+        const int64_t end = (p->gate_start + p->gate_bins + 2) * (int64_t)p->sample_multiplier;
+        const int64_t fwd = end - t_surface + pulse + 4;                           // queries start >= t_surface
+        const int64_t bwd = end - std::max<int64_t>(t_surface - pulse, 0) + 4;     // records start >= t_surface - pulse
+        if (p->gather_radius > 0.0) {
+            s.stop_step[ALB_FORWARD] = std::min(s.total_steps, std::max<int64_t>(fwd, 0));
+            s.stop_step[ALB_BACKWARD] = std::min(s.total_steps, std::max<int64_t>(bwd, 0));
+        }
     }
     s.mult = p->sample_multiplier;
     s.k = p->k;
@@ -1233,8 +1254,29 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
     std::atomic<uint64_t> next{0};
     std::mutex msg_mu;
     std::string last_msg;
+    // Device-memory admission. A context keeps the buffers of the largest instance it ran,
+    // so each worker holds an estimate of that footprint against a budget (80% of the free
+    // memory at the start); a worker whose next instance needs more waits until the pool
+    // has room or it is the only one running, and a worker dropping to instances a quarter
+    // of its footprint releases its context. Footprint = forward photons x records per
+    // photon (the largest seen so far x 1.5, 200 before any instance finished) x bytes per
+    // record (append store, index, build temporaries; scores with the adjoint) + 64 MiB.
+    cudaSetDevice(opt->device);
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const double budget = 0.8 * (double)free_b;
+    const double bytes_per_record = opt->adjoint ? 160.0 : 128.0;
+    std::mutex mem_mu;
+    std::condition_variable mem_cv;
+    double held_total = 0.0, rpp_seen = 0.0;
+    int running = 0;
+    auto need_of = [&](const AlbBatchInstance& I) {
+        const double rpp = rpp_seen > 0.0 ? 1.5 * rpp_seen : 200.0;
+        return (double)I.n_forward * rpp * bytes_per_record + 64.0 * 1048576.0;
+    };
     auto worker = [&]() {
         cudaSetDevice(opt->device);
+        double held = 0.0;
         cudaStream_t st = nullptr;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) st = nullptr;
         AlbCtx* ctx = nullptr;
@@ -1246,6 +1288,24 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
             I.device_ms = 0.f;
             int rc = ALB_OK;
             std::string msg;
+            {
+                std::unique_lock<std::mutex> g(mem_mu);
+                const double need = need_of(I);
+                if (ctx && held > (double)(1 << 30) && 4.0 * need < held) {  // shrink for the small tail
+                    g.unlock();
+                    alb_destroy(ctx);
+                    ctx = nullptr;
+                    g.lock();
+                    held_total -= held;
+                    held = 0.0;
+                    mem_cv.notify_all();
+                }
+                const double grow = std::max(0.0, need - held);
+                mem_cv.wait(g, [&] { return held_total + grow <= budget || running == 0; });
+                held_total += grow;
+                held += grow;
+                ++running;
+            }
             if (!ctx) {
                 rc = alb_create(I.scene, opt->device, &ctx);
                 if (rc) {
@@ -1285,17 +1345,36 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                 cudaEventElapsedTime(&I.device_ms, e0, e1);
                 if (rc) msg = ctx->err;
             }
+            {
+                std::lock_guard<std::mutex> g(mem_mu);
+                if (!rc && ctx && I.n_forward > 0) {
+                    uint64_t recs = 0;
+                    for (int c = 0; c < ALB_CHANNELS; ++c) recs += ctx->h_rec_count[c];
+                    rpp_seen = std::max(rpp_seen, (double)recs / (double)I.n_forward);
+                }
+                --running;
+                mem_cv.notify_all();
+            }
             I.status = rc;
             if (rc) {
                 std::lock_guard<std::mutex> g(msg_mu);
                 last_msg = msg;
-                if (ctx && (rc == ALB_ERR_CUDA || rc == ALB_ERR_ITER_CAP)) {  // start the next instance clean
-                    alb_destroy(ctx);
+                if (ctx && (rc == ALB_ERR_CUDA || rc == ALB_ERR_ITER_CAP || rc == ALB_ERR_CAPACITY)) {
+                    alb_destroy(ctx);  // start the next instance clean
                     ctx = nullptr;
+                    std::lock_guard<std::mutex> m(mem_mu);
+                    held_total -= held;
+                    held = 0.0;
+                    mem_cv.notify_all();
                 }
             }
         }
         if (ctx) alb_destroy(ctx);
+        {
+            std::lock_guard<std::mutex> g(mem_mu);
+            held_total -= held;
+            mem_cv.notify_all();
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (st) cudaStreamDestroy(st);

@@ -21,6 +21,7 @@ constexpr int kMaxEventsPerPhoton = 1 << 22;    // device loop cap -> ALB_ERR_IT
 struct SceneDev {
     double dt;
     int64_t total_steps;      // steps * sample_multiplier
+    int64_t stop_step[2];     // per pass: steps traced (total_steps unless a gate ends earlier)
     int64_t nbins;            // 2 * steps, or the gate's length
     int64_t gate_lo;          // first timeline bin of the waveform (gated windows)
     int32_t gated;            // 1: bins outside the window are dropped, not an error

@@ -660,7 +660,7 @@ ALB_DEVICE void emit_photon(const SceneDev& sc, Ph& ph, Src& src) {
 template <int PASS, class Src>
 ALB_DEVICE void trace_photon(const SceneDev& sc, const TraceOut& out, Ph& ph, Src& src, uint32_t pid,
                              unsigned long long& events) {
-    const int64_t S = sc.total_steps;
+    const int64_t S = sc.stop_step[PASS];
     int guard = 0;
     while (ph.s < S) {
         if (++guard > kMaxEventsPerPhoton) {

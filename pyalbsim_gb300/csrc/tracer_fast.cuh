@@ -113,7 +113,7 @@ ALB_DEVICE float water_alpha_f(const SceneDev& sc, float y) {
 template <int PASS>
 ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const TraceOut& out, PhF& ph,
                                   PhiloxSrc& src, uint32_t pid, unsigned long long& events) {
-    const int S = (int)sc.total_steps;
+    const int S = (int)sc.stop_step[PASS];
     const float ys = (float)sc.ys, yf = (float)sc.yf, dt = (float)sc.dt;
     const float eta = (float)sc.eta, f0 = (float)sc.f0;
     int guard = 0;

@@ -14,7 +14,7 @@ from typing import Optional
 import numpy as np
 
 
-def _config(height, a, b, fov, rate, albedo, ggx_alpha, hg: Optional[float]):
+def _config(height, a, b, fov, rate, albedo, ggx_alpha, hg: Optional[float], radius: Optional[float] = None):
     from pyalbsim_gb300.config import (
         HeatmapConfig, LaserConfig, SceneConfig, SeaFloorConfig, SeaSurfaceConfig, SensorConfig,
         SimulationConfig, TurbidityLayerConfig, WaterConfig,
@@ -30,15 +30,16 @@ def _config(height, a, b, fov, rate, albedo, ggx_alpha, hg: Optional[float]):
         sea_floor=SeaFloorConfig(albedo=albedo),
         sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(ggx_alpha))),
         heatmap=HeatmapConfig(enabled=False),
+        gather_radius=radius,
     )
 
 
-def large(hg: Optional[float] = None):
-    return _config(20.0, 0.10, 0.40, 50e-3, 2e10, 0.20, 0.10, hg)
+def large(hg: Optional[float] = None, radius: Optional[float] = None):
+    return _config(20.0, 0.10, 0.40, 50e-3, 2e10, 0.20, 0.10, hg, radius)
 
 
-def small(hg: Optional[float] = None):
-    return _config(5.0, 0.05, 0.20, 20e-3, 1e10, 0.15, 0.05, hg)
+def small(hg: Optional[float] = None, radius: Optional[float] = None):
+    return _config(5.0, 0.05, 0.20, 20e-3, 1e10, 0.15, 0.05, hg, radius)
 
 
 def workload_config(name: str, hg: Optional[float] = None):

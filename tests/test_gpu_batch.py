@@ -45,9 +45,21 @@ def test_gated_waveform_is_the_slice_of_the_full_one(gpu_available, adjoint):
         np.testing.assert_array_equal(jg, jf[:, :, gs.gate_start:gs.gate_start + gs.n_bins])
 
 
+def test_gate_with_fixed_radius_stops_early_and_keeps_the_window(gpu_available):
+    """Fixed-radius gather: photons stop at the last step that can still reach the window,
+    and the window is bit-identical to the full-timeline run's bins."""
+    base = workloads.small(0.9, radius=0.5)
+    full, _ = _single(base, 50000, 12500, 6)
+    gcfg = dataclasses.replace(base, waveform_gate=batch.surface_gate(base))
+    gs = build_scene(gcfg)
+    g, _ = _single(gcfg, 50000, 12500, 6)
+    np.testing.assert_array_equal(g, full[:, gs.gate_start:gs.gate_start + gs.n_bins])
+    assert g.sum() > 0
+
+
 @pytest.mark.parametrize("adjoint,streams", [(False, 4), (True, 3)])
 def test_batch_equals_single_instance_runs(gpu_available, adjoint, streams):
-    base = workloads.small(0.9)
+    base = workloads.small(0.9, radius=0.5)
     inst = batch.hypercube_instances(base, 12, seed=7, photons=(2e3, 4e4), gate=batch.surface_gate(base))
     w, j, st, ms, wall = batch.run_batch(inst, streams=streams, adjoint=adjoint)
     assert np.all(st == 0), st
@@ -61,7 +73,7 @@ def test_batch_equals_single_instance_runs(gpu_available, adjoint, streams):
 
 
 def test_batch_reports_a_failed_instance_and_runs_the_rest(gpu_available):
-    base = workloads.small(0.9)
+    base = workloads.small(0.9, radius=0.5)
     inst = batch.hypercube_instances(base, 4, seed=9, photons=(2e3, 1e4), gate=batch.surface_gate(base))
     scenes = [build_scene(x.config) for x in inst]
     scenes[1].gate_start = 10 ** 9  # a window past the timeline: rejected for this instance only
