@@ -145,6 +145,10 @@ typedef struct AlbSceneParams {
      * where a bin outside it is an error (ALB_ERR_CAPACITY). */
     int64_t gate_start;
     int64_t gate_bins;
+    /* Extension: Gaussian surface slopes. > 0: at every surface interaction the facet normal
+     * is normalize(-gx, 1, -gz), gx, gz ~ N(0, slope_sigma^2), for reflection, refraction and
+     * Fresnel (Philox mode only); 0: the reference's flat surface. */
+    double slope_sigma;
 } AlbSceneParams;
 
 /* Caller-supplied variates (replay mode): photon i consumes values[offsets[i] ..

@@ -366,6 +366,19 @@ static void record(OrBuf* out, int channel, int photon, int64_t step, const doub
     buf_push(out, &r);
 }
 
+/* Extension (the reference's surface is flat): Gaussian surface slopes. Facet normal
+ * normalize(-gx, 1, -gz), gx, gz ~ N(0, sigma^2) from one Box-Muller block; a facet facing
+ * away from the photon, or one sending it to the wrong side, falls back to the flat surface. */
+static void draw_facet(const AlbSceneParams* P, Src* s, double mf[3]) {
+    U4 b = src_block(s);
+    double r0 = sqrt(-2.0 * log(u01(b.x))), a0 = TWO_PI * u01(b.y);
+    double gx = r0 * cos(a0) * P->slope_sigma, gz = r0 * sin(a0) * P->slope_sigma;
+    double nn = norm3(gx, 1.0, gz);
+    mf[0] = -gx / nn;
+    mf[1] = 1.0 / nn;
+    mf[2] = -gz / nn;
+}
+
 static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBuf* out, unsigned* hm_radius) {
     const AlbSceneParams* P = m->p;
     const double ys = P->surface_y, yf = P->floor_y, dt = P->dt;
@@ -430,32 +443,88 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
             for (int i = 0; i < 3; ++i) ph->fwi[i] = (float)xs[i];
             double F = schlick(P->f0, -ph->d[1]);
             record(out, pass == ALB_FORWARD ? ALB_SURFACE_REFLECTION : 2, photon, step, xs, ph);
-            double ci = -ph->d[1];
-            ci = ci < -1.0 ? -1.0 : (ci > 1.0 ? 1.0 : ci);
-            double sin2 = (m->eta * m->eta) * (1.0 - ci * ci);
-            double ct = sqrt(fmax(0.0, 1.0 - sin2));
-            double t[3] = {m->eta * ph->d[0], m->eta * ph->d[1] + (m->eta * ci - ct), m->eta * ph->d[2]};
-            double tn = norm3(t[0], t[1], t[2]);
-            for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+            int flat = 1;
+            if (P->slope_sigma > 0.0) {
+                double mf[3];
+                draw_facet(P, s, mf);
+                double cf = -(ph->d[0] * mf[0] + ph->d[1] * mf[1] + ph->d[2] * mf[2]);
+                if (cf > 0.0) {
+                    cf = cf > 1.0 ? 1.0 : cf;
+                    double ctf = sqrt(fmax(0.0, 1.0 - (m->eta * m->eta) * (1.0 - cf * cf)));
+                    double k = m->eta * cf - ctf;
+                    double t[3];
+                    for (int i = 0; i < 3; ++i) t[i] = m->eta * ph->d[i] + k * mf[i];
+                    if (t[1] < 0.0) {
+                        double tn = norm3(t[0], t[1], t[2]);
+                        for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+                        F = schlick(P->f0, cf);
+                        flat = 0;
+                    }
+                }
+            }
+            if (flat) {
+                double ci = -ph->d[1];
+                ci = ci < -1.0 ? -1.0 : (ci > 1.0 ? 1.0 : ci);
+                double sin2 = (m->eta * m->eta) * (1.0 - ci * ci);
+                double ct = sqrt(fmax(0.0, 1.0 - sin2));
+                double t[3] = {m->eta * ph->d[0], m->eta * ph->d[1] + (m->eta * ci - ct), m->eta * ph->d[2]};
+                double tn = norm3(t[0], t[1], t[2]);
+                for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+            }
             ph->E = (float)((double)ph->E * (1.0 - F));
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
             ph->taut = s->replay ? src_next_tau(s) : tau_of(u01(src_block(s).x));
         } else if (st == 4) {
-            double F = schlick(P->f0, ph->d[1]);
+            double mf[3] = {0.0, 1.0, 0.0}, cf = ph->d[1];
+            int tilted = 0;
+            if (P->slope_sigma > 0.0) {
+                draw_facet(P, s, mf);
+                cf = ph->d[0] * mf[0] + ph->d[1] * mf[1] + ph->d[2] * mf[2];
+                tilted = cf > 0.0;
+                if (!tilted) {
+                    mf[0] = 0.0; mf[1] = 1.0; mf[2] = 0.0;
+                    cf = ph->d[1];
+                }
+            }
+            double F = schlick(P->f0, tilted ? (cf > 1.0 ? 1.0 : cf) : ph->d[1]);
             double U = s->replay ? src_next(s) : u01(src_block(s).x);
             int reflect = U < F;
             if (pass == ALB_FORWARD && !reflect) record(out, ALB_SURFACE_TRANSMISSION_UP, photon, step, xs, ph);
-            double ci = ph->d[1];
+            double ci = tilted ? cf : ph->d[1];
             ci = ci < -1.0 ? -1.0 : (ci > 1.0 ? 1.0 : ci);
             double sin2 = (m->eta * m->eta) * (1.0 - ci * ci);
             double ct = sqrt(fmax(0.0, 1.0 - sin2));
             if (sin2 > 1.0) reflect = 1;
-            if (reflect) {
-                ph->d[1] = -ph->d[1];
-            } else {
-                double t[3] = {m->eta * ph->d[0], m->eta * ph->d[1] - (m->eta * ci - ct), m->eta * ph->d[2]};
-                double tn = norm3(t[0], t[1], t[2]);
-                for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+            int done = 0;
+            if (tilted) {
+                if (reflect) {
+                    double r[3];
+                    for (int i = 0; i < 3; ++i) r[i] = ph->d[i] - 2.0 * cf * mf[i];
+                    if (r[1] < 0.0) {
+                        for (int i = 0; i < 3; ++i) ph->d[i] = r[i];
+                        done = 1;
+                    }
+                } else {
+                    double k = m->eta * ci - ct, t[3];
+                    for (int i = 0; i < 3; ++i) t[i] = m->eta * ph->d[i] - k * mf[i];
+                    if (t[1] > 0.0) {
+                        double tn = norm3(t[0], t[1], t[2]);
+                        for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+                        done = 1;
+                    }
+                }
+            }
+            if (!done) {
+                if (reflect) {
+                    ph->d[1] = -ph->d[1];
+                } else {
+                    double c0 = ph->d[1];
+                    c0 = c0 < -1.0 ? -1.0 : (c0 > 1.0 ? 1.0 : c0);
+                    double ct0 = sqrt(fmax(0.0, 1.0 - (m->eta * m->eta) * (1.0 - c0 * c0)));
+                    double t[3] = {m->eta * ph->d[0], m->eta * ph->d[1] - (m->eta * c0 - ct0), m->eta * ph->d[2]};
+                    double tn = norm3(t[0], t[1], t[2]);
+                    for (int i = 0; i < 3; ++i) ph->d[i] = t[i] / tn;
+                }
             }
             for (int i = 0; i < 3; ++i) ph->p[i] = xs[i] + ph->d[i] * rem;
             if (reflect) {

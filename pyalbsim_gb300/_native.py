@@ -102,6 +102,7 @@ class AlbSceneParams(C.Structure):
         ("gather_radius", C.c_double),
         ("gate_start", C.c_int64),
         ("gate_bins", C.c_int64),
+        ("slope_sigma", C.c_double),
     ]
 
 
@@ -259,6 +260,7 @@ def scene_struct(scene: SceneModel):
     p.gather_radius = float(scene.gather_radius or 0.0)
     p.gate_start = int(scene.gate_start)
     p.gate_bins = int(scene.gate_bins)
+    p.slope_sigma = float(scene.slope_sigma)
     p.heatmap_enabled = int(scene.heatmap_enabled)
     p.heatmap_bins = scene.heatmap_bins
     p.heatmap_water_extent = scene.heatmap_water_extent

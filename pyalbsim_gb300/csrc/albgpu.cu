@@ -293,6 +293,8 @@ static std::string set_scene(AlbCtx* ctx, const AlbSceneParams* p) {
     s.rayleigh_mass = -std::expm1(-(p->divergence * p->divergence) / (2.0 * s.rayleigh_sigma * s.rayleigh_sigma));
     s.n_layers = p->n_layers;
     if (!(p->gather_radius >= 0.0)) return std::string("gather_radius must be >= 0 (0 selects the k-NN gather)");
+    if (!(p->slope_sigma >= 0.0)) return std::string("slope_sigma must be >= 0");
+    s.slope_sigma = p->slope_sigma;
     s.radius = p->gather_radius;
     s.heatmap = p->heatmap_enabled;
     s.hm_bins = p->heatmap_bins;
@@ -679,6 +681,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
     if (pass != ALB_FORWARD && pass != ALB_BACKWARD) return fail(ctx, ALB_ERR_INVALID, "pass must be 0 or 1");
     if (pass == ALB_BACKWARD && !ctx->maps_built) return fail(ctx, ALB_ERR_STATE, "backward trace before alb_build_maps");
     if (first + n > (1ull << 32)) return fail(ctx, ALB_ERR_INVALID, "photon ids are 32-bit per pass");
+    if (rp && ctx->sc.slope_sigma > 0.0)
+        return fail(ctx, ALB_ERR_INVALID, "surface slopes draw variates the reference never records (Philox only)");
     CK(cudaSetDevice(ctx->device));
     ctx->err.clear();
     // replay streams to the device

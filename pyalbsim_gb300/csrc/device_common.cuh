@@ -32,6 +32,7 @@ struct SceneDev {
     double n_water, eta, f0;
     double floor_albedo, surface_albedo, roughness;
     double radius;            // extension: fixed gather radius (m), 0 = k nearest
+    double slope_sigma;       // extension: Gaussian surface-slope std (0 = flat surface)
     float floor_albedo32;
     float ggx_a2;             // (roughness^2)^2 as used by the GGX distribution
     double rot_d[9];          // float32 laser rotation, widened

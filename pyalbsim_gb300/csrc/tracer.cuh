@@ -486,6 +486,22 @@ ALB_DEVICE void emit_event(const TraceOut& out, int channel, int qkind, const Ph
 // Event handlers (one crossing step each)
 // ----------------------------------------------------------------------------------------
 
+// Extension (no counterpart in the reference, whose surface normal is +y / -y): Gaussian
+// surface slopes. At every surface interaction the facet normal is normalize(-gx, 1, -gz)
+// with slope components gx, gz ~ N(0, sigma^2) (one Box-Muller block). Reflection, Snell
+// refraction and the Fresnel factor use the facet; a facet facing away from the photon, or
+// one that would send it to the wrong side of the mean surface, falls back to the flat one.
+template <class Src>
+ALB_DEVICE void draw_facet(const SceneDev& sc, Src& src, double& mx, double& my, double& mz) {
+    double n0, n1, n2;
+    draw_normals(src, n0, n1, n2);
+    const double gx = n0 * sc.slope_sigma, gz = n1 * sc.slope_sigma;
+    const double nn = norm3(gx, 1.0, gz);
+    mx = -gx / nn;
+    my = 1.0 / nn;
+    mz = -gz / nn;
+}
+
 template <int PASS, class Src>
 ALB_DEVICE void handle_enter(const SceneDev& sc, const TraceOut& out, Ph& ph, Src& src,
                              double svx, double svy, double svz, uint32_t pid) {
@@ -497,14 +513,34 @@ ALB_DEVICE void handle_enter(const SceneDev& sc, const TraceOut& out, Ph& ph, Sr
     ph.fwi[0] = (float)xs; ph.fwi[1] = (float)ys; ph.fwi[2] = (float)zs;
     double F = schlick64(sc.f0, -ph.dy);
     emit_event<PASS>(out, ALB_SURFACE_REFLECTION, kQuerySurface, ph, xs, ys, zs, ph.s, pid);
-    // Snell, air -> water, normal +y
     double eta = sc.eta;
-    double ci = fmin(fmax(-ph.dy, -1.0), 1.0);
-    double sin2 = (eta * eta) * (1.0 - ci * ci);
-    double ct = sqrt(fmax(0.0, 1.0 - sin2));
-    double tx = eta * ph.dx, ty = eta * ph.dy + (eta * ci - ct), tz = eta * ph.dz;
-    double tn = norm3(tx, ty, tz);
-    ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+    bool flat = true;
+    if (sc.slope_sigma > 0.0) {
+        double mx, my, mz;
+        draw_facet(sc, src, mx, my, mz);
+        double ci = -(ph.dx * mx + ph.dy * my + ph.dz * mz);
+        if (ci > 0.0) {
+            ci = fmin(ci, 1.0);
+            double ct = sqrt(fmax(0.0, 1.0 - (eta * eta) * (1.0 - ci * ci)));
+            double k = eta * ci - ct;
+            double tx = eta * ph.dx + k * mx, ty = eta * ph.dy + k * my, tz = eta * ph.dz + k * mz;
+            if (ty < 0.0) {
+                double tn = norm3(tx, ty, tz);
+                ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+                F = schlick64(sc.f0, ci);
+                flat = false;
+            }
+        }
+    }
+    if (flat) {
+        // Snell, air -> water, normal +y
+        double ci = fmin(fmax(-ph.dy, -1.0), 1.0);
+        double sin2 = (eta * eta) * (1.0 - ci * ci);
+        double ct = sqrt(fmax(0.0, 1.0 - sin2));
+        double tx = eta * ph.dx, ty = eta * ph.dy + (eta * ci - ct), tz = eta * ph.dz;
+        double tn = norm3(tx, ty, tz);
+        ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+    }
     ph.E = (float)((double)ph.E * (1.0 - F));
     double len = norm3(stx, sty, stz);
     double rem = (1.0 - f) * len;
@@ -520,24 +556,54 @@ ALB_DEVICE void handle_exit(const SceneDev& sc, const TraceOut& out, Ph& ph, Src
     double f = (sc.ys - ph.py) / sty;
     f = fmin(fmax(f, 0.0), 1.0);
     double xs = ph.px + f * stx, ys = ph.py + f * sty, zs = ph.pz + f * stz;
-    double F = schlick64(sc.f0, ph.dy);
+    double mx = 0.0, my = 1.0, mz = 0.0, cf = ph.dy;  // facet (upward) and cos to it
+    bool tilted = false;
+    if (sc.slope_sigma > 0.0) {
+        draw_facet(sc, src, mx, my, mz);
+        cf = ph.dx * mx + ph.dy * my + ph.dz * mz;
+        tilted = cf > 0.0;
+        if (!tilted) { mx = 0.0; my = 1.0; mz = 0.0; cf = ph.dy; }
+    }
+    double F = schlick64(sc.f0, tilted ? fmin(cf, 1.0) : ph.dy);
     double U = draw_uniform(src);
     bool reflect = U < F;
     if (PASS == ALB_FORWARD && !reflect)
         emit_event<PASS>(out, ALB_SURFACE_TRANSMISSION_UP, 0, ph, xs, ys, zs, ph.s, pid);
     // Snell with the reference's fixed 1 -> n_water ratio and normal -y
     double eta = sc.eta;
-    double ci = fmin(fmax(ph.dy, -1.0), 1.0);
+    double ci = fmin(fmax(tilted ? cf : ph.dy, -1.0), 1.0);
     double sin2 = (eta * eta) * (1.0 - ci * ci);
     double ct = sqrt(fmax(0.0, 1.0 - sin2));
     reflect = reflect || (sin2 > 1.0);
     double len = norm3(stx, sty, stz);
-    if (reflect) {
-        ph.dy = -ph.dy;
-    } else {
-        double tx = eta * ph.dx, ty = eta * ph.dy - (eta * ci - ct), tz = eta * ph.dz;
-        double tn = norm3(tx, ty, tz);
-        ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+    bool done = false;
+    if (tilted) {
+        if (reflect) {
+            double rx = ph.dx - 2.0 * cf * mx, ry = ph.dy - 2.0 * cf * my, rz = ph.dz - 2.0 * cf * mz;
+            if (ry < 0.0) {
+                ph.dx = rx; ph.dy = ry; ph.dz = rz;
+                done = true;
+            }
+        } else {
+            double k = eta * ci - ct;
+            double tx = eta * ph.dx - k * mx, ty = eta * ph.dy - k * my, tz = eta * ph.dz - k * mz;
+            if (ty > 0.0) {
+                double tn = norm3(tx, ty, tz);
+                ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+                done = true;
+            }
+        }
+    }
+    if (!done) {
+        if (reflect) {
+            ph.dy = -ph.dy;
+        } else {
+            double cf0 = fmin(fmax(ph.dy, -1.0), 1.0);
+            double ct0 = sqrt(fmax(0.0, 1.0 - (eta * eta) * (1.0 - cf0 * cf0)));
+            double tx = eta * ph.dx, ty = eta * ph.dy - (eta * cf0 - ct0), tz = eta * ph.dz;
+            double tn = norm3(tx, ty, tz);
+            ph.dx = tx / tn; ph.dy = ty / tn; ph.dz = tz / tn;
+        }
     }
     double rem = (1.0 - f) * len;
     ph.px = xs + ph.dx * rem; ph.py = ys + ph.dy * rem; ph.pz = zs + ph.dz * rem;

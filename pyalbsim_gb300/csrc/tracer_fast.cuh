@@ -110,6 +110,21 @@ ALB_DEVICE float water_alpha_f(const SceneDev& sc, float y) {
     return sc.layer_prof[L] ? water_alpha(sc, (double)y) : sc.layer_alpha[L];
 }
 
+// Gaussian surface slopes (extension; see draw_facet in tracer.cuh): facet normal
+// normalize(-gx, 1, -gz), gx, gz ~ N(0, sigma^2) from one Box-Muller block.
+ALB_DEVICE void draw_facet_f(const SceneDev& sc, PhiloxSrc& src, float& mx, float& my, float& mz) {
+    U4 b = src.block();
+    const float r = sqrtf(-2.f * __logf(uf(b.x)));
+    float sa, ca;
+    __sincosf(6.283185307179586f * uf(b.y), &sa, &ca);
+    const float s = (float)sc.slope_sigma;
+    const float gx = r * ca * s, gz = r * sa * s;
+    const float inv = rsqrtf(fmaf(gx, gx, fmaf(gz, gz, 1.f)));
+    mx = -gx * inv;
+    my = inv;
+    mz = -gz * inv;
+}
+
 template <int PASS>
 ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const TraceOut& out, PhF& ph,
                                   PhiloxSrc& src, uint32_t pid, unsigned long long& events) {
@@ -142,9 +157,21 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.fwi[0] = xs; ph.fwi[1] = yss; ph.fwi[2] = zs;
             float F = schlick_f(f0, -ph.dy);
             emit_event_f<PASS>(out, ALB_SURFACE_REFLECTION, kQuerySurface, ph, xs, yss, zs, ph.s, pid);
-            float ci = fminf(fmaxf(-ph.dy, -1.f), 1.f);
+            float mx = 0.f, my = 1.f, mz = 0.f;
+            if (sc.slope_sigma > 0.0) {
+                draw_facet_f(sc, src, mx, my, mz);
+                if (!(-(ph.dx * mx + ph.dy * my + ph.dz * mz) > 0.f)) { mx = 0.f; my = 1.f; mz = 0.f; }
+            }
+            float ci = fminf(fmaxf(-(ph.dx * mx + ph.dy * my + ph.dz * mz), -1.f), 1.f);
             float ct = sqrtf(fmaxf(0.f, 1.f - eta * eta * (1.f - ci * ci)));
-            float tx = eta * ph.dx, ty = eta * ph.dy + (eta * ci - ct), tz = eta * ph.dz;
+            float kt = eta * ci - ct;
+            float tx = fmaf(kt, mx, eta * ph.dx), ty = fmaf(kt, my, eta * ph.dy), tz = fmaf(kt, mz, eta * ph.dz);
+            if (!(ty < 0.f)) {  // a steep facet would send the photon up: the mean surface instead
+                ci = fminf(fmaxf(-ph.dy, -1.f), 1.f);
+                ct = sqrtf(fmaxf(0.f, 1.f - eta * eta * (1.f - ci * ci)));
+                tx = eta * ph.dx; ty = eta * ph.dy + (eta * ci - ct); tz = eta * ph.dz;
+            }
+            F = schlick_f(f0, ci);
             float tn = rsqrtf(fmaf(tx, tx, fmaf(ty, ty, tz * tz)));
             ph.dx = tx * tn; ph.dy = ty * tn; ph.dz = tz * tn;
             ph.E *= (1.f - F);
@@ -226,16 +253,30 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             // handle_exit
             float f = fminf(fmaxf((ys - ph.py) / svy, 0.f), 1.f);
             float xs = fmaf(f, svx, ph.px), yss = ys, zs = fmaf(f, svz, ph.pz);
-            float F = schlick_f(f0, ph.dy);
+            float mx = 0.f, my = 1.f, mz = 0.f;
+            if (sc.slope_sigma > 0.0) {
+                draw_facet_f(sc, src, mx, my, mz);
+                if (!(ph.dx * mx + ph.dy * my + ph.dz * mz > 0.f)) { mx = 0.f; my = 1.f; mz = 0.f; }
+            }
+            const float cf = fminf(ph.dx * mx + ph.dy * my + ph.dz * mz, 1.f);
+            float F = schlick_f(f0, cf);
             bool reflect = uf(src.block().x) < F;
             if (PASS == ALB_FORWARD && !reflect)
                 emit_event_f<PASS>(out, ALB_SURFACE_TRANSMISSION_UP, 0, ph, xs, yss, zs, ph.s, pid);
             if (reflect) {
-                ph.dy = -ph.dy;
+                const float rx = ph.dx - 2.f * cf * mx, ry = ph.dy - 2.f * cf * my, rz = ph.dz - 2.f * cf * mz;
+                if (ry < 0.f) { ph.dx = rx; ph.dy = ry; ph.dz = rz; }
+                else ph.dy = -ph.dy;
             } else {
-                float ci = fminf(fmaxf(ph.dy, -1.f), 1.f);
+                float ci = fmaxf(cf, -1.f);
                 float ct = sqrtf(fmaxf(0.f, 1.f - eta * eta * (1.f - ci * ci)));
-                float tx = eta * ph.dx, ty = eta * ph.dy - (eta * ci - ct), tz = eta * ph.dz;
+                float k = eta * ci - ct;
+                float tx = fmaf(-k, mx, eta * ph.dx), ty = fmaf(-k, my, eta * ph.dy), tz = fmaf(-k, mz, eta * ph.dz);
+                if (!(ty > 0.f)) {
+                    ci = fminf(fmaxf(ph.dy, -1.f), 1.f);
+                    ct = sqrtf(fmaxf(0.f, 1.f - eta * eta * (1.f - ci * ci)));
+                    tx = eta * ph.dx; ty = eta * ph.dy - (eta * ci - ct); tz = eta * ph.dz;
+                }
                 float tn = rsqrtf(fmaf(tx, tx, fmaf(ty, ty, tz * tz)));
                 ph.dx = tx * tn; ph.dy = ty * tn; ph.dz = tz * tn;
             }

@@ -294,6 +294,7 @@ class SceneModel:
     # extension: gated waveform window [gate_start, gate_start + gate_bins) of the timeline
     gate_start: int = 0
     gate_bins: int = 0
+    slope_sigma: float = 0.0  # extension: Gaussian surface-slope std (0 = flat)
 
     @property
     def n_bins(self) -> int:
@@ -453,4 +454,5 @@ def build_scene(cfg) -> SceneModel:
         floor_center=floor_center,
         gate_start=gate_start,
         gate_bins=gate_bins,
+        slope_sigma=float(getattr(cfg.sea_surface, "slope_sigma", None) or 0.0),
     )

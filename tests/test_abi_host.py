@@ -91,6 +91,7 @@ REF_SRC = "/root/reference/src"
 EXTENSION_FIELDS = {
     "TurbidityLayerConfig": ["henyey_greenstein_g"],
     "SimulationConfig": ["gather_radius", "waveform_gate"],
+    "SeaSurfaceConfig": ["slope_sigma"],
 }
 
 _EXT_NAMES = {f for fs in EXTENSION_FIELDS.values() for f in fs}

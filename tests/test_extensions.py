@@ -148,3 +148,38 @@ def test_oracle_radius_gather_on_empty_map_is_zero():
     wf = np.zeros(scene.n_bins)
     Oracle(scene).gather(ALB_BOTTOM_REFLECTION, m, q, wf)
     assert not wf.any()
+
+
+def _slope_cfg(sigma, name="replay_small.npz"):
+    cfg = config_from_fixture(load(name))
+    return dataclasses.replace(cfg, sea_surface=dataclasses.replace(cfg.sea_surface, slope_sigma=sigma))
+
+
+def test_slope_config_validation():
+    with pytest.raises(ValueError):
+        _slope_cfg(-0.1)
+    assert build_scene(_slope_cfg(0.1)).slope_sigma == 0.1
+    assert build_scene(_slope_cfg(None)).slope_sigma == 0.0
+
+
+def test_oracle_slopes_spread_the_refracted_beam():
+    """Tilted facets spread the refracted beam: the direction a photon carries into its
+    first scatter (the refracted one) varies with the slope std, by about sigma (1 - 1/n)
+    per axis, and a zero std is the flat surface exactly."""
+    from oracle.oracle import oracle_run
+
+    def first_scatter_dirs(sigma):
+        r = oracle_run(build_scene(_slope_cfg(sigma)), 3000, 10, seed=4)
+        m = r["maps"][1]
+        first = np.unique(m["photon"], return_index=True)[1]
+        return r, m["dir"][first]
+
+    flat, dflat = first_scatter_dirs(None)
+    zero, _ = first_scatter_dirs(0.0)
+    np.testing.assert_array_equal(flat["maps"][0]["pos"], zero["maps"][0]["pos"])
+    _, dtilt = first_scatter_dirs(0.2)
+    # photons whose first scatter follows a seafloor reflection travel upwards: left out
+    dflat, dtilt = dflat[dflat[:, 1] < 0], dtilt[dtilt[:, 1] < 0]
+    s_flat, s_tilt = np.std(dflat[:, 2]), np.std(dtilt[:, 2])
+    expect = 0.2 * (1 - 1 / 1.33)
+    assert s_flat < 0.1 * expect and 0.5 * expect < s_tilt < 2.0 * expect, (s_flat, s_tilt, expect)

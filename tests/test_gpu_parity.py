@@ -475,3 +475,56 @@ def test_fast_and_precise_agree_in_distribution_hg(gpu_available):
     a, b = tot[True], tot[False]
     se = np.sqrt(a.var(0, ddof=1) / 8 + b.var(0, ddof=1) / 8)
     assert np.all(np.abs(a.mean(0) - b.mean(0)) < 4 * se + 1e-30), (a.mean(0), b.mean(0), se)
+
+
+def _slope_cfg(sigma, name="replay_small.npz"):
+    import dataclasses
+
+    cfg = config_from_fixture(load(name))
+    return dataclasses.replace(cfg, sea_surface=dataclasses.replace(cfg.sea_surface, slope_sigma=sigma))
+
+
+def test_philox_slopes_match_oracle_photon_by_photon(gpu_available):
+    """Gaussian surface slopes (extension): same facet draws on both sides, so records match
+    the oracle photon by photon and the waveform within the parity tolerance."""
+    cfg = _slope_cfg(0.1)
+    nf, nb, seed = 4000, 1000, 77
+    fexit, maps, wf = _philox_run(cfg, nf, nb, seed)
+    orc = oracle_run(build_scene(cfg), nf, nb, seed=seed)
+    for c in range(4):
+        pos, dr, e, t, fwi, sfi, pid = maps[c]
+        om = orc["maps"][c]
+        assert len(e) == len(om["energy"]), c
+        ia = np.lexsort((t, pid))
+        ib = np.lexsort((om["time"], om["photon"]))
+        np.testing.assert_array_equal(pid[ia], om["photon"][ib])
+        np.testing.assert_array_equal(t[ia], om["time"][ib])
+        np.testing.assert_allclose(pos[ia], om["pos"][ib], rtol=1e-5, atol=1e-5)
+    for c in range(4):
+        den = np.abs(orc["waveform"][c]).sum()
+        if den:
+            assert np.abs(wf[c] - orc["waveform"][c]).sum() / den < REL_WAVEFORM_L1, c
+
+
+def test_fast_and_precise_agree_in_distribution_slopes(gpu_available):
+    cfg = _slope_cfg(0.1, "stats_small.npz")
+    nf, nb = 60000, 15000
+    tot = {}
+    for precise in (True, False):
+        tot[precise] = np.stack(
+            [_philox_run(cfg, nf, nb, 1300 + r, ids=False, precise=precise)[2].sum(1) / (nf * nb) for r in range(8)]
+        )
+    a, b = tot[True], tot[False]
+    se = np.sqrt(a.var(0, ddof=1) / 8 + b.var(0, ddof=1) / 8)
+    assert np.all(np.abs(a.mean(0) - b.mean(0)) < 4 * se + 1e-30), (a.mean(0), b.mean(0), se)
+
+
+def test_slopes_refuse_replay(gpu_available):
+    d = load("replay_small.npz")
+    cfg = _slope_cfg(0.1)
+    eng = _engine(cfg)
+    try:
+        with pytest.raises(ValueError):
+            eng.forward(int(d["n_fwd"]), 0, replay=replay_streams(d, "fwd"))
+    finally:
+        eng.close()
