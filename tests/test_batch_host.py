@@ -69,3 +69,15 @@ def test_oracle_gated_window_is_a_slice_of_the_timeline():
     assert g.shape == (4, sc.n_bins)
     np.testing.assert_allclose(g, full[:, sc.gate_start:sc.gate_start + sc.n_bins], rtol=1e-12, atol=0)
     assert g.sum() > 0
+
+
+def test_inversion_targets_follow_the_sweep_ranges():
+    pytest.importorskip("scipy")
+    from pyalbsim_gb300 import inversion
+
+    t = inversion.hypercube_targets(32, seed=4)
+    assert t.shape == (32, 6)
+    assert np.all((t[:, 0] >= 1) & (t[:, 0] <= 40)) and np.all((t[:, 3] >= 0.8) & (t[:, 3] <= 0.95))
+    assert np.all((t[:, 5] ** 2 >= 0.01) & (t[:, 5] ** 2 <= 0.30))
+    sc = build_scene(inversion.gated_base())
+    assert sc.n_bins == round(400e-9 * sc.sample_rate)

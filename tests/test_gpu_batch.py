@@ -81,3 +81,15 @@ def test_batch_reports_a_failed_instance_and_runs_the_rest(gpu_available):
                             [x.seed for x in inst], streams=2)
     assert st[1] != 0 and all(st[i] == 0 for i in (0, 2, 3))
     assert not w[1].any() and all(w[i].sum() > 0 for i in (0, 2, 3))
+
+
+def test_inversion_decreases_the_loss(gpu_available):
+    """Adam over the six parameters, every iteration one batch (adjoint + depth pair per
+    target): the fixed-key log loss falls."""
+    pytest.importorskip("scipy")
+    from pyalbsim_gb300 import inversion
+
+    targets = inversion.hypercube_targets(2, seed=4)
+    r = inversion.fit(targets, iters=25, lr=2e-2, photons=20000, streams=2)
+    h = r["loss_history"]
+    assert np.all(np.isfinite(h)) and h[-1] < 0.9 * h[0], h
