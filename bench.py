@@ -233,7 +233,7 @@ def main():
         "phases_ms_per_step": {p: v[0] / args.steps for p, v in phases.items()},
         "gathers_per_step": int(n_gathers / args.steps),
         "dominant_phase": top,
-        "roofline": {"bound": "hbm", "kernel": "k_gather<1> (scatter map)", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "k_gather<1, 0> (scatter map, k-NN)", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak if peak else None,
                      "traffic": DRAM_BYTES_PER_SCATTER_QUERY * q_per_launch,
                      "algorithmic_bytes_per_launch": ALG_BYTES_PER_GATHER * q_per_launch,

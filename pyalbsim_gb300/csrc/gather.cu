@@ -798,7 +798,12 @@ ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, 
     }
 }
 
-template <int CHANNEL>
+// MODE: kModeKnn (the reference's estimator, the hot path), kModeKnnAdjoint (k-NN with the
+// Jacobian), kModeRadius (fixed radius, Jacobian when acc.jac_lo is set). Separate
+// instantiations keep the extensions' code out of the k-NN kernel's instruction stream.
+constexpr int kModeKnn = 0, kModeKnnAdjoint = 1, kModeRadius = 2;
+
+template <int CHANNEL, int MODE>
 __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
     __shared__ WarpSmem smem[kGatherWarps];
@@ -822,7 +827,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             uint64_t src = q.perm ? q.perm[qi] : qi;
             float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
             double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
-            if (sc.radius > 0.0) {
+            if (MODE == kModeRadius) {
                 // extension: every record within the fixed radius contributes at once
                 KnnResult r;
                 const float Es = qa.w, ts = qb.w;
@@ -900,7 +905,8 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             if (CHANNEL == ALB_SURFACE_TRANSMISSION_UP) wconst = (float)(sc.surface_albedo / kPi);
             // WaterModel.scatter_energy picks the layer of the query depth (water.py:418-447)
             const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
-            const float4 sq = q.s ? q.s[src] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 sq = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (MODE == kModeKnnAdjoint && q.s) sq = q.s[src];
             for (int j = l; j < k; j += 32) {
                 const uint32_t idx = s.ci[j];
                 const float4 pb = m.b[idx];
@@ -912,7 +918,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 const int bin = (int)((ts + pb.w) / (float)sc.mult) - (int)sc.gate_lo;
                 if (bin >= 0 && bin < acc.nbins) {
                     bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-                    if (acc.jac_lo) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
+                    if (MODE == kModeKnnAdjoint) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
                 } else if (!sc.gated) {
                     atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }
@@ -996,29 +1002,34 @@ static unsigned gather_blocks(uint64_t nq) {
     return (unsigned)(want < cap ? (want ? want : 1) : cap);
 }
 
+template <int MODE>
+static void launch_gather_mode(const MapDev& map, const QueryDev& q, int channel, const SceneDev& sc, const Accum& acc,
+                               int* err, unsigned blocks, int k, cudaStream_t st) {
+    switch (channel) {
+        case ALB_BOTTOM_REFLECTION:
+            k_gather<ALB_BOTTOM_REFLECTION, MODE><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            break;
+        case ALB_SCATTER:
+            k_gather<ALB_SCATTER, MODE><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            break;
+        case ALB_SURFACE_REFLECTION:
+            k_gather<ALB_SURFACE_REFLECTION, MODE><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            break;
+        default:
+            k_gather<ALB_SURFACE_TRANSMISSION_UP, MODE><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
+            break;
+    }
+    note_launch();
+}
+
 void launch_gather(const SceneDev& sc, const MapDev& map, const QueryDev& q, int channel, const Accum& acc,
                    int* err, int* launches, cudaStream_t st) {
     if (q.n == 0) return;
     unsigned blocks = gather_blocks(q.n);
     int k = sc.k;
-    switch (channel) {
-        case ALB_BOTTOM_REFLECTION:
-            k_gather<ALB_BOTTOM_REFLECTION><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
-            note_launch();
-            break;
-        case ALB_SCATTER:
-            k_gather<ALB_SCATTER><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
-            note_launch();
-            break;
-        case ALB_SURFACE_REFLECTION:
-            k_gather<ALB_SURFACE_REFLECTION><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
-            note_launch();
-            break;
-        default:
-            k_gather<ALB_SURFACE_TRANSMISSION_UP><<<blocks, kGatherWarps * 32, 0, st>>>(sc, map, q, acc, k, err);
-            note_launch();
-            break;
-    }
+    if (sc.radius > 0.0) launch_gather_mode<kModeRadius>(map, q, channel, sc, acc, err, blocks, k, st);
+    else if (acc.jac_lo) launch_gather_mode<kModeKnnAdjoint>(map, q, channel, sc, acc, err, blocks, k, st);
+    else launch_gather_mode<kModeKnn>(map, q, channel, sc, acc, err, blocks, k, st);
     if (launches) ++*launches;
 }
 
