@@ -798,9 +798,11 @@ ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, 
     }
 }
 
-// MODE: kModeKnn (the reference's estimator, the hot path), kModeKnnAdjoint (k-NN with the
-// Jacobian), kModeRadius (fixed radius, Jacobian when acc.jac_lo is set). Separate
-// instantiations keep the extensions' code out of the k-NN kernel's instruction stream.
+// MODE: kModeKnn (the reference's estimator without heatmaps, the hot path),
+// kModeKnnAdjoint (k-NN with the Jacobian and/or the sampled heatmaps), kModeRadius (fixed
+// radius; Jacobian and heatmaps when their accumulators are set). Separate instantiations
+// keep code the hot path never runs out of its instruction stream: the kernel is bound by
+// instruction issue and fetch.
 constexpr int kModeKnn = 0, kModeKnnAdjoint = 1, kModeRadius = 2;
 
 template <int CHANNEL, int MODE>
@@ -918,12 +920,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 const int bin = (int)((ts + pb.w) / (float)sc.mult) - (int)sc.gate_lo;
                 if (bin >= 0 && bin < acc.nbins) {
                     bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
-                    if (MODE == kModeKnnAdjoint) jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
+                    if (MODE == kModeKnnAdjoint && acc.jac_lo)
+                        jac_add<CHANNEL>(sc, m, acc, layer, bin, idx, c, sq, pb, vx, vy, vz);
                 } else if (!sc.gated) {
                     atomicCAS(err, 0, ALB_ERR_CAPACITY);
                 }
             }
-            if (acc.hw_lo && m.fwi) {
+            if (MODE != kModeKnn && acc.hw_lo && m.fwi) {
                 // accumulate_to_heatmap, alb_sim/math/accumulate_heatmap.py:6-61 (a separate,
                 // non-unrolled pass: heatmaps are off in production runs)
 #pragma unroll 1
@@ -1028,7 +1031,8 @@ void launch_gather(const SceneDev& sc, const MapDev& map, const QueryDev& q, int
     unsigned blocks = gather_blocks(q.n);
     int k = sc.k;
     if (sc.radius > 0.0) launch_gather_mode<kModeRadius>(map, q, channel, sc, acc, err, blocks, k, st);
-    else if (acc.jac_lo) launch_gather_mode<kModeKnnAdjoint>(map, q, channel, sc, acc, err, blocks, k, st);
+    else if (acc.jac_lo || (acc.hw_lo && map.fwi))
+        launch_gather_mode<kModeKnnAdjoint>(map, q, channel, sc, acc, err, blocks, k, st);
     else launch_gather_mode<kModeKnn>(map, q, channel, sc, acc, err, blocks, k, st);
     if (launches) ++*launches;
 }
