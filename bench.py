@@ -32,8 +32,8 @@ METRIC = "photons/s & waveform-grads/s on 1 GB300: batched+adjoint vs plain @≤
 UNIT = "photons/s"
 ALG_BYTES_PER_GATHER = 16 + 100 * 32  # query record + k neighbour records (pos 12, dir 12, E 4, t 4)
 # DRAM bytes per scatter-map query measured by ncu on the same kernel (dram__bytes_read.sum +
-# dram__bytes_write.sum of one k_gather<1> launch / its queries; 1e6-photon case of this scene)
-DRAM_BYTES_PER_SCATTER_QUERY = 846
+# dram__bytes_write.sum of one k_gather<1, 0> launch / its queries; 1e6-photon case of this scene)
+DRAM_BYTES_PER_SCATTER_QUERY = 849
 
 
 def workload_config(name: str):
@@ -215,7 +215,7 @@ def main():
     ms_step = ms / args.steps
     value = world * (nf + nb) / (ms_step / 1e3)
 
-    # roofline of the dominant kernel, the scatter-map gather k_gather<1>: HBM-bound by the
+    # roofline of the dominant kernel, the scatter-map gather k_gather<1, 0>: HBM-bound by the
     # algorithmic convention (3216 B per query), timed with CUDA events around its launches
     n_gathers = int(gathers.sum())
     sc_ms, sc_calls = phases["gather_scatter"]
