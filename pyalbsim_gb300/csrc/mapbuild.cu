@@ -596,6 +596,7 @@ ALB_DEVICE unsigned agg_inc(unsigned* cnt, uint64_t key, unsigned active) {
 // that find no slot go to global memory directly.
 constexpr int kLvlThreads = 256;
 constexpr int kSlots = 8;
+constexpr int kHistItems = 4;
 constexpr unsigned kNoTag = 0xffffffffu;
 
 // claim the slot of `key` (path or child id); returns the slot or -1
@@ -621,33 +622,60 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
     if (threadIdx.x < kSlots) tag[threadIdx.x] = kNoTag;
     __syncthreads();
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
-    for (uint64_t base = r0 + (threadIdx.x & ~31u); base < r1; base += blockDim.x) {
-        const uint64_t i = base + lane_id();
-        bool act = false;
-        uint32_t path = 0, h = 0;
-        if (i < r1) {
-            uint64_t a, c;
-            int r;
-            kd_node_path(i / 32, L, d, a, c, path, r);
-            if (r == d && c > 1) {
-                const uint32_t q = kd_quant16(X[i], nb, path);
-                if (PASS == 1) {
-                    act = true;
-                    h = q >> 8;
-                } else if ((q >> 8) == sel[path].x) {
-                    act = true;
-                    h = q & 255u;
+    // kHistItems records per thread and iteration, all loads issued before any is used:
+    // the pass streams the records once, so loads in flight set its speed
+    const uint64_t stride = (uint64_t)blockDim.x * kHistItems;
+    for (uint64_t base0 = r0 + (threadIdx.x & ~31u); base0 < r1; base0 += stride) {
+        float4 pv[kHistItems];
+#pragma unroll
+        for (int t = 0; t < kHistItems; ++t) {
+            const uint64_t i = base0 + (uint64_t)t * blockDim.x + lane_id();
+            if (i < r1) pv[t] = X[i];
+        }
+#pragma unroll
+        for (int t = 0; t < kHistItems; ++t) {
+            const uint64_t base = base0 + (uint64_t)t * blockDim.x;
+            const uint64_t i = base + lane_id();
+            bool act = false;
+            uint32_t path = 0, h = 0;
+            if (i < r1) {
+                uint64_t a, c;
+                int r;
+                kd_node_path(i / 32, L, d, a, c, path, r);
+                if (r == d && c > 1) {
+                    const uint32_t q = kd_quant16(pv[t], nb, path);
+                    if (PASS == 1) {
+                        act = true;
+                        h = q >> 8;
+                    } else if ((q >> 8) == sel[path].x) {
+                        act = true;
+                        h = q & 255u;
+                    }
                 }
             }
-        }
-        const unsigned am = __ballot_sync(0xffffffffu, act);
-        if (act) {
-            const unsigned key = (path << 8) | h;
-            const unsigned peers = __match_any_sync(am, key);
-            if ((int)lane_id() == __ffs(peers) - 1) {
-                const int sl = slot_of(tag, path);
-                if (sl >= 0) atomicAdd(&sh[sl * 256 + h], (unsigned)__popc(peers));
-                else atomicAdd(hist + (uint64_t)path * 256 + h, (unsigned)__popc(peers));
+            const unsigned am = __ballot_sync(0xffffffffu, act);
+            if (am) {
+                // a warp covers one 32-record leaf, so its records share one node: one slot
+                // lookup per warp, then plain shared-memory atomics per record
+                const int lead = __ffs(am) - 1;
+                const uint32_t p0 = __shfl_sync(0xffffffffu, path, lead);
+                if (__all_sync(0xffffffffu, !act || path == p0)) {
+                    int sl = 0;
+                    if ((int)lane_id() == lead) sl = slot_of(tag, p0);
+                    sl = __shfl_sync(0xffffffffu, sl, lead);
+                    if (act) {
+                        if (sl >= 0) atomicAdd(&sh[sl * 256 + h], 1u);
+                        else atomicAdd(hist + (uint64_t)path * 256 + h, 1u);
+                    }
+                } else if (act) {
+                    const unsigned key = (path << 8) | h;
+                    const unsigned peers = __match_any_sync(am, key);
+                    if ((int)lane_id() == __ffs(peers) - 1) {
+                        const int sl = slot_of(tag, path);
+                        if (sl >= 0) atomicAdd(&sh[sl * 256 + h], (unsigned)__popc(peers));
+                        else atomicAdd(hist + (uint64_t)path * 256 + h, (unsigned)__popc(peers));
+                    }
+                }
             }
         }
     }
@@ -779,6 +807,11 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
         uint32_t path[kSplitItems], rank[kSplitItems];
         int code[kSplitItems];       // slot * 2 + side while the tile reservation is pending, else -1
 #pragma unroll
+        for (int t = 0; t < kSplitItems; ++t) {  // every load in flight before the first use
+            const uint64_t i = t0 + (uint64_t)t * blockDim.x + threadIdx.x;
+            if (i < r1) p[t] = X[i];
+        }
+#pragma unroll
         for (int t = 0; t < kSplitItems; ++t) {
             const uint64_t i = t0 + (uint64_t)t * blockDim.x + threadIdx.x;
             code[t] = -1;
@@ -792,7 +825,6 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             if (i < r1) {
                 int r;
                 kd_node_path(i / 32, L, d, a, c, path[t], r);
-                p[t] = X[i];
                 if (r == d && c > 1) {
                     moves = true;
                     left = 1ull << (63 - __clzll((long long)(c - 1)));
@@ -809,9 +841,14 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             }
             // per-warp aggregation of (path, side) for the tile counters
             const unsigned am = __ballot_sync(0xffffffffu, moves);
+            // a warp covers one 32-record leaf, so its moving records share one node and the
+            // peers of a record are the lanes on its side (match only as a fallback)
+            const unsigned right = __ballot_sync(0xffffffffu, moves && side);
+            const uint32_t p0 = __shfl_sync(0xffffffffu, path[t], am ? __ffs(am) - 1 : 0);
+            const bool one_node = __all_sync(0xffffffffu, !moves || path[t] == p0);
             if (moves) {
                 const unsigned key = (path[t] << 1) | side;
-                const unsigned peers = __match_any_sync(am, key);
+                const unsigned peers = one_node ? (side ? right : (am & ~right)) : __match_any_sync(am, key);
                 const int leader = __ffs(peers) - 1;
                 const unsigned lrank = __popc(peers & lanemask_lt());
                 unsigned b = 0;
@@ -835,8 +872,8 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     else atomicOr(err, 1u);
                 }
                 // child box: shared slots per child id, global otherwise
-                const unsigned child = (path[t] << 1) | side;
-                const unsigned cpeers = __match_any_sync(am, child);
+                const unsigned child = key;
+                const unsigned cpeers = peers;
                 const unsigned ox = f2ord(p[t].x), oy = f2ord(p[t].y), oz = f2ord(p[t].z);
                 const unsigned mnx = __reduce_min_sync(cpeers, ox), mny = __reduce_min_sync(cpeers, oy),
                                mnz = __reduce_min_sync(cpeers, oz);
