@@ -7,7 +7,8 @@ log-uniform over a range (uneven work). ``run_batch`` runs every instance throug
 ``alb_batch_run``: host workers, each owning a device context on its own CUDA stream, take
 instances from one queue, largest first, so that small instances overlap on the GPU.
 ``tune_streams`` is the autotuner. It times the batch on a pilot subset for each candidate
-worker count and keeps the fastest.
+worker count and keeps the fastest. ``run_hypercube`` is the reference's own sweep (seven
+config fields, ``run_config`` photon counts) as one batched call.
 """
 
 from __future__ import annotations
@@ -120,3 +121,79 @@ def tune_streams(
         rates[k] = photons / wall
     best = max(rates, key=rates.get)
     return best, rates
+
+
+# The reference's own sweep (its hypercube notebook) varies seven SimulationConfig fields;
+# these names select them (plus "asymmetry", the HG extension).
+SWEEP_FIELDS = ("height", "absorption", "scattering", "floor_albedo", "surface_roughness",
+                "field_of_view", "aperture_radius", "asymmetry")
+
+
+def config_from_sample(params: Dict[str, float], base=None):
+    """A SimulationConfig with the sampled fields set on ``base`` (default: the defaults of
+    SimulationConfig) and one water layer; unknown names raise ValueError."""
+    from pyalbsim_gb300.config import SimulationConfig, TurbidityLayerConfig, WaterConfig
+
+    unknown = set(params) - set(SWEEP_FIELDS)
+    if unknown:
+        raise ValueError(f"unknown sweep fields: {sorted(unknown)}")
+    cfg = base if base is not None else SimulationConfig()
+    layer = cfg.water.layers[0] if base is not None else TurbidityLayerConfig()
+    lk = {}
+    if "height" in params:
+        lk["height"] = float(params["height"])
+    if "absorption" in params:
+        lk["absorption_coefficient"] = float(params["absorption"])
+    if "scattering" in params:
+        lk["scattering_coefficient"] = float(params["scattering"])
+    if "asymmetry" in params:
+        lk["henyey_greenstein_g"] = float(params["asymmetry"])
+    sk = {}
+    if "field_of_view" in params:
+        sk["field_of_view"] = float(params["field_of_view"])
+    if "aperture_radius" in params:
+        sk["aperture_radius"] = float(params["aperture_radius"])
+    cfg = dataclasses.replace(
+        cfg,
+        water=WaterConfig(layers=(dataclasses.replace(layer, **lk),)),
+        sensor=dataclasses.replace(cfg.sensor, **sk),
+    )
+    if "floor_albedo" in params:
+        cfg = dataclasses.replace(cfg, sea_floor=dataclasses.replace(cfg.sea_floor, albedo=float(params["floor_albedo"])))
+    if "surface_roughness" in params:
+        cfg = dataclasses.replace(
+            cfg, sea_surface=dataclasses.replace(cfg.sea_surface, roughness=float(params["surface_roughness"])))
+    return cfg
+
+
+def run_hypercube(param_ranges: Dict[str, Tuple[float, float]], n_samples: int, run_config, seed: Optional[int] = None,
+                  base=None, streams: int = 8, device: int = 0) -> List[Dict]:
+    """The hypercube sweep in one batched call: n_samples LatinHypercube(d) points scaled to
+    ``param_ranges``, each simulated with the run_config's photon counts (forward batches x
+    photons per batch, backward likewise) through alb_batch_run. Returns
+    [{"params": dict, "waveform": {PhotonType: float32 array}}, ...] in sample order.
+    With ``seed`` the samples and every instance's Philox key are reproducible."""
+    import secrets
+
+    from scipy.stats import qmc
+
+    from pyalbsim_gb300.photon_mapping.photon_type import PhotonType
+
+    names = list(param_ranges)
+    lo = [param_ranges[k][0] for k in names]
+    hi = [param_ranges[k][1] for k in names]
+    pts = qmc.scale(qmc.LatinHypercube(d=len(names), seed=seed).random(n=n_samples), lo, hi)
+    samples = [dict(zip(names, map(float, row))) for row in pts]
+    nf = run_config.batches_forward * run_config.photons_per_batch_forward
+    nb = run_config.batches_backward * run_config.photons_per_batch_backward
+    inst = []
+    for i, p in enumerate(samples):
+        key = ((int(seed) & 0xFFFFFFFF) << 32) + i if seed is not None else secrets.randbits(64)
+        inst.append(Instance(config_from_sample(p, base), nf, nb, key, np.array(list(p.values()))))
+    w, _, st, _, _ = run_batch(inst, streams=streams, device=device)
+    out = []
+    for i, p in enumerate(samples):
+        if st[i] != 0:
+            raise RuntimeError(f"sample {i} ({p}) failed with status {int(st[i])}")
+        out.append({"params": p, "waveform": {t: w[i][c].astype(np.float32) for c, t in enumerate(PhotonType)}})
+    return out

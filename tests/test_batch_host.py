@@ -81,3 +81,13 @@ def test_inversion_targets_follow_the_sweep_ranges():
     assert np.all((t[:, 5] ** 2 >= 0.01) & (t[:, 5] ** 2 <= 0.30))
     sc = build_scene(inversion.gated_base())
     assert sc.n_bins == round(400e-9 * sc.sample_rate)
+
+
+def test_config_from_sample_sets_the_sweep_fields():
+    p = {"height": 3.0, "absorption": 0.02, "scattering": 2.0, "floor_albedo": 0.1,
+         "surface_roughness": 0.05, "field_of_view": 0.01, "aperture_radius": 0.05}
+    sc = build_scene(batch.config_from_sample(p))
+    assert (sc.depth, sc.fov, sc.aperture_radius, sc.seafloor_albedo, sc.roughness) == (3.0, 0.01, 0.05, 0.1, 0.05)
+    assert sc.layers[0].absorption == 0.02
+    with pytest.raises(ValueError):
+        batch.config_from_sample({"depth": 3.0})

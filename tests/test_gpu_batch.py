@@ -93,3 +93,27 @@ def test_inversion_decreases_the_loss(gpu_available):
     r = inversion.fit(targets, iters=25, lr=2e-2, photons=20000, streams=2)
     h = r["loss_history"]
     assert np.all(np.isfinite(h)) and h[-1] < 0.9 * h[0], h
+
+
+def test_run_hypercube_matches_single_instance_runs(gpu_available):
+    """The reference's sweep as one batched call: every sample equals its own run."""
+    pytest.importorskip("scipy")
+    from pyalbsim_gb300.config import RunConfig
+    from pyalbsim_gb300.config import HeatmapConfig
+
+    ranges = {"height": (0.5, 7.5), "absorption": (0.005, 0.05), "scattering": (1.0, 5.0),
+              "floor_albedo": (0.05, 0.3), "surface_roughness": (0.01, 0.1),
+              "field_of_view": (5e-3, 40e-3), "aperture_radius": (0.001, 0.2)}
+    rc = RunConfig(photons_per_batch_forward=3000, photons_per_batch_backward=1000, batches_forward=2,
+                   batches_backward=2)
+    base = batch.config_from_sample({}, base=None)
+    base = dataclasses.replace(base, heatmap=HeatmapConfig(enabled=False))
+    res = batch.run_hypercube(ranges, 4, rc, seed=11, base=base, streams=2)
+    assert len(res) == 4
+    for i, r in enumerate(res):
+        cfg = batch.config_from_sample(r["params"], base)
+        key = (11 << 32) + i
+        w, _ = _single(cfg, 6000, 2000, key)
+        got = np.stack([r["waveform"][t] for t in r["waveform"]])
+        np.testing.assert_array_equal(got, w.astype(np.float32))
+        assert got.sum() > 0
