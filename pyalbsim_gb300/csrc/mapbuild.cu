@@ -783,18 +783,10 @@ constexpr int kSplitItems = 4;
 __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
                                                            uint64_t n, uint64_t L, int d, LevelNodes nb,
                                                            const uint2* __restrict__ cut, unsigned* cursors,
-                                                           unsigned* ties, unsigned* clo, unsigned* chi,
-                                                           unsigned* err, uint64_t per) {
+                                                           unsigned* ties, unsigned* err, uint64_t per) {
     __shared__ unsigned ntag[kSlots];           // node slots of the current tile
     __shared__ unsigned ncnt[kSlots * 2];       // records per (slot, side) in the tile
     __shared__ unsigned nbase[kSlots * 2];      // their global start (cursor reservation)
-    __shared__ unsigned btag[kSlots];           // child slots (whole block range)
-    __shared__ unsigned bmin[kSlots * 3], bmax[kSlots * 3];
-    if (threadIdx.x < kSlots) btag[threadIdx.x] = kNoTag;
-    for (int j = threadIdx.x; j < kSlots * 3; j += blockDim.x) {
-        bmin[j] = 0xffffffffu;
-        bmax[j] = 0u;
-    }
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     const uint64_t tile = (uint64_t)kSplitItems * blockDim.x;
     for (uint64_t t0 = r0; t0 < r1; t0 += tile) {
@@ -871,21 +863,6 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     if (dst < dend[t]) X2[dst] = p[t];
                     else atomicOr(err, 1u);
                 }
-                // child box: shared slots per child id, global otherwise
-                const unsigned child = key;
-                const unsigned cpeers = peers;
-                const unsigned ox = f2ord(p[t].x), oy = f2ord(p[t].y), oz = f2ord(p[t].z);
-                const unsigned mnx = __reduce_min_sync(cpeers, ox), mny = __reduce_min_sync(cpeers, oy),
-                               mnz = __reduce_min_sync(cpeers, oz);
-                const unsigned mxx = __reduce_max_sync(cpeers, ox), mxy = __reduce_max_sync(cpeers, oy),
-                               mxz = __reduce_max_sync(cpeers, oz);
-                if ((int)lane_id() == __ffs(cpeers) - 1) {
-                    const int bs = slot_of(btag, child);
-                    unsigned* lo = bs >= 0 ? bmin + 3 * bs : clo + 3 * (uint64_t)child;
-                    unsigned* hi = bs >= 0 ? bmax + 3 * bs : chi + 3 * (uint64_t)child;
-                    atomicMin(lo, mnx); atomicMin(lo + 1, mny); atomicMin(lo + 2, mnz);
-                    atomicMax(hi, mxx); atomicMax(hi + 1, mxy); atomicMax(hi + 2, mxz);
-                }
             }
         }
         __syncthreads();
@@ -905,16 +882,41 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
         }
         __syncthreads();
     }
-    // flush the children's boxes
-    if (threadIdx.x < kSlots) {
-        const unsigned ch = btag[threadIdx.x];
-        if (ch != kNoTag) {
-            const int j = threadIdx.x;
-            atomicMin(clo + 3 * (uint64_t)ch, bmin[3 * j]); atomicMin(clo + 3 * (uint64_t)ch + 1, bmin[3 * j + 1]);
-            atomicMin(clo + 3 * (uint64_t)ch + 2, bmin[3 * j + 2]);
-            atomicMax(chi + 3 * (uint64_t)ch, bmax[3 * j]); atomicMax(chi + 3 * (uint64_t)ch + 1, bmax[3 * j + 1]);
-            atomicMax(chi + 3 * (uint64_t)ch + 2, bmax[3 * j + 2]);
-        }
+}
+
+// Children's boxes of a level: the parent's box cut on its split axis at the cut value,
+// left [lo, lo + (cut + 1) / scale], right [lo + cut / scale, hi] (they overlap by one
+// quantisation step). Only the next level's axis and quantisation come from these boxes;
+// any box that holds the records gives the same exact median split, and the gather's box
+// tree is built from the final leaves.
+__global__ void k_kdl_child_boxes(const unsigned* __restrict__ lo, const unsigned* __restrict__ hi,
+                                  const float4* __restrict__ par, const uint2* __restrict__ cut, uint32_t nodes,
+                                  unsigned* clo, unsigned* chi) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    unsigned l[3], h[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        l[k] = lo[3 * i + k];
+        h[k] = hi[3 * i + k];
+    }
+    unsigned ll[3] = {l[0], l[1], l[2]}, lh[3] = {h[0], h[1], h[2]};
+    unsigned rl[3] = {l[0], l[1], l[2]}, rh[3] = {h[0], h[1], h[2]};
+    const float4 np = par[i];
+    const int axis = __float_as_int(np.x);
+    if (axis >= 0 && axis < 3 && np.z > 0.f) {
+        const float q = (float)cut[i].x;
+        const unsigned split_hi = f2ord(np.y + (q + 1.f) / np.z);
+        const unsigned split_lo = f2ord(np.y + q / np.z);
+        lh[axis] = min(h[axis], max(l[axis], split_hi));
+        rl[axis] = max(l[axis], min(h[axis], split_lo));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        clo[3 * (2 * (uint64_t)i) + k] = ll[k];
+        chi[3 * (2 * (uint64_t)i) + k] = lh[k];
+        clo[3 * (2 * (uint64_t)i + 1) + k] = rl[k];
+        chi[3 * (2 * (uint64_t)i + 1) + k] = rh[k];
     }
 }
 
@@ -1198,7 +1200,9 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
             note_launch();
             k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
             note_launch();
-            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, clo, chi, err, per);
+            k_kdl_child_boxes<<<(nodes + 255) / 256, 256, 0, st>>>(lo, hi, par, cut, nodes, clo, chi);
+            note_launch();
+            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, err, per);
             note_launch();
             std::swap(X, X2);
             std::swap(lo, clo);
