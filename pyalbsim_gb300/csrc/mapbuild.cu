@@ -783,10 +783,19 @@ constexpr int kSplitItems = 4;
 __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
                                                            uint64_t n, uint64_t L, int d, LevelNodes nb,
                                                            const uint2* __restrict__ cut, unsigned* cursors,
-                                                           unsigned* ties, unsigned* err, uint64_t per) {
+                                                           unsigned* ties, unsigned* err, uint64_t per,
+                                                           LevelNodes nbn, unsigned* hist_next) {
     __shared__ unsigned ntag[kSlots];           // node slots of the current tile
     __shared__ unsigned ncnt[kSlots * 2];       // records per (slot, side) in the tile
     __shared__ unsigned nbase[kSlots * 2];      // their global start (cursor reservation)
+    // next level's first histogram (top byte of the child's 16-bit coordinate), fused into
+    // this pass: child slots for the block's whole range, global counters otherwise
+    __shared__ unsigned htag[kSlots];
+    __shared__ unsigned hsh[kSlots * 256];
+    if (hist_next) {
+        for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) hsh[j] = 0u;
+        if (threadIdx.x < kSlots) htag[threadIdx.x] = kNoTag;
+    }
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     const uint64_t tile = (uint64_t)kSplitItems * blockDim.x;
     for (uint64_t t0 = r0; t0 < r1; t0 += tile) {
@@ -811,8 +820,8 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             dend[t] = 0;
             path[t] = 0;
             rank[t] = 0;
-            bool moves = false;
-            unsigned side = 0;
+            bool moves = false, counts_next = false;
+            unsigned side = 0, hbin = 0;
             uint64_t a = 0, c = 0, left = 0;
             if (i < r1) {
                 int r;
@@ -827,6 +836,11 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     else side = (atomicAdd(ties + path[t], 1u) < ct.y) ? 0u : 1u;
                     dst0[t] = a * 32 + (side ? left * 32 : 0);
                     dend[t] = side ? min((a + c) * 32, n) : (a + left) * 32;
+                    // the child node is split again at the next level if it has > 1 leaf
+                    if (hist_next && (side ? c - left : left) > 1) {
+                        counts_next = true;
+                        hbin = kd_quant16(p[t], nbn, (path[t] << 1) | side) >> 8;
+                    }
                 } else {
                     X2[i] = p[t];  // already in place (a leaf of an earlier level)
                 }
@@ -864,6 +878,12 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     else atomicOr(err, 1u);
                 }
             }
+            if (counts_next) {
+                const unsigned child = (path[t] << 1) | side;
+                const int hs = slot_of(htag, child);
+                if (hs >= 0) atomicAdd(&hsh[hs * 256 + hbin], 1u);
+                else atomicAdd(hist_next + (uint64_t)child * 256 + hbin, 1u);
+            }
         }
         __syncthreads();
         if (threadIdx.x < kSlots * 2) {
@@ -881,6 +901,12 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             }
         }
         __syncthreads();
+    }
+    if (hist_next) {
+        for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) {
+            const unsigned tg = htag[j >> 8];
+            if (tg != kNoTag && hsh[j]) atomicAdd(hist_next + (uint64_t)tg * 256 + (j & 255), hsh[j]);
+        }
     }
 }
 
@@ -1157,7 +1183,10 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         unsigned* clo = ws.take_u32(maxnodes * 6);  // children boxes
         unsigned* chi = ws.take_u32(maxnodes * 6);
         float4* par = (float4*)ws.take_bytes(maxnodes * 16);
-        if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi || !par) {
+        float4* cpar = (float4*)ws.take_bytes(maxnodes * 16);  // children's parameters
+        unsigned* hist1n = ws.take_u32(maxnodes * 256);       // children's first histogram
+        if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi || !par || !cpar ||
+            !hist1n) {
             ws.release(mark);
             return -1;
         }
@@ -1181,32 +1210,41 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         uint64_t per = (n + lvl_blocks - 1) / lvl_blocks;
         per = (per + 1023) & ~1023ull;
         const unsigned lb = (unsigned)((n + per - 1) / per);
+        // level 0: its parameters and first histogram; every later level gets both from
+        // the previous level (children's boxes, and the histogram fused into the split pass)
+        k_kdl_params<<<1, 256, 0, st>>>(lo, hi, 1u, par);
+        note_launch();
+        cudaMemsetAsync(hist1, 0, 256 * 4, st);
+        k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, n, L, 0, LevelNodes{par}, nullptr, hist1, per);
+        note_launch();
         for (int d = 0; d < D; ++d) {
             const uint32_t nodes = 1u << d;
-            cudaMemsetAsync(hist1, 0, (size_t)nodes * 256 * 4, st);
+            const bool more = d + 1 < D;
             cudaMemsetAsync(hist2, 0, (size_t)nodes * 256 * 4, st);
             cudaMemsetAsync(cursors, 0, (size_t)nodes * 8, st);
             cudaMemsetAsync(ties, 0, (size_t)nodes * 4, st);
-            cudaMemsetAsync(clo, 0xff, (size_t)nodes * 2 * 12, st);
-            cudaMemsetAsync(chi, 0x00, (size_t)nodes * 2 * 12, st);
-            k_kdl_params<<<(nodes + 255) / 256, 256, 0, st>>>(lo, hi, nodes, par);
-            note_launch();
             LevelNodes nb{par};
-            k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, nullptr, hist1, per);
-            note_launch();
             k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
             note_launch();
             k_kdl_hist<2><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, sel, hist2, per);
             note_launch();
             k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
             note_launch();
-            k_kdl_child_boxes<<<(nodes + 255) / 256, 256, 0, st>>>(lo, hi, par, cut, nodes, clo, chi);
-            note_launch();
-            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, err, per);
+            if (more) {
+                k_kdl_child_boxes<<<(nodes + 255) / 256, 256, 0, st>>>(lo, hi, par, cut, nodes, clo, chi);
+                note_launch();
+                k_kdl_params<<<(2 * nodes + 255) / 256, 256, 0, st>>>(clo, chi, 2 * nodes, cpar);
+                note_launch();
+                cudaMemsetAsync(hist1n, 0, (size_t)nodes * 2 * 256 * 4, st);
+            }
+            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, err, per,
+                                                     LevelNodes{cpar}, more ? hist1n : nullptr);
             note_launch();
             std::swap(X, X2);
             std::swap(lo, clo);
             std::swap(hi, chi);
+            std::swap(par, cpar);
+            std::swap(hist1, hist1n);
         }
     }
     // local levels: one CTA per remaining node
