@@ -260,6 +260,7 @@ def main():
             line["e2e"] = e2e_measure(cfg, nf, nb)
         if not args.no_gradients:
             line["gradients"] = gradients_measure(int(args.grad_photons))
+            line["gradients_batched"] = batched_gradients_measure()
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -343,6 +344,71 @@ def gradients_measure(nf: int):
                   "400 m, FOV 50 mrad, 0.05 ns bins in a 200 ns window at the surface return, k = 100, "
                   "fast tracer",
         "waveform_l1_vs_plain": float(np.abs(w.detach().numpy() - w_plain).sum() / max(np.abs(w_plain).sum(), 1e-300)),
+    }
+
+
+def batched_gradients_measure(n_targets: int = 16, photons: int = 1_000_000, streams: int = 4):
+    """Batched form: six-parameter gradients of n_targets Latin-hypercube instances (seed 4)
+    at 1e6 + 2.5e5 photons, small scene with an HG layer and a 400 ns window. One
+    alb_batch_run holds, per target, the adjoint instance and the depth pair. Baseline: the
+    plain single-instance run of every target through the engine, one after another (their
+    mean time), 13 runs per central-difference gradient."""
+    import torch
+
+    from pyalbsim_gb300.adjoint import with_parameters
+    from pyalbsim_gb300.batch import Instance, run_batch
+    from pyalbsim_gb300.config.gpu import GpuRunOptions
+    from pyalbsim_gb300.engine import GpuEngine
+    from pyalbsim_gb300.inversion import gated_base, hypercube_targets
+
+    base = gated_base()
+    nb = photons // 4
+    pts = 1.1 * hypercube_targets(n_targets, seed=4)
+    pts[:, 3] = np.minimum(pts[:, 3], 0.99)
+
+    def instances():
+        out = []
+        for i, p in enumerate(pts):
+            out.append(Instance(with_parameters(base, p), photons, nb, 3000 + i, p))
+            for s in (1.0, -1.0):
+                q = p.copy()
+                q[0] += s * max(0.01 * p[0], 0.01)
+                out.append(Instance(with_parameters(base, q), photons, nb, 3000 + i, q))
+        return out
+
+    run_batch(instances()[:6], streams=streams, adjoint=True)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, _, st, _, _ = run_batch(instances(), streams=streams, adjoint=True)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+
+    def plain(p):
+        eng = GpuEngine(with_parameters(base, p), GpuRunOptions(precise=False))
+        try:
+            eng.forward(photons, 5)
+            eng.build_maps()
+            eng.backward(nb, 5)
+            eng.waveform_array(f64=True)
+        finally:
+            eng.close()
+
+    plain(pts[0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in pts:
+        plain(p)
+    torch.cuda.synchronize()
+    t_plain = (time.perf_counter() - t0) / n_targets
+    rate = n_targets / t_batch
+    return {
+        "value": rate, "unit": "waveform-gradients/s (6 parameters)", "instances": n_targets,
+        "photons_per_run": photons + nb, "streams": streams, "failed": int((st != 0).sum()),
+        "s_per_batch": t_batch, "s_per_plain_run_mean": t_plain,
+        "fd_baseline": {"value": 1.0 / (13 * t_plain), "unit": "waveform-gradients/s", "runs_per_gradient": 13},
+        "speedup_vs_fd": rate * 13 * t_plain,
+        "config": "small scene (400 m, 0.1 ns bins), HG layer, 400 ns window, k = 100; Latin-hypercube "
+                  "parameters (seed 4) +10%; per target one adjoint instance + depth pair, fast tracer",
     }
 
 
