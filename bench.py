@@ -165,9 +165,9 @@ def main():
 
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from pyalbsim_gb300.replicas import aggregate_rate, max_over_ranks, rank_info, replica_seed
+
+    world, rank, local = rank_info()
     if world > 1:
         import torch.distributed as dist
 
@@ -179,15 +179,15 @@ def main():
     cfg = workload_config(args.workload)
     nf = int(args.photons)
     nb = max(nf // 4, 1)
-    seed = 1 + rank  # replicas: every rank traces its own photons (no data-path exchange)
+    # replicas: every rank traces its own photons (no data-path exchange)
     eng = GpuEngine(cfg, GpuRunOptions(device=local, precise=args.precise))
 
     def step(s):
         eng.ctx.reset()
         eng.n_forward = eng.n_backward = 0
-        eng.forward(nf, seed + 1000 * s)
+        eng.forward(nf, replica_seed(1, rank, s))
         eng.build_maps()
-        eng.backward(nb, seed + 1000 * s)
+        eng.backward(nb, replica_seed(1, rank, s))
 
     for w in range(args.warmup):
         step(w)
@@ -203,17 +203,13 @@ def main():
             step(args.warmup + s)
         ev1.record()
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), device="cuda")
     gstats = eng.ctx.stats()
     launches = gstats.pop("launches") - launches0
     phases, gathers = eng.ctx.phase_times(reset=True)
     wf = eng.waveform_array(f64=True)
     ms_step = ms / args.steps
-    value = world * (nf + nb) / (ms_step / 1e3)
+    value = aggregate_rate(nf + nb, world, ms_step)
 
     # roofline of the dominant kernel, the scatter-map gather k_gather<1, 0>: HBM-bound by the
     # algorithmic convention (3216 B per query), timed with CUDA events around its launches
