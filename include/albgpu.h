@@ -268,7 +268,7 @@ typedef struct AlbBatchInstance {
     uint64_t n_backward;
     uint64_t seed;
     double* waveform;             /* out, caller-owned host memory */
-    double* jacobian;             /* out (adjoint), nullable */
+    double* jacobian;             /* out (adjoint), nullable: NULL runs the instance plain */
     int32_t status;               /* out: ALB_OK or the instance's error code */
     float device_ms;              /* out: CUDA-event time of the instance on its stream */
 } AlbBatchInstance;

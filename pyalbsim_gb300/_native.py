@@ -502,10 +502,13 @@ class NativeContext:
         self._check(self.lib.alb_reset(self.h))
 
 
-def batch_run(scenes, n_forward, n_backward, seeds, streams=4, precise=False, adjoint=False, device=0):
+def batch_run(scenes, n_forward, n_backward, seeds, streams=4, precise=False, adjoint=False, device=0,
+              jacobian_mask=None):
     """alb_batch_run over SceneModels: returns (waveforms: list of float64 [4, nbins],
-    jacobians: list of float64 [5, 4, nbins] or None, statuses int32 [n], device_ms [n]).
-    Instances that failed keep a zero waveform and a non-zero status."""
+    jacobians: list of float64 [5, 4, nbins] (None for masked-out instances) or None,
+    statuses int32 [n], device_ms [n]). With adjoint, ``jacobian_mask`` (bools) selects the
+    instances that accumulate a Jacobian; the others run plain. Instances that failed keep a
+    zero waveform and a non-zero status."""
     lib = load_library()
     n = len(scenes)
     structs, keep, waves, jacs = [], [], [], []
@@ -515,7 +518,8 @@ def batch_run(scenes, n_forward, n_backward, seeds, streams=4, precise=False, ad
         structs.append(p)
         keep.append(k)
         w = np.zeros((4, sc.n_bins), np.float64)
-        j = np.zeros((5, 4, sc.n_bins), np.float64) if adjoint else None
+        want = adjoint and (jacobian_mask is None or bool(jacobian_mask[i]))
+        j = np.zeros((5, 4, sc.n_bins), np.float64) if want else None
         waves.append(w)
         jacs.append(j)
         arr[i].scene = C.pointer(p)
@@ -523,7 +527,7 @@ def batch_run(scenes, n_forward, n_backward, seeds, streams=4, precise=False, ad
         arr[i].n_backward = int(n_backward[i])
         arr[i].seed = int(seeds[i]) & 0xFFFFFFFFFFFFFFFF
         arr[i].waveform = w.ctypes.data_as(C.POINTER(C.c_double))
-        arr[i].jacobian = j.ctypes.data_as(C.POINTER(C.c_double)) if adjoint else None
+        arr[i].jacobian = j.ctypes.data_as(C.POINTER(C.c_double)) if want else None
     opt = AlbBatchOptions(device, int(streams), int(bool(precise)), int(bool(adjoint)))
     rc = lib.alb_batch_run(arr, n, C.byref(opt))
     raise_for(rc, lib.alb_last_error(None).decode())

@@ -86,14 +86,16 @@ def hypercube_instances(
 
 
 def run_batch(instances: Sequence[Instance], streams: int = 8, adjoint: bool = False, precise: bool = False,
-              device: int = 0):
+              device: int = 0, jacobian_mask: Optional[Sequence[bool]] = None):
     """Every instance through alb_batch_run. Returns (waveforms, jacobians or None,
-    statuses, per-instance device ms, wall seconds)."""
+    statuses, per-instance device ms, wall seconds). With adjoint, ``jacobian_mask`` picks
+    the instances that need a Jacobian; the rest run plain."""
     scenes = [build_scene(x.config) for x in instances]
     t0 = time.perf_counter()
     w, j, st, ms = batch_run(
         scenes, [x.n_forward for x in instances], [x.n_backward for x in instances],
         [x.seed for x in instances], streams=streams, precise=precise, adjoint=adjoint, device=device,
+        jacobian_mask=jacobian_mask,
     )
     return w, j, st, ms, time.perf_counter() - t0
 

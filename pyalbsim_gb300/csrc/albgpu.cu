@@ -852,7 +852,9 @@ extern "C" int alb_build_maps(AlbCtx* ctx) {
     PhaseTimer pt(ctx, 1);
     for (int c = 0; c < ALB_CHANNELS; ++c) {
         if (ctx->rec_released[c]) continue;  // already indexed, nothing appended since
-        if (build_map_index(ctx->ws, ctx->rec[c], ctx->h_rec_count[c], ctx->map[c], ctx->st) != 0)
+        RecordStore r = ctx->rec[c];
+        if (!ctx->sc.adjoint) r.sco = nullptr;  // a store kept from an adjoint run: no scores now
+        if (build_map_index(ctx->ws, r, ctx->h_rec_count[c], ctx->map[c], ctx->st) != 0)
             return fail(ctx, ALB_ERR_CAPACITY, "photon-map index build failed (device memory or partition)");
         CK(cudaStreamSynchronize(ctx->st));
         if (ctx->keep_records) continue;  // the store stays for the next simulation
@@ -1341,9 +1343,15 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                     if (rc) msg = ctx->err;
                 }
             }
+            // with the adjoint option, an instance without a Jacobian buffer runs plain
+            const int adj = opt->adjoint && I.jacobian ? 1 : 0;
+            if (!rc && ctx && ctx->sc.adjoint != adj) {
+                rc = alb_set_option(ctx, ALB_OPT_ADJOINT, adj);
+                if (rc) msg = ctx->err;
+            }
             if (!rc && ctx) {
                 cudaEventRecord(e0, ctx->st);
-                rc = run_instance(ctx, I, opt->adjoint);
+                rc = run_instance(ctx, I, adj);
                 cudaEventRecord(e1, ctx->st);
                 cudaEventSynchronize(e1);
                 cudaEventElapsedTime(&I.device_ms, e0, e1);

@@ -117,3 +117,20 @@ def test_run_hypercube_matches_single_instance_runs(gpu_available):
         got = np.stack([r["waveform"][t] for t in r["waveform"]])
         np.testing.assert_array_equal(got, w.astype(np.float32))
         assert got.sum() > 0
+
+
+def test_batch_jacobian_mask_runs_masked_instances_plain(gpu_available):
+    """With the adjoint on, instances without a Jacobian buffer run plain on the same
+    contexts; every waveform still equals its single run."""
+    base = workloads.small(0.9, radius=0.5)
+    inst = batch.hypercube_instances(base, 6, seed=12, photons=(2e3, 2e4), gate=batch.surface_gate(base))
+    mask = [True, False, False, True, False, True]
+    w, j, st, _, _ = batch.run_batch(inst, streams=2, adjoint=True, jacobian_mask=mask)
+    assert np.all(st == 0), st
+    for i, x in enumerate(inst):
+        ws, js = _single(x.config, x.n_forward, x.n_backward, x.seed, mask[i])
+        np.testing.assert_array_equal(w[i], ws)
+        if mask[i]:
+            np.testing.assert_array_equal(j[i], js)
+        else:
+            assert j[i] is None
