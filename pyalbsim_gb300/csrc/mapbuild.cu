@@ -796,6 +796,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
         for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) hsh[j] = 0u;
         if (threadIdx.x < kSlots) htag[threadIdx.x] = kNoTag;
     }
+    __syncthreads();  // the slots are read by every thread, whatever the block's range holds
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     const uint64_t tile = (uint64_t)kSplitItems * blockDim.x;
     for (uint64_t t0 = r0; t0 < r1; t0 += tile) {
