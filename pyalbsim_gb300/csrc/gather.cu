@@ -808,11 +808,12 @@ ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, 
 }
 
 // MODE: kModeKnn (the reference's estimator without heatmaps, the hot path),
-// kModeKnnAdjoint (k-NN with the Jacobian and/or the sampled heatmaps), kModeRadius (fixed
-// radius; Jacobian and heatmaps when their accumulators are set). Separate instantiations
-// keep code the hot path never runs out of its instruction stream: the kernel is bound by
-// instruction issue and fetch.
-constexpr int kModeKnn = 0, kModeKnnAdjoint = 1, kModeRadius = 2;
+// kModeKnnAdjoint (k-NN with the Jacobian, and heatmaps when set), kModeRadius (fixed
+// radius; Jacobian and heatmaps when their accumulators are set), kModeKnnHeat (k-NN with
+// the sampled heatmaps, the reference's default). Separate instantiations keep code a run
+// never executes out of its instruction stream: the kernel is bound by instruction issue
+// and fetch.
+constexpr int kModeKnn = 0, kModeKnnAdjoint = 1, kModeRadius = 2, kModeKnnHeat = 3;
 
 template <int CHANNEL, int MODE>
 __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
@@ -1042,8 +1043,8 @@ void launch_gather(const SceneDev& sc, const MapDev& map, const QueryDev& q, int
     unsigned blocks = gather_blocks(q.n);
     int k = sc.k;
     if (sc.radius > 0.0) launch_gather_mode<kModeRadius>(map, q, channel, sc, acc, err, blocks, k, st);
-    else if (acc.jac_lo || (acc.hw_lo && map.fwi))
-        launch_gather_mode<kModeKnnAdjoint>(map, q, channel, sc, acc, err, blocks, k, st);
+    else if (acc.jac_lo) launch_gather_mode<kModeKnnAdjoint>(map, q, channel, sc, acc, err, blocks, k, st);
+    else if (acc.hw_lo && map.fwi) launch_gather_mode<kModeKnnHeat>(map, q, channel, sc, acc, err, blocks, k, st);
     else launch_gather_mode<kModeKnn>(map, q, channel, sc, acc, err, blocks, k, st);
     if (launches) ++*launches;
 }
