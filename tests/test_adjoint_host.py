@@ -166,3 +166,27 @@ def test_torch_function_contracts_the_jacobian(monkeypatch):
     (w * torch.from_numpy(G)).sum().backward()
     np.testing.assert_allclose(p.grad.numpy(), np.einsum("pcb,cb->p", J, G), rtol=1e-12)
     assert calls["with_depth"] is True
+
+
+def test_with_parameters_moves_the_lowest_layer_of_a_stack():
+    cfg = config_from_fixture(load("replay_twolayer.npz"))
+    p = adj.parameters_of(cfg)
+    top = float(cfg.water.layers[0].height)
+    q = p.copy()
+    q[0] = p[0] + 1.5
+    c2 = adj.with_parameters(cfg, q)
+    assert float(c2.water.layers[0].height) == top  # the upper layer keeps its height
+    assert abs(sum(float(L.height) for L in c2.water.layers) - q[0]) < 1e-12
+    assert all(float(L.absorption_coefficient) == q[1] for L in c2.water.layers)
+    with pytest.raises(ValueError):
+        adj.with_parameters(cfg, [top * 0.5, *p[1:]])  # the lowest layer would vanish
+
+
+def test_workloads_match_their_stated_geometry():
+    from pyalbsim_gb300 import workloads
+
+    big, small = build_scene(workloads.large()), build_scene(workloads.small(0.9, radius=0.5))
+    assert big.depth == 20.0 and big.sample_rate == int(2e10) and abs(big.fov - 50e-3) < 1e-15
+    assert abs(big.roughness ** 2 - 0.10) < 1e-12 and big.layers[0].hg_g == 0.0
+    assert small.depth == 5.0 and small.sample_rate == int(1e10) and small.gather_radius == 0.5
+    assert small.layers[0].hg_g == 0.9 and abs(small.seafloor_albedo - 0.15) < 1e-15
