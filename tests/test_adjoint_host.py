@@ -190,3 +190,31 @@ def test_workloads_match_their_stated_geometry():
     assert abs(big.roughness ** 2 - 0.10) < 1e-12 and big.layers[0].hg_g == 0.0
     assert small.depth == 5.0 and small.sample_rate == int(1e10) and small.gather_radius == 0.5
     assert small.layers[0].hg_g == 0.9 and abs(small.seafloor_albedo - 0.15) < 1e-15
+
+
+def test_depth_column_is_the_aligned_central_difference(monkeypatch):
+    """simulate_with_jacobian: the depth column is (W(D + h) - W(D - h)) / 2h on this run's
+    bins, the shifted runs cut or zero-padded (their time span follows the depth)."""
+    calls = []
+
+    def fake_run(cfg, nf, nb, seed, options, adjoint):
+        d = adj.parameters_of(cfg)[0]
+        calls.append((round(d, 6), adjoint, seed))
+        nbins = 100 + int(round(10 * (d - 2.0)))  # deeper: longer time span
+        w = np.tile(np.arange(nbins, dtype=np.float64) * d, (4, 1))
+        j = np.ones((5, 4, nbins)) if adjoint else None
+        return w, j
+
+    monkeypatch.setattr(adj, "_run", fake_run)
+    cfg = _hg_cfg(0.9)
+    D = adj.parameters_of(cfg)[0]
+    w, jac = adj.simulate_with_jacobian(cfg, 10, 10, 7, depth_step=0.5)
+    n = w.shape[1]
+    n_minus = 100 + int(round(10 * (D - 0.5 - 2.0)))  # the shallower run's span
+    t = np.arange(n, dtype=np.float64)
+    expect = t * (D + 0.5) - np.where(t < n_minus, t * (D - 0.5), 0.0)  # its missing bins are zero
+    np.testing.assert_allclose(jac[0, 0], expect / 1.0)
+    np.testing.assert_array_equal(jac[1:], 1.0)
+    assert [c[1] for c in calls] == [True, False, False] and len({c[2] for c in calls}) == 1
+    _, jac2 = adj.simulate_with_jacobian(cfg, 10, 10, 7, with_depth=False)
+    assert not jac2[0].any() and len(calls) == 4
