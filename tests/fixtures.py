@@ -125,3 +125,31 @@ def assert_statistically_equal(w, st, family_alpha=1e-3):
     if tested:
         worst = min(tested, key=lambda t: t[2])
         assert worst[2] > family_alpha / len(tested), worst
+
+
+def per_photon_times(photon, time):
+    """{photon id: sorted tuple of its record times}."""
+    out = {}
+    for p, t in zip(np.asarray(photon).tolist(), np.asarray(time, dtype=np.float64).tolist()):
+        out.setdefault(int(p), []).append(t)
+    return {p: tuple(sorted(v)) for p, v in out.items()}
+
+
+def diverged_photons(mine_photon, mine_time, ref_photon, ref_time):
+    """Photon ids whose record-time sequences differ between two runs of the same streams."""
+    a = per_photon_times(mine_photon, mine_time)
+    b = per_photon_times(ref_photon, ref_time)
+    return {p for p in set(a) | set(b) if a.get(p) != b.get(p)}
+
+
+def assert_same_records_except(mine, ref, skip, rtol_pos=1e-5, atol_pos=1e-5):
+    """Records of photons not in ``skip``: same ids and times, energies to 1e-6, positions
+    to the given tolerance. mine/ref: dicts with photon, time, energy, pos arrays."""
+    km = ~np.isin(mine["photon"], list(skip))
+    kr = ~np.isin(ref["photon"], list(skip))
+    ia = np.lexsort((mine["time"][km], mine["photon"][km]))
+    ib = np.lexsort((ref["time"][kr], ref["photon"][kr]))
+    np.testing.assert_array_equal(mine["photon"][km][ia], ref["photon"][kr][ib])
+    np.testing.assert_array_equal(mine["time"][km][ia], ref["time"][kr][ib])
+    np.testing.assert_allclose(mine["energy"][km][ia], ref["energy"][kr][ib], rtol=1e-6)
+    np.testing.assert_allclose(mine["pos"][km][ia], ref["pos"][kr][ib], rtol=rtol_pos, atol=atol_pos)

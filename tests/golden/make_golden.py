@@ -481,6 +481,29 @@ def config0_geometry():
     )
 
 
+def config1_geometry():
+    """The large single-instance scene at parity size: 400 m, 20 m water (a 0.10, b 0.40, FF),
+    GGX alpha 0.10, albedo 0.20, FOV 50 mrad, 2e10 Hz (0.05 ns bins)."""
+    return SimulationConfig(
+        scene=SceneConfig(flying_height=400.0),
+        water=WaterConfig(
+            layers=(
+                TurbidityLayerConfig(
+                    height=20.0,
+                    absorption_coefficient=0.10,
+                    scattering_coefficient=0.40,
+                    refractive_index=1.34,
+                ),
+            )
+        ),
+        laser=LaserConfig(divergence_angle=1e-3, nadir_angle=0.0, pulse_fwhm=3e-9),
+        sensor=SensorConfig(field_of_view=50e-3, sample_rate=int(2e10)),
+        sea_floor=SeaFloorConfig(albedo=0.20),
+        sea_surface=SeaSurfaceConfig(roughness=float(np.sqrt(0.10))),
+        heatmap=HeatmapConfig(enabled=False),
+    )
+
+
 def profiled_config():
     """Two depth-profiled layers: linear IOPs and index, then exponential ones with a
     linear salinity profile (TurbidityLayerModel's attenuation LUT, per-step speed)."""
@@ -518,6 +541,7 @@ def make_replay(only=None):
         ("twolayer", two_layer_config(), 800, 200, 12),
         ("cfg0", config0_geometry(), 300, 60, 0),
         ("profiled", profiled_config(), 1200, 300, 13),
+        ("cfg1", config1_geometry(), 250, 60, 1),
     ]
     if only:
         jobs = [j for j in jobs if j[0] in only]
@@ -696,5 +720,7 @@ if __name__ == "__main__":
         make_replay()
     if what == "replay_profiled":
         make_replay(only=("profiled",))
+    if what == "replay_cfg1":
+        make_replay(only=("cfg1",))
     if what in ("stats", "all"):
         make_stats()
