@@ -528,3 +528,66 @@ def test_slopes_refuse_replay(gpu_available):
             eng.forward(int(d["n_fwd"]), 0, replay=replay_streams(d, "fwd"))
     finally:
         eng.close()
+
+
+@pytest.mark.gpu
+def test_bench_geometry_replay_matches_reference(gpu_available):
+    """Replay at the large scene's geometry (400 m, 20 m water, 420 000 integrator steps).
+    A float32-ulp direction residual can move one crossing of a long path by a step, so up
+    to 1% of photons may diverge; every other photon's map records and gather queries match
+    the reference in step and energy (positions to 1 mm), and the waveform matches the
+    reference's float64 accumulation and the oracle to 1e-4 in L1."""
+    from fixtures import assert_same_records_except, diverged_photons
+
+    d = load("replay_cfg1.npz")
+    cfg = config_from_fixture(d)
+    nf, nb = int(d["n_fwd"]), int(d["n_bwd"])
+    eng = _engine(cfg)
+    try:
+        assert eng.scene.steps == int(d["steps"])
+        eng.forward(nf, 0, replay=replay_streams(d, "fwd"))
+        fexit = eng.ctx.exit_states(nf)
+        maps = {c: eng.ctx.export_map(c) for c in range(4)}
+        eng.build_maps()
+        eng.backward(nb, 0, replay=replay_streams(d, "bwd"))
+        bexit = eng.ctx.exit_states(nb)
+        queries = {k: eng.ctx.export_queries(k) for k in range(3)}
+        wf = eng.waveform_array(f64=True)
+        scene = eng.scene
+    finally:
+        eng.close()
+    fwd_div = set(np.nonzero(fexit["time"] != d["fwd_final_time"])[0].tolist())
+    for c in range(4):
+        pos, dr, e, t, fwi, sfi, pid = maps[c]
+        if f"map{c}_pos" in d:
+            fwd_div |= diverged_photons(pid, t, d[f"map{c}_ids"], d[f"map{c}_time"])
+        else:
+            assert len(e) == 0
+    q = d["queries"]
+    bwd_div = set(np.nonzero(bexit["time"] != d["bwd_final_time"])[0].tolist())
+    for kind in range(3):
+        ref = q[q[:, 0] == kind]
+        bwd_div |= diverged_photons(queries[kind]["id"], queries[kind]["time"], ref[:, 1].astype(np.int64),
+                                    ref[:, 9].astype(np.float32))
+    assert len(fwd_div) <= 0.01 * nf and len(bwd_div) <= 0.01 * nb, (fwd_div, bwd_div)
+    for c in range(4):
+        if f"map{c}_pos" not in d:
+            continue
+        pos, dr, e, t, fwi, sfi, pid = maps[c]
+        assert_same_records_except(dict(photon=pid, time=t, energy=e, pos=pos),
+                                   dict(photon=d[f"map{c}_ids"], time=d[f"map{c}_time"],
+                                        energy=d[f"map{c}_energy"], pos=d[f"map{c}_pos"]),
+                                   fwd_div, atol_pos=1e-3)
+    for kind in range(3):
+        ref = q[q[:, 0] == kind]
+        mine = queries[kind]
+        assert_same_records_except(dict(photon=mine["id"], time=mine["time"], energy=mine["energy"], pos=mine["pos"]),
+                                   dict(photon=ref[:, 1].astype(np.int64), time=ref[:, 9].astype(np.float32),
+                                        energy=ref[:, 8], pos=ref[:, 2:5]),
+                                   bwd_div, atol_pos=1e-3)
+    orc = oracle_run(scene, nf, nb, replay_fwd=replay_streams(d, "fwd"), replay_bwd=replay_streams(d, "bwd"))
+    for c in range(4):
+        for ref in (d["waveform64"][c], orc["waveform"][c]):
+            den = np.abs(ref).sum()
+            if den:
+                assert np.abs(wf[c] - ref).sum() / den < 1e-4, c

@@ -159,8 +159,8 @@ def test_bench_geometry_replay_matches_reference_photon_by_photon():
     steps). Over paths this long, a direction that differs from NumPy's vectorised kernels
     by a float32 ulp (the residual of the other replays) can move one plane or
     optical-depth crossing by a step; that photon then diverges. At most 1% of photons may
-    do so. Every other photon's records match exactly in step and energy (positions to
-    1 mm), and the waveform matches the reference's float64 accumulation to 1e-4 in L1."""
+    do so. Every other photon's map records and gather queries match in step and energy
+    (positions to 1 mm), and the waveform matches the reference's float64 accumulation to 1e-4 in L1."""
     from fixtures import assert_same_records_except, diverged_photons
 
     d = load("replay_cfg1.npz")
@@ -191,6 +191,11 @@ def test_bench_geometry_replay_matches_reference_photon_by_photon():
         # over ~100 m of path a float32-ulp direction difference moves a position by < 1 mm
         assert_same_records_except(dict(photon=mp["photon"], time=mp["time"], energy=mp["energy"], pos=mp["pos"]),
                                    ref, fwd_div, atol_pos=1e-3)
+    for kind in range(3):
+        ref = q[q[:, 0] == kind]
+        mine = r["queries"][kind]
+        assert_same_records_except(mine, dict(photon=ref[:, 1].astype(np.int64), time=ref[:, 9].astype(np.float32),
+                                              energy=ref[:, 8], pos=ref[:, 2:5]), bwd_div, atol_pos=1e-3)
     for c in range(4):
         ref = d["waveform64"][c]
         den = np.abs(ref).sum()
