@@ -1,8 +1,8 @@
 """Generate the golden fixtures under tests/golden/ by running the reference simulator.
 
 Run in a container where the reference is importable (default path below, or
-``ALB_REFERENCE_SRC``). The GPU machine never runs this script: the fixtures it writes are
-committed. Nothing here restates the reference's physics; the script only drives the
+``ALB_REFERENCE_SRC``). The GPU tests never run this script: the fixtures it writes
+are committed. Nothing here restates the reference's physics; the script only drives the
 reference's own objects and records what they do:
 
 * a proxy ``numpy.random.Generator`` logs every draw and attributes it to photon ids

@@ -83,7 +83,8 @@ def test_config_validation_like_reference():
     assert isinstance(layer.salinity, float) and layer.num_sublayers == 60
 
 
-REF_SRC = "/root/reference/src"
+# reference sources for the config-field comparison (present only where the fixtures are made)
+REF_SRC = os.environ.get("ALB_REFERENCE_SRC", "/root/reference/src")
 
 
 # Fields with no counterpart in the reference, appended after its own and defaulting to
