@@ -788,8 +788,9 @@ static double ggx_dlog_da2(double rough, const double wi_in[3], const double wo_
     double nh = h[1] < 0 ? 0 : (h[1] > 1 ? 1 : h[1]);
     if (!(n_wi > 0 && n_wo > 0)) return 0.0;
     double den = (a2 - 1.0) * nh * nh + 1.0;
+    double pd2 = PI * den * den; /* D = a2 / (pd2 + eps): the epsilon's share of the denominator */
     double si = sqrt(a2 + (1 - a2) * (n_wi * n_wi)), so = sqrt(a2 + (1 - a2) * (n_wo * n_wo));
-    return 1.0 / a2 - 2.0 * nh * nh / den - (1.0 - n_wi * n_wi) / (2.0 * si * (n_wi + si)) -
+    return 1.0 / a2 - 2.0 * nh * nh / den * (pd2 / (pd2 + (double)EPS32)) - (1.0 - n_wi * n_wi) / (2.0 * si * (n_wi + si)) -
            (1.0 - n_wo * n_wo) / (2.0 * so * (n_wo + so));
 }
 

@@ -156,3 +156,84 @@ class WaveformFunction:
 
             cls._impl = _Fn
         return cls._impl.apply(params, cfg, n_fwd, n_bwd, seed, options)
+
+
+# Relative half-steps of the central differences in ``difference_check``: a, b and g move
+# paths (free-path lengths, scatter counts, directions), so their differences need steps
+# that span many integrator and neighbour-set jumps; albedo and roughness leave every path
+# unchanged and differ smoothly at a small step.
+CHECK_STEPS = {1: 0.05, 2: 0.05, 3: 0.02, 4: 1e-3, 5: 1e-3}
+
+
+def difference_check(cfg, n_fwd: int, n_bwd: int, seeds: Sequence[int], steps=None, streams: int = 4,
+                     runner=None) -> dict:
+    """The adjoint's columns against central differences with common random numbers, in
+    expectation over seeds.
+
+    Per seed: one adjoint run at ``cfg`` and, per parameter p in ``steps`` (PARAMS index ->
+    relative half-step; default ``CHECK_STEPS``, without g on a Fournier-Forand column), two
+    plain runs at p(1 +- h) with the seed's streams. Compared per parameter and channel: the
+    total over bins of the column (d total / d p) and of the difference. A single seed says
+    little for a, b and g (a path that moves changes its integrator step and neighbour set,
+    so both estimates carry noise), hence the seeds and the paired standard error.
+
+    runner(configs, seeds, jacobian_mask) -> (waveforms, jacobians) replaces the device
+    batch (tests); by default every run goes through one ``alb_batch_run``.
+
+    Returns {PARAMS name: {"adjoint": [4], "difference": [4], "rel_diff": [4],
+    "rel_diff_se": [4]}} with rel_diff = mean(adjoint - difference) / |mean(difference)|
+    and its paired standard error over seeds (NaN in channels the parameter does not
+    reach)."""
+    p0 = parameters_of(cfg)
+    if steps is None:
+        steps = dict(CHECK_STEPS)
+        if getattr(cfg.water.layers[0], "henyey_greenstein_g", None) is None:
+            steps.pop(3)
+    if any(i == 0 for i in steps):
+        raise ValueError("the depth column is itself a difference; it has no adjoint to check")
+    configs, run_seeds, mask = [], [], []
+    for s in seeds:
+        configs.append(cfg)
+        run_seeds.append(s)
+        mask.append(True)
+        for i, h in steps.items():
+            for sign in (1.0, -1.0):
+                q = p0.copy()
+                q[i] *= 1.0 + sign * h
+                configs.append(with_parameters(cfg, q))
+                run_seeds.append(s)
+                mask.append(False)
+    if runner is None:
+        from pyalbsim_gb300.batch import Instance, run_batch
+
+        inst = [Instance(c, n_fwd, n_bwd, s, None) for c, s in zip(configs, run_seeds)]
+        waves, jacs, status, _, _ = run_batch(inst, streams=streams, adjoint=True, jacobian_mask=mask)
+        if np.any(status != 0):
+            raise RuntimeError(f"difference check: {int((status != 0).sum())} runs failed")
+    else:
+        waves, jacs = runner(configs, run_seeds, mask)
+    per = 1 + 2 * len(steps)
+    S = len(seeds)
+    adj = {i: np.zeros((S, 4)) for i in steps}
+    dif = {i: np.zeros((S, 4)) for i in steps}
+    for k in range(S):
+        base = k * per
+        for n, (i, h) in enumerate(steps.items()):
+            adj[i][k] = jacs[base][i - 1].sum(axis=1)
+            wp = waves[base + 1 + 2 * n].sum(axis=1)
+            wm = waves[base + 2 + 2 * n].sum(axis=1)
+            dif[i][k] = (wp - wm) / (2.0 * h * p0[i])
+    out = {}
+    for i in steps:
+        a, d = adj[i], dif[i]
+        dm = d.mean(axis=0)
+        # a channel the parameter does not reach has an all-zero column and a difference of
+        # summation-order rounding: no ratio
+        den = np.where((dm != 0) & np.any(a != 0, axis=0), np.abs(dm), np.nan)
+        diff = a - d
+        se = diff.std(axis=0, ddof=1) / np.sqrt(S) if S > 1 else np.full(4, np.nan)
+        out[PARAMS[i]] = {
+            "adjoint": a.mean(axis=0).tolist(), "difference": dm.tolist(),
+            "rel_diff": (diff.mean(axis=0) / den).tolist(), "rel_diff_se": (se / den).tolist(),
+        }
+    return out

@@ -620,8 +620,9 @@ ALB_DEVICE float scatter_weight(const SceneDev& sc, int layer, float dx, float d
 }
 
 // Adjoint (extension): d ln(ggx_weight) / d(alpha^2), the same vectors as ggx_weight:
-// 1/a2 - 2 Hy^2 / (|H|^2 den) from the distribution term and -(1 - n^2) / (2 s (n + s)),
-// s = sqrt((1 - a2) n^2 + a2), from each Smith G1 factor; the Fresnel term has no a2.
+// 1/a2 - 2 Hy^2 / (|H|^2 den) * pi den^2 / (pi den^2 + eps) from the distribution term and
+// -(1 - n^2) / (2 s (n + s)), s = sqrt((1 - a2) n^2 + a2), from each Smith G1 factor; the
+// Fresnel term has no a2.
 ALB_DEVICE float ggx_dlog_da2(float a2, float wix, float wiy, float wiz, float wox, float woy, float woz) {
     float ni = rsqrtf(fmaf(wix, wix, fmaf(wiy, wiy, wiz * wiz)));
     wix *= ni; wiy *= ni; wiz *= ni;
@@ -634,7 +635,10 @@ ALB_DEVICE float ggx_dlog_da2(float a2, float wix, float wiy, float wiz, float w
     float d = 1.f / a2;
     if (H2 > 0.f && Hy > 0.f) {
         float den = fmaf(a2 * Hy, Hy, t) / H2;
-        d -= 2.f * (Hy * Hy / H2) / den;
+        // D = a2 / (pi den^2 + eps): the epsilon takes the share eps / (pi den^2 + eps) of
+        // the denominator (about 0.6% at the specular peak for a2 = 0.0025)
+        float pd2 = 3.14159265358979f * den * den;
+        d -= 2.f * (Hy * Hy / H2) / den * (pd2 / (pd2 + kEps32));
     }
     float si = sqrtf(fmaf(1.f - a2, n_wi * n_wi, a2)), so = sqrtf(fmaf(1.f - a2, n_wo * n_wo, a2));
     d -= (1.f - n_wi * n_wi) / (2.f * si * (n_wi + si));

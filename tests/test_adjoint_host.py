@@ -218,3 +218,87 @@ def test_depth_column_is_the_aligned_central_difference(monkeypatch):
     assert [c[1] for c in calls] == [True, False, False] and len({c[2] for c in calls}) == 1
     _, jac2 = adj.simulate_with_jacobian(cfg, 10, 10, 7, with_depth=False)
     assert not jac2[0].any() and len(calls) == 4
+
+
+def _oracle_runner(nf, nb):
+    def run(configs, seeds, mask):
+        waves, jacs = [], []
+        for c, s, m in zip(configs, seeds, mask):
+            r = oracle_run(build_scene(c), nf, nb, seed=s, adjoint=bool(m))
+            waves.append(r["waveform"])
+            jacs.append(r["jacobian"] if m else None)
+        return waves, jacs
+    return run
+
+
+def test_difference_check_on_the_oracle():
+    """The seed-averaged check, run on the oracle: the albedo and roughness columns (paths
+    unchanged by the parameter) equal their differences on every seed, so their paired
+    difference is ~0; a, b and g are reported with a standard error."""
+    cfg = _hg_cfg(0.9)
+    out = adj.difference_check(cfg, 600, 150, seeds=[1, 2, 3], runner=_oracle_runner(600, 150))
+    assert set(out) == {"absorption", "scattering", "asymmetry", "seafloor_albedo", "roughness"}
+    for name in ("seafloor_albedo", "roughness"):
+        r = out[name]
+        scale = max(abs(x) for x in r["difference"])
+        for ch in range(4):
+            if r["adjoint"][ch] == 0:  # a channel the parameter does not reach: rounding only
+                assert abs(r["difference"][ch]) < 1e-6 * scale, (name, ch, r)
+                assert np.isnan(r["rel_diff"][ch])
+            else:
+                assert abs(r["rel_diff"][ch]) < 1e-4, (name, ch, r)
+    for name in ("absorption", "scattering", "asymmetry"):
+        assert all(len(out[name][k]) == 4 for k in ("adjoint", "difference", "rel_diff", "rel_diff_se"))
+
+
+def test_difference_check_steps_and_plumbing():
+    """A Fournier-Forand column has no g step; the depth has no adjoint column; every seed
+    runs one adjoint instance and two plain runs per parameter at p(1 +- h)."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    p0 = adj.parameters_of(cfg)
+    seen = []
+
+    def fake(configs, seeds, mask):
+        seen.append((configs, seeds, mask))
+        nb = 3
+        waves = [np.full((4, nb), adj.parameters_of(c)[1]) for c in configs]
+        jacs = [np.ones((5, 4, nb)) if m else None for m in mask]
+        return waves, jacs
+
+    out = adj.difference_check(cfg, 10, 10, seeds=[7, 8], runner=fake)
+    assert "asymmetry" not in out
+    configs, seeds, mask = seen[0]
+    assert len(configs) == 2 * (1 + 2 * 4) and seeds == [7] * 9 + [8] * 9
+    assert mask == ([True] + [False] * 8) * 2
+    pa = adj.parameters_of(configs[1])
+    np.testing.assert_allclose(pa[1], p0[1] * (1 + adj.CHECK_STEPS[1]))
+    # waveform = a in every bin: d total / d a = 3 per channel; the adjoint's column says 3
+    np.testing.assert_allclose(out["absorption"]["difference"], 3.0)
+    np.testing.assert_allclose(out["absorption"]["rel_diff"], 0.0, atol=1e-12)
+    np.testing.assert_allclose(out["scattering"]["difference"], 0.0)
+    with pytest.raises(ValueError):
+        adj.difference_check(cfg, 10, 10, seeds=[1], steps={0: 0.01}, runner=fake)
+
+
+def test_oracle_roughness_column_at_the_specular_peak():
+    """At nadir the surface return is gathered next to the specular direction, where the
+    GGX distribution's denominator pi den^2 (den = alpha^2 there) is small enough that its
+    float32 epsilon takes ~0.6% of it (alpha^2 = 0.0025); the column carries that share."""
+    from pyalbsim_gb300.workloads import small
+
+    cfg = small()
+    rough = cfg.sea_surface.roughness
+    h = 1e-4 * rough
+    ss = cfg.sea_surface
+
+    def run(c, adjoint=False):
+        return oracle_run(build_scene(c), 3000, 750, seed=5, adjoint=adjoint)
+
+    r = run(cfg, adjoint=True)
+    wp = run(dataclasses.replace(cfg, sea_surface=dataclasses.replace(ss, roughness=rough + h)))["waveform"]
+    wm = run(dataclasses.replace(cfg, sea_surface=dataclasses.replace(ss, roughness=rough - h)))["waveform"]
+    fd = (wp[2] - wm[2]) / (2 * h)
+    j = r["jacobian"][4][2]
+    assert np.abs(fd).sum() > 0
+    assert abs(j.sum() - fd.sum()) / abs(fd.sum()) < 1e-4
+    assert np.abs(j - fd).sum() / np.abs(fd).sum() < 1e-3
