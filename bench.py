@@ -236,6 +236,11 @@ def main():
                      "launches_per_step": sc_calls / args.steps, "peak_source": peak_kind,
                      "traffic_source": "ncu dram bytes per query of a 1e6-photon capture, scaled to a launch"},
         "gpu_launches": int(launches),
+        # interaction events (scatters, surface crossings, seafloor hits) of the last step's
+        # forward and backward traces over the mean step time
+        "interaction_events": {
+            "value": world * (gstats["forward_events"] + gstats["events"]) / (ms_step / 1e3), "unit": "events/s",
+            "per_step": gstats["forward_events"] + gstats["events"]},
         "last_step_counters": gstats,
         "clocks": clk.summary(),
         "waveform_total": float(wf.sum()),

@@ -282,7 +282,10 @@ typedef struct AlbBatchOptions {
 
 int alb_batch_run(AlbBatchInstance* instances, uint64_t n, const AlbBatchOptions* options);
 
-/* Device-side counters of the last trace / gather (events, records, queries, launches). */
+/* Device-side counters: [0] events and [1] photons of the last trace, [2] kernels launched
+ * by this library, [4 + 4c .. 7 + 4c] gather counters of channel c (leaves, nodes, selects,
+ * queries), [24 + c] inexact queries of channel c, [28] events and [29] photons of the last
+ * forward trace. n entries are written (at most 32). */
 int alb_stats(AlbCtx* ctx, int64_t* out, int n);
 
 /* Accumulated device time (ms, CUDA events on the context's stream) and call counts per

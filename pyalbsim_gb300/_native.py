@@ -474,12 +474,14 @@ class NativeContext:
         return dist, idx
 
     def stats(self):
-        """Counters of the last trace (events, photons) and gathers (per channel: leaves
+        """Counters of the last trace (events, photons), of the last forward trace
+        (forward_events, forward_photons) and of the gathers (per channel: leaves
         opened, internal nodes expanded, candidate reductions, queries, and queries whose
         answer a buffer bound made inexact, which takes mass ties of distances)."""
         out = np.zeros(32, np.int64)
         self._check(self.lib.alb_stats(self.h, _ptr(out), 32))
-        st = {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2])}
+        st = {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2]),
+              "forward_events": int(out[28]), "forward_photons": int(out[29])}
         for c, name in enumerate(("bottom", "scatter", "surface_reflection", "transmission_up")):
             lv, nd, se, nq = (int(x) for x in out[4 + 4 * c: 8 + 4 * c])
             st[f"gather_{name}"] = {

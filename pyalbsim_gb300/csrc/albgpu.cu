@@ -712,7 +712,8 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
         }
         ctx->ex_n = n;
     }
-    CK(cudaMemsetAsync(ctx->d_stats, 0, 32 * 8, ctx->st));
+    // slots 28/29 keep the last forward trace's events and photons across the backward trace
+    CK(cudaMemsetAsync(ctx->d_stats, 0, 28 * 8, ctx->st));
     if (pass == ALB_FORWARD) {
         ctx->maps_built = false;
         uint64_t before[ALB_CHANNELS];
@@ -749,10 +750,12 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             }
             if (!overflow) {
                 for (int c = 0; c < ALB_CHANNELS; ++c) ctx->h_rec_count[c] = cnt[c];
+                CK(cudaMemcpyAsync(ctx->d_stats + 28, ctx->d_stats, 2 * 8, cudaMemcpyDeviceToDevice, ctx->st));
                 ctx->ws.release(mark);
                 return ALB_OK;
             }
             // undo and retry with the measured sizes
+            CK(cudaMemsetAsync(ctx->d_stats, 0, 2 * 8, ctx->st));
             CK(cudaMemcpyAsync(ctx->d_rec_count, before, sizeof before, cudaMemcpyHostToDevice, ctx->st));
             if (hb) CK(cudaMemcpyAsync(ctx->hm_radius, radius_backup.data(), hb * 4, cudaMemcpyHostToDevice, ctx->st));
             CK(cudaStreamSynchronize(ctx->st));

@@ -591,3 +591,23 @@ def test_bench_geometry_replay_matches_reference(gpu_available):
             den = np.abs(ref).sum()
             if den:
                 assert np.abs(wf[c] - ref).sum() / den < 1e-4, c
+
+
+@pytest.mark.gpu
+def test_stats_keep_the_forward_trace_counters(gpu_available):
+    """The last forward trace's events and photons survive the backward trace (slots 28/29),
+    so a step's interaction events are readable after it without a mid-step sync."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    eng = _engine(cfg, ids=False, exits=False, precise=False)
+    try:
+        eng.forward(4000, 11)
+        fwd = eng.ctx.stats()
+        eng.build_maps()
+        eng.backward(1000, 11)
+        st = eng.ctx.stats()
+    finally:
+        eng.close()
+    # every photon meets the surface at least once inside the window
+    assert fwd["photons"] == 4000 and fwd["events"] >= 4000
+    assert st["forward_events"] == fwd["events"] and st["forward_photons"] == 4000
+    assert st["photons"] == 1000 and st["events"] >= 1000
