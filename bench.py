@@ -278,16 +278,15 @@ def gradients_measure(nf: int):
     separately, in expectation over seeds (``gradient_check_measure``): on one seed a central
     difference of a, b or the depth jumps with every integrator step and neighbour set that
     its step moves, so a single-seed comparison says nothing about either estimate."""
+    import dataclasses
+
     import torch
 
-    from pyalbsim_gb300.adjoint import WaveformFunction, parameters_of, with_parameters
+    from pyalbsim_gb300.adjoint import WaveformFunction, with_parameters
+    from pyalbsim_gb300.batch import surface_gate
     from pyalbsim_gb300.config.gpu import GpuRunOptions
     from pyalbsim_gb300.engine import GpuEngine
     from pyalbsim_gb300.workloads import large
-
-    import dataclasses
-
-    from pyalbsim_gb300.batch import surface_gate
 
     nb = max(nf // 4, 1)
     truth = np.array([12.0, 0.08, 0.30, 0.90, 0.18, float(np.sqrt(0.08))])
