@@ -15,12 +15,14 @@ reference's own objects and records what they do:
 
 Fixtures:
   kat_physics.npz      known-answer values of the reference's physics functions
+  fd_ref.npz           reference waveforms at seafloor albedo and surface roughness +- h
+                       (common-random-number differences of the reference itself)
   replay_<name>.npz    per-photon variate streams, photon maps, exit states, queries and
                        waveforms of a small reference run
   knn.npz              scipy KDTree k-nearest-neighbour answers on clustered maps
   stats_small.npz      per-bin mean / standard error over independent reference runs
 
-Usage: python tests/golden/make_golden.py [kat|replay|knn|stats|all]
+Usage: python tests/golden/make_golden.py [kat|replay|knn|stats|fd_ref|all]
 """
 
 from __future__ import annotations
@@ -552,6 +554,47 @@ def make_replay(only=None):
         print(f"replay_{name}: {time.time() - t:.1f}s, queries {len(out['queries'])}")
 
 
+def make_fd_ref():
+    """Central differences of the reference simulator itself, for the adjoint columns.
+
+    The 'small' (10 degrees off nadir) and 'cfg0' (nadir: the surface return is gathered at
+    the GGX specular peak) replay scenes and seeds, run at seafloor albedo +- 1% and surface
+    roughness +- 0.1%. Neither parameter moves a photon or changes how many variates a step
+    draws (the albedo scales energies, the roughness only the surface-reflection gather
+    weight), so with the same seed each pair replays the base run's variates: a
+    common-random-number difference. The generator checks that by comparing the recorded
+    streams with the base fixture's. Waveforms are the float64 accumulation of the
+    reference's own contributions."""
+    import dataclasses
+
+    out = {}
+    for job, cfg, nf, nb, seed in (("small", small_config(), 1500, 400, 11),
+                                   ("cfg0", config0_geometry(), 300, 60, 0)):
+        base = np.load(os.path.join(OUT_DIR, f"replay_{job}.npz"))
+        assert int(base["seed"]) == seed and int(base["n_fwd"]) == nf and int(base["n_bwd"]) == nb
+        alb = cfg.sea_floor.albedo
+        rough = cfg.sea_surface.roughness
+        h_alb, h_rough = 0.01 * alb, 1e-3 * rough
+        out[f"{job}_h_albedo"] = h_alb
+        out[f"{job}_h_roughness"] = h_rough
+        floor, surf = cfg.sea_floor, cfg.sea_surface
+        runs = (
+            ("albedo_plus", dataclasses.replace(cfg, sea_floor=dataclasses.replace(floor, albedo=alb + h_alb))),
+            ("albedo_minus", dataclasses.replace(cfg, sea_floor=dataclasses.replace(floor, albedo=alb - h_alb))),
+            ("roughness_plus", dataclasses.replace(cfg, sea_surface=dataclasses.replace(surf, roughness=rough + h_rough))),
+            ("roughness_minus",
+             dataclasses.replace(cfg, sea_surface=dataclasses.replace(surf, roughness=rough - h_rough))),
+        )
+        for name, c in runs:
+            t = time.time()
+            r = run_recorded(c, nf, nb, seed)
+            for p in ("fwd", "bwd"):
+                assert np.array_equal(r[f"{p}_stream"], base[f"{p}_stream"]), (job, name, p, "variates differ")
+            out[f"{job}_{name}_waveform64"] = r["waveform64"]
+            print(f"fd_ref {job} {name}: {time.time() - t:.1f}s")
+    np.savez_compressed(os.path.join(OUT_DIR, "fd_ref.npz"), **out)
+
+
 def make_kat():
     from alb_sim.math.direction_cone import sample_directions_in_cone_uniform  # noqa: F401
     from alb_sim.math.rotation_matrix import rotation_from_z_batch
@@ -722,5 +765,7 @@ if __name__ == "__main__":
         make_replay(only=("profiled",))
     if what == "replay_cfg1":
         make_replay(only=("cfg1",))
+    if what in ("fd_ref", "all"):
+        make_fd_ref()
     if what in ("stats", "all"):
         make_stats()
