@@ -37,6 +37,9 @@ from pyalbsim_gb300.batch import Instance, RANGES, run_batch, surface_gate
 from pyalbsim_gb300.workloads import small
 
 INITIAL = np.array([10.0, 0.1, 0.3, 0.9, 0.2, math.sqrt(0.1)])
+# counts added to the scaled waveform in the Poisson likelihood: bins the model leaves empty
+# while the target holds counts keep a finite loss
+POISSON_FLOOR = 1e-2
 
 
 def gated_base(length: float = 400e-9):
@@ -80,9 +83,23 @@ def fit(
     loss: str = "log",
     resample: bool = False,
     depth_grid: Optional[Sequence[float]] = None,
+    fixed: Optional[Sequence[bool]] = None,
+    prior_sigma: Optional[Sequence[Optional[float]]] = None,
 ) -> Dict:
     """Fit every row of ``targets`` (n x 6). Returns final parameters, depth errors and the
-    per-iteration mean loss."""
+    per-iteration mean data loss.
+
+    loss: "log" (squared difference of log(1 + counts)), "mse", or "poisson" (the negative
+    log-likelihood of the Poisson counts, sum(lambda - counts ln lambda), lambda the scaled
+    waveform plus a floor of ``POISSON_FLOOR`` counts).
+
+    From one waveform the depth trades against attenuation and scattering, so the free
+    six-parameter fit is not identifiable. Two ways to constrain it:
+    ``fixed``: six booleans; a fixed parameter stays at its initial value.
+    ``prior_sigma``: six standard deviations (None = flat) of Gaussian priors on
+    u = ln(theta / initial); the fit then minimises the data loss plus sum((u / sigma)^2) / 2.
+    With the Poisson loss that is the maximum a posteriori estimate; with the others the
+    sigmas are relative to the loss's own scale."""
     base = base or gated_base()
     targets = np.asarray(targets, dtype=np.float64)
     n = len(targets)
@@ -98,12 +115,37 @@ def fit(
 
     theta0 = np.array(initial if initial is not None else INITIAL, dtype=np.float64)
     u = np.zeros((n, 6))
+    free = np.ones(6) if fixed is None else 1.0 - np.asarray(fixed, dtype=np.float64)
+    if free.shape != (6,):
+        raise ValueError("fixed needs six entries")
+    inv_var = np.zeros(6)
+    if prior_sigma is not None:
+        if len(prior_sigma) != 6:
+            raise ValueError("prior_sigma needs six entries")
+        for k, sd in enumerate(prior_sigma):
+            if sd is not None:
+                if not sd > 0:
+                    raise ValueError("prior standard deviations must be positive")
+                inv_var[k] = 1.0 / (sd * sd)
+
+    if loss not in ("log", "mse", "poisson"):
+        raise ValueError(f"unknown loss {loss!r}")
 
     def loss_of(wi, i):
+        return loss_and_grad(wi, i)[0]
+
+    def loss_and_grad(wi, i):
+        """(loss, d loss / d waveform) of one target."""
         sw = np.clip(scale[i] * wi, 0.0, None)
         if loss == "mse":
-            return float(((sw - counts[i]) ** 2).sum())
-        return float(((np.log1p(sw) - np.log1p(counts[i])) ** 2).sum())
+            r = sw - counts[i]
+            return float((r ** 2).sum()), 2.0 * scale[i] * r
+        if loss == "poisson":
+            lam = sw + POISSON_FLOOR
+            c = counts[i]
+            return float((lam - c * np.log(lam)).sum()), scale[i] * (1.0 - c / lam)
+        r = np.log1p(sw) - np.log1p(counts[i])
+        return float((r ** 2).sum()), 2.0 * r * scale[i] / (1.0 + sw)
 
     if depth_grid is not None:
         grid = np.asarray(depth_grid, dtype=np.float64)
@@ -118,7 +160,8 @@ def fit(
         for i in range(n):
             ls = [loss_of(gw[i * len(grid) + j], i) if gst[i * len(grid) + j] == 0 else np.inf
                   for j in range(len(grid))]
-            u[i, 0] = math.log(grid[int(np.argmin(ls))] / theta0[0])
+            if free[0]:
+                u[i, 0] = math.log(grid[int(np.argmin(ls))] / theta0[0])
     m_ = np.zeros((n, 6))
     v_ = np.zeros((n, 6))
     b1, b2, eps = 0.9, 0.999, 1e-8
@@ -126,35 +169,29 @@ def fit(
     for it in range(iters):
         theta = _clip(theta0 * np.exp(u))
         key = (seed << 40) + (1 << 32) + (it if resample else 0)
+        per = 3 if free[0] else 1  # the depth pair only while the depth is free
         inst = []
         for i in range(n):
             inst.append(Instance(with_parameters(base, theta[i]), photons, nb, key, theta[i]))
-            for sgn in (1.0, -1.0):
+            for sgn in ((1.0, -1.0) if free[0] else ()):
                 q = theta[i].copy()
                 q[0] += sgn * depth_step
                 inst.append(Instance(with_parameters(base, q), photons, nb, key, q))
         w, jac, st, _, _ = run_batch(inst, streams=streams, adjoint=True,
-                                     jacobian_mask=[k % 3 == 0 for k in range(len(inst))])
+                                     jacobian_mask=[k % per == 0 for k in range(len(inst))])
         grads = np.zeros((n, 6))
         losses = np.zeros(n)
-
-        def loss_and_grad(wi, i):
-            sw = np.clip(scale[i] * wi, 0.0, None)
-            if loss == "mse":
-                r = sw - counts[i]
-                return float((r ** 2).sum()), 2.0 * scale[i] * r
-            r = np.log1p(sw) - np.log1p(counts[i])
-            return float((r ** 2).sum()), 2.0 * r * scale[i] / (1.0 + sw)
-
         for i in range(n):
-            if np.any(st[3 * i:3 * i + 3] != 0):
-                raise RuntimeError(f"iteration {it}, target {i}: status {st[3 * i:3 * i + 3]}")
-            losses[i], dl_dw = loss_and_grad(w[3 * i], i)
-            grads[i, 1:] = np.einsum("pcb,cb->p", jac[3 * i], dl_dw)
-            lp = loss_and_grad(w[3 * i + 1], i)[0]
-            lm = loss_and_grad(w[3 * i + 2], i)[0]
-            grads[i, 0] = (lp - lm) / (2.0 * depth_step)
-        gu = grads * theta  # d L / d u for theta = theta0 e^u
+            k = per * i
+            if np.any(st[k:k + per] != 0):
+                raise RuntimeError(f"iteration {it}, target {i}: status {st[k:k + per]}")
+            losses[i], dl_dw = loss_and_grad(w[k], i)
+            grads[i, 1:] = np.einsum("pcb,cb->p", jac[k], dl_dw)
+            if free[0]:
+                lp = loss_and_grad(w[k + 1], i)[0]
+                lm = loss_and_grad(w[k + 2], i)[0]
+                grads[i, 0] = (lp - lm) / (2.0 * depth_step)
+        gu = (grads * theta + u * inv_var) * free  # d (L + prior) / d u for theta = theta0 e^u
         m_ = b1 * m_ + (1 - b1) * gu
         v_ = b2 * v_ + (1 - b2) * gu * gu
         mh = m_ / (1 - b1 ** (it + 1))

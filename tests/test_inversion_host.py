@@ -49,7 +49,7 @@ def fake(monkeypatch):
     monkeypatch.setattr(inversion, "with_parameters", lambda base, p: None)
 
 
-@pytest.mark.parametrize("loss", ["mse", "log"])
+@pytest.mark.parametrize("loss", ["mse", "log", "poisson"])
 def test_fit_recovers_a_nearby_target(fake, loss):
     target = np.array([[11.0, 0.12, 0.33, 0.88, 0.22, 0.30]])
     r = inversion.fit(target, iters=400, lr=2e-2, photons=100, peak=1e6, base=object(), loss=loss,
@@ -74,3 +74,45 @@ def test_depth_grid_start_finds_a_distant_seafloor(fake):
                          depth_grid=np.linspace(2, 38, 10))
     assert abs(plain["depth_error"][0]) > 5.0
     assert abs(grid["depth_error"][0]) < 0.1, grid["params"]
+
+
+def test_fixed_parameters_make_attenuation_identifiable(fake):
+    """With the albedo and g known (fixed at the truth) the toy separates a from the albedo
+    and b from g: a and b are recovered individually, and fixed values do not move."""
+    target = np.array([[11.0, 0.12, 0.33, 0.88, 0.22, 0.30]])
+    initial = np.array([10.0, 0.10, 0.30, 0.88, 0.22, 0.25])
+    r = inversion.fit(target, iters=400, lr=2e-2, photons=100, peak=1e6, base=object(), loss="mse",
+                      initial=initial, fixed=[False, False, False, True, True, False])
+    P = r["params"][0]
+    assert P[3] == initial[3] and P[4] == initial[4]
+    np.testing.assert_allclose(P[[0, 1, 2, 5]], target[0, [0, 1, 2, 5]], rtol=0.03)
+
+
+def test_fixed_depth_skips_the_depth_pair(fake, monkeypatch):
+    calls = []
+
+    def counting(instances, **kw):
+        calls.append(len(instances))
+        return _fake_run_batch(instances, **kw)
+
+    monkeypatch.setattr(inversion, "run_batch", counting)
+    target = np.array([[11.0, 0.12, 0.33, 0.88, 0.22, 0.30], [9.0, 0.1, 0.3, 0.9, 0.2, 0.3]])
+    inversion.fit(target, iters=3, photons=100, base=object(), fixed=[True] + [False] * 5)
+    assert calls == [2, 2, 2, 2]  # the targets, then one adjoint instance per target and iteration
+    calls.clear()
+    inversion.fit(target, iters=2, photons=100, base=object())
+    assert calls == [2, 6, 6]
+
+
+def test_prior_holds_a_parameter_near_its_start(fake):
+    """With the Poisson likelihood, a tight prior on ln(b / b0) keeps b near its start (g
+    takes up the product b g the toy sees); a flat one lets b move."""
+    target = np.array([[11.0, 0.12, 0.45, 0.88, 0.22, 0.30]])
+    kw = dict(iters=300, lr=2e-2, photons=100, peak=1e6, base=object(), loss="poisson")
+    flat = inversion.fit(target, **kw)
+    tight = inversion.fit(target, prior_sigma=[None, None, 1e-5, None, None, None], **kw)
+    b0 = inversion.INITIAL[2]
+    assert abs(tight["params"][0, 2] / b0 - 1.0) < 0.05, tight["params"]
+    assert abs(flat["params"][0, 2] / b0 - 1.0) > 0.15, flat["params"]
+    with pytest.raises(ValueError):
+        inversion.fit(target, prior_sigma=[0.0] * 6, **kw)
