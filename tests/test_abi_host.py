@@ -178,3 +178,43 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_native, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _native.load_library(str(tmp_path / "absent.so"))
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """A plain C11 program includes the header, takes the address of every declared entry
+    point and links against the library (so each declaration names an exported C symbol),
+    then prints the batch structs' layout, which must equal the ctypes mirror."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    from pyalbsim_gb300._native import AlbBatchInstance, AlbBatchOptions
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = build_library()
+    fns = declared_functions()
+    src = ["#include <stddef.h>", "#include <stdio.h>", '#include "albgpu.h"', "int main(void) {"]
+    src.append("    void (*volatile fn)(void);")
+    for f in fns:  # a volatile function pointer keeps each reference to the symbol
+        src += [f"    fn = (void (*)(void)){f};", '    printf("%d\\n", fn != 0);']
+    src.append('    printf("%zu %zu\\n", sizeof(AlbBatchInstance), sizeof(AlbBatchOptions));')
+    for name, _ in AlbBatchInstance._fields_:
+        src.append(f'    printf("%zu\\n", offsetof(AlbBatchInstance, {name}));')
+    for name, _ in AlbBatchOptions._fields_:
+        src.append(f'    printf("%zu\\n", offsetof(AlbBatchOptions, {name}));')
+    src += ["    return 0;", "}"]
+    c_file = tmp_path / "abi.c"
+    c_file.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "abi"
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-I", INCLUDE, str(c_file), lib,
+                        f"-Wl,-rpath,{os.path.dirname(lib)}", "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out[:len(fns)] == ["1"] * len(fns)
+    rest = [int(x) for x in out[len(fns):]]
+    assert rest[:2] == [ctypes.sizeof(AlbBatchInstance), ctypes.sizeof(AlbBatchOptions)]
+    expect = [getattr(AlbBatchInstance, n).offset for n, _ in AlbBatchInstance._fields_]
+    expect += [getattr(AlbBatchOptions, n).offset for n, _ in AlbBatchOptions._fields_]
+    assert rest[2:] == expect
