@@ -43,10 +43,14 @@ class GpuEngine:
         self.config = simulation_config
         self.scene = build_scene(simulation_config)
         self.ctx = NativeContext(self.scene, device=self.options.device)
-        self.ctx.set_option(ALB_OPT_SORT_QUERIES, 1 if self.options.sort_queries else 0)
-        self.ctx.set_option(ALB_OPT_PRECISE, 1 if self.options.precise else 0)
-        if self.options.adjoint:
-            self.ctx.set_option(ALB_OPT_ADJOINT, 1)
+        try:
+            self.ctx.set_option(ALB_OPT_SORT_QUERIES, 1 if self.options.sort_queries else 0)
+            self.ctx.set_option(ALB_OPT_PRECISE, 1 if self.options.precise else 0)
+            if self.options.adjoint:
+                self.ctx.set_option(ALB_OPT_ADJOINT, 1)
+        except Exception:
+            self.ctx.close()  # e.g. the adjoint refused on depth-profiled layers
+            raise
         self.n_forward = 0
         self.n_backward = 0
         self._maps_stale = True
@@ -114,3 +118,10 @@ class GpuEngine:
 
     def close(self):
         self.ctx.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False

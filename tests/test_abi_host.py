@@ -218,3 +218,34 @@ def test_header_compiles_as_c_and_links(tmp_path):
     expect = [getattr(AlbBatchInstance, n).offset for n, _ in AlbBatchInstance._fields_]
     expect += [getattr(AlbBatchOptions, n).offset for n, _ in AlbBatchOptions._fields_]
     assert rest[2:] == expect
+
+
+def test_engine_closes_its_context(monkeypatch):
+    """GpuEngine is a context manager, and a context whose options are refused at creation
+    (the adjoint on depth-profiled layers) is released before the error propagates."""
+    from pyalbsim_gb300 import engine as eng_mod
+    from pyalbsim_gb300.config.gpu import GpuRunOptions
+
+    closed = []
+
+    class FakeContext:
+        def __init__(self, scene, device=0):
+            self.scene = scene
+
+        def set_option(self, key, value):
+            if key == eng_mod.ALB_OPT_ADJOINT:
+                raise ValueError("the adjoint needs constant layers")
+
+        def close(self):
+            closed.append(True)
+
+    monkeypatch.setattr(eng_mod, "NativeContext", FakeContext)
+    from fixtures import config_from_fixture, load
+
+    cfg = config_from_fixture(load("replay_small.npz"))
+    with eng_mod.GpuEngine(cfg) as e:
+        assert isinstance(e.ctx, FakeContext)
+    assert closed == [True]
+    with pytest.raises(ValueError):
+        eng_mod.GpuEngine(cfg, GpuRunOptions(adjoint=True))
+    assert closed == [True, True]
