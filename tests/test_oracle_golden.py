@@ -201,3 +201,15 @@ def test_bench_geometry_replay_matches_reference_photon_by_photon():
         den = np.abs(ref).sum()
         if den:
             assert np.abs(r["waveform"][c] - ref).sum() / den < 1e-4, c
+
+
+def test_oracle_edge_cases_zero_photons_and_empty_maps():
+    """No photons trace to an all-zero waveform; backward photons against empty maps, or
+    maps with fewer than k records, raise IndexError (the reference's KDTree quirk)."""
+    cfg = config_from_fixture(load("replay_small.npz"))
+    scene = build_scene(cfg)
+    assert not oracle_run(scene, 0, 0, seed=1)["waveform"].any()
+    assert not oracle_run(scene, 50, 0, seed=1)["waveform"].any()
+    for nf in (0, 5):
+        with pytest.raises(IndexError):
+            oracle_run(scene, nf, 10, seed=1)
