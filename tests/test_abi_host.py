@@ -249,3 +249,17 @@ def test_engine_closes_its_context(monkeypatch):
     with pytest.raises(ValueError):
         eng_mod.GpuEngine(cfg, GpuRunOptions(adjoint=True))
     assert closed == [True, True]
+
+
+def test_integration_examples_compile_and_name_real_entry_points():
+    """The Python examples in INTEGRATION.md are valid Python, and every ``lib.alb_*`` they
+    call is an entry point the header declares."""
+    path = os.path.join(os.path.dirname(INCLUDE), "INTEGRATION.md")
+    text = open(path).read()
+    blocks = re.findall(r"```python\n(.*?)```", text, flags=re.S)
+    assert blocks
+    declared = set(declared_functions())
+    for b in blocks:
+        compile(b, "INTEGRATION.md", "exec")
+        used = set(re.findall(r"\blib\.(alb_[a-z0-9_]+)", b))
+        assert used <= declared, used - declared
