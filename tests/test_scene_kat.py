@@ -149,3 +149,32 @@ def test_profiled_attenuation_lut_matches_reference():
         np.testing.assert_array_equal(layer.lut_z, d[f"lut{i}_z"])
         np.testing.assert_array_equal(layer.lut_alpha, d[f"lut{i}_alpha"])
     assert n == 2
+
+
+def test_fast_tracer_free_paths_at_the_bench_geometry():
+    """The float32 tracer takes ceil((tau* - tau) / inc) steps to the next scatter, while the
+    reference accumulates tau <- fl32(fl64(tau) + inc) step by step, whose rounding is a
+    fixed fraction of an ulp inside each binade of tau. At the large scene's attenuation and
+    step length (inc ~ 4.9e-4) the two step counts agree to 1e-4 in the mean over
+    exponential tau* (measured 1.5e-5 at 2e5 samples), far below one integrator step over a
+    20 m path."""
+    from pyalbsim_gb300.workloads import large
+
+    sc = build_scene(large())
+    L = sc.layers[0]
+    inc = np.float32(np.float32(L.alpha32) * np.float32(np.float32(L.speed32) * np.float32(sc.dt)))
+    rng = np.random.default_rng(1)
+    taut = (-np.log(rng.random(20000).astype(np.float32))).astype(np.float32)
+    tau = np.zeros_like(taut)
+    steps = np.zeros(len(taut), np.int64)
+    active = np.ones(len(taut), bool)
+    for _ in range(200000):
+        if not active.any():
+            break
+        tau[active] = (tau[active].astype(np.float64) + np.float64(inc)).astype(np.float32)
+        steps[active] += 1
+        active &= ~(tau >= taut)
+    assert not active.any()
+    closed = np.maximum(np.ceil(taut.astype(np.float64) / np.float64(inc)).astype(np.int64), 1)
+    assert abs(steps.sum() / closed.sum() - 1.0) < 1e-4
+    assert np.abs(steps - closed).max() <= 0.005 * closed.max()
