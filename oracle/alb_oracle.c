@@ -24,6 +24,14 @@
  * Positions and directions are float64, energies and optical depths float32, matching the
  * dtypes the reference's arrays carry. Variates come either from a recorded replay
  * stream or from the same Philox4x32-10 streams and transforms the GPU uses.
+ *
+ * Pinned against the reference itself: tests/golden/make_golden.py runs the reference and
+ * records its variates, photon maps, gather queries, waveforms, KDTree answers, 32-run
+ * statistics and its own finite differences in albedo and roughness; the tests hold this
+ * restatement to those fixtures record by record. The extensions the reference lacks
+ * (path scores and the Jacobian, Henyey-Greenstein phase, fixed-radius gather, gated
+ * windows, Gaussian surface slopes) are restated here from their definitions and pinned
+ * by closed forms and differences instead.
  */
 #include <float.h>
 #include <math.h>
