@@ -237,6 +237,7 @@ def main():
                    "parallelism": f"replicas x{world}", "l2": "working set of GBs per step, far above L2"},
         "phases_ms_per_step": {p: v[0] / args.steps for p, v in phases.items()},
         "gathers_per_step": int(n_gathers / args.steps),
+        "gathers_per_s": world * (n_gathers / args.steps) / (ms_step / 1e3),
         "dominant_phase": top,
         "roofline": {"bound": "hbm", "kernel": "k_gather<1, 0> (scatter map, k-NN)", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak if peak else None,
