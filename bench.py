@@ -9,7 +9,8 @@ FOV 50 mrad, 0.05 ns bins, 1e8 forward photons, Philox seed 1).
 
 Prints one JSON line (rank 0). ``--impl reference`` times the CPU restatement of the
 reference's algorithm (the oracle, all host threads) on a bounded sample of the same
-workload instead.
+workload instead, and once, on a fixed subset, the reference's own ``run_linear`` and
+``run_parallel`` (installed unmodified under ``baseline/_ref``).
 """
 
 from __future__ import annotations
@@ -106,7 +107,8 @@ def measured(fn, *args):
 
 
 def cpu_oracle_rate(cfg, nf, nb, seed, threads):
-    """(photons/s, seconds) of the oracle on nf forward + nb backward photons."""
+    """(photons/s, seconds) of the oracle on nf forward + nb backward photons (its k-d tree
+    neighbour search, the exact answer scipy's KDTree gives the reference)."""
     from oracle.oracle import oracle_run
     from pyalbsim_gb300.scene import build_scene
 
@@ -115,6 +117,110 @@ def cpu_oracle_rate(cfg, nf, nb, seed, threads):
     oracle_run(scene, nf, nb, seed=seed, threads=threads)
     dt = time.perf_counter() - t0
     return (nf + nb) / dt, dt
+
+
+def cpu_model() -> str:
+    """Host CPU model (lscpu's model name; /proc/cpuinfo or the platform as fallbacks)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline_port(cfg, ns, threads):
+    """The oracle on two sample sizes of the workload (ns/2 and ns forward photons, a quarter
+    as many backward): photons/s of the larger and the ratio of the two rates, which shows
+    whether the figure is a per-photon rate or depends on the sample chosen."""
+    small_rate, small_dt = cpu_oracle_rate(cfg, ns // 2, max(ns // 8, 1), 8, threads)
+    rate, dt = cpu_oracle_rate(cfg, ns, max(ns // 4, 1), 7, threads)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "model": cpu_model(),
+            "sample": f"{ns} forward + {max(ns // 4, 1)} backward photons ({dt:.1f} s), oracle/alb_oracle.c "
+                      "(exact k-d tree k-NN)",
+            "rate_at_half_sample": small_rate, "rate_ratio_full_over_half": rate / small_rate}
+
+
+def _reference_config(cfg):
+    """The reference's own SimulationConfig with the same field values as ``cfg`` (a
+    configuration of this package's drop-in classes; the extension fields, absent from the
+    reference, must be unset)."""
+    import dataclasses
+    import importlib
+
+    classes = {}
+    for mod in ("laser", "scene", "sensor", "sea_floor", "sea_surface", "heatmap", "water", "simulation", "run"):
+        m = importlib.import_module(f"alb_sim.config.{mod}")
+        classes.update({n: getattr(m, n) for n in dir(m) if dataclasses.is_dataclass(getattr(m, n))})
+    prof = importlib.import_module("alb_sim.utils.parameter_profile")
+    classes.update({n: getattr(prof, n) for n in ("LinearParameter", "ExponentialParameter")})
+
+    def conv(obj):
+        if dataclasses.is_dataclass(obj):
+            cls = classes[type(obj).__name__]
+            names = {f.name for f in dataclasses.fields(cls) if f.init}
+            for f in dataclasses.fields(obj):
+                if f.name not in names and f.init and getattr(obj, f.name) is not None:
+                    raise ValueError(f"{type(obj).__name__}.{f.name} has no counterpart in the reference")
+            return cls(**{f.name: conv(getattr(obj, f.name)) for f in dataclasses.fields(obj) if f.name in names})
+        if isinstance(obj, tuple):
+            return tuple(conv(x) for x in obj)
+        return obj
+
+    return conv(cfg)
+
+
+def reference_python_rates(cfg, nf_linear, nb_linear, nf_parallel, nb_parallel, processes):
+    """The reference's own CPU path, installed unmodified under baseline/_ref, on a fixed
+    subset of the workload: ``run_linear`` (one process) and ``run_parallel`` (``processes``
+    worker processes, one forward and one backward batch each; ``multiprocess`` is not
+    installed, so the standard library's ``multiprocessing`` stands in for it). Photons/s of
+    each; the workload's 1e8 + 2.5e7 photons would take the time these rates extrapolate to."""
+    import contextlib
+    import io
+    import multiprocessing
+
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "alb_sim")):
+        return {"unavailable": "the reference is not installed under baseline/_ref"}
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    sys.modules.setdefault("multiprocess", multiprocessing)
+    from alb_sim.config.run import RunConfig
+    from alb_sim.execution.linear import run_linear
+    from alb_sim.execution.parallel import run_parallel
+
+    rcfg = _reference_config(cfg)
+    out = {"model": cpu_model(), "code": "alb_sim (baseline/_ref), unmodified", "extrapolated": True}
+    rc = RunConfig(photons_per_batch_forward=nf_linear, photons_per_batch_backward=nb_linear, batches_forward=1,
+                   batches_backward=1)
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        run_linear(rcfg, rc, rng=np.random.default_rng(5))
+    dt = time.perf_counter() - t0
+    out["run_linear"] = {"value": (nf_linear + nb_linear) / dt, "unit": UNIT, "cores": 1, "seconds": dt,
+                         "sample": f"{nf_linear} forward + {nb_linear} backward photons"}
+    rc = RunConfig(processes=processes, photons_per_batch_forward=nf_parallel,
+                   photons_per_batch_backward=nb_parallel, batches_forward=processes, batches_backward=processes)
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        run_parallel(rcfg, rc, seed=None)  # a fixed seed would make every batch identical
+    dt = time.perf_counter() - t0
+    n = processes * (nf_parallel + nb_parallel)
+    out["run_parallel"] = {"value": n / dt, "unit": UNIT, "cores": processes, "seconds": dt,
+                           "sample": f"{processes} x ({nf_parallel} forward + {nb_parallel} backward) photons"}
+    return out
 
 
 def run_reference(args):
@@ -141,11 +247,17 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload_label, "sample_forward_photons": nf, "sample_backward_photons": nb},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "model": cpu_model(),
                          "sample": f"{nf} forward + {nb} backward photons of the workload per step, "
-                                   "step-by-step C restatement of the reference (oracle/alb_oracle.c)"},
+                                   "step-by-step C restatement of the reference with an exact k-d tree "
+                                   "k-NN (oracle/alb_oracle.c)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_reference_python:
+        # the reference's own Python path, once, on a fixed subset (not part of `value`)
+        line["reference_python"] = measured(
+            reference_python_rates, cfg, args.ref_linear_photons, max(args.ref_linear_photons // 4, 1),
+            args.ref_parallel_photons, max(args.ref_parallel_photons // 4, 1), threads)
     print(json.dumps(line), flush=True)
 
 
@@ -157,8 +269,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large", choices=["large", "small"])
     ap.add_argument("--photons", type=float, default=1e8, help="forward photons per step (backward = 1/4)")
-    ap.add_argument("--ref-photons", type=int, default=20000)
-    ap.add_argument("--cpu-sample", type=int, default=40000)
+    ap.add_argument("--ref-photons", type=int, default=40000)
+    ap.add_argument("--ref-linear-photons", type=int, default=1000,
+                    help="forward photons of the reference's own run_linear (at least k records per map)")
+    ap.add_argument("--ref-parallel-photons", type=int, default=250,
+                    help="forward photons per worker of the reference's own run_parallel")
+    ap.add_argument("--no-reference-python", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=60000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-gradients", action="store_true")
     ap.add_argument("--grad-photons", type=float, default=1e7)
@@ -262,11 +379,7 @@ def main():
     if rank == 0:
         # CPU baseline: the oracle on a bounded sample of the same workload, all host threads
         threads = os.cpu_count() or 1
-        ns = args.cpu_sample
-        rate, dt = cpu_oracle_rate(cfg, ns, max(ns // 4, 1), 7, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{ns} forward + {max(ns // 4, 1)} backward photons ({dt:.1f} s), "
-                                          "oracle/alb_oracle.c"}
+        line["cpu_baseline"] = cpu_baseline_port(cfg, args.cpu_sample, threads)
         if not args.no_e2e:
             line["e2e"] = measured(e2e_measure, cfg, nf, nb)
         if not args.no_gradients:

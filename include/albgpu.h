@@ -228,7 +228,10 @@ int alb_knn(AlbCtx* ctx, const float* points, uint64_t m, const double* queries,
  * k <= 256, larger inputs are rejected with ALB_ERR_INVALID. The first call on a device
  * resolves the array's address (make it before any stream capture); calls that overlap
  * on the GPU share the array and race. Asynchronous on `stream`; the message of a failed
- * call is alb_last_error(NULL). */
+ * call is alb_last_error(NULL). The call returns before the GPU has run, so a query the
+ * search could not answer (NaN or infinite coordinates, or a traversal that hit its
+ * iteration cap) is reported in the output instead: all k of its slots hold index -1 and
+ * distance NaN. */
 #define ALB_NOALLOC_MAX_POINTS 4096
 int alb_knn_noalloc(const float* points_dev, uint64_t m, const double* queries_dev, uint64_t q, int k,
                     int32_t* idx_dev, double* dist_dev, void* stream);

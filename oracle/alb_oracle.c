@@ -733,22 +733,210 @@ static void knn_brute(const float* pts, int64_t m, const double q[3], int k, Can
     qsort(out, (size_t)k, sizeof(Cand), cand_cmp);
 }
 
+/* k-d tree over the float32 points of a map, for the exact k-NN the reference takes from
+ * scipy's KDTree (photon_mapping/photon_map_index.py:17, core/simulation.py:139-142). It
+ * returns what knn_brute returns: the k smallest (float64 squared distance, index) pairs,
+ * sorted. A point replaces the current k-th when its pair is smaller, and a subtree is
+ * skipped only when the float64 lower bound of its box is strictly above the k-th distance
+ * (the bound is formed with the same operations as a point's distance, so rounding keeps it
+ * at or below the distance of every point inside). Ties at the k-th distance therefore go
+ * to the smaller index, whatever order the tree visits the points in. */
+#define KD_LEAF 16
+typedef struct {
+    int32_t* perm;
+    int64_t nnodes, cap;
+    float* box;       /* 6 per node: lo xyz, hi xyz */
+    int64_t* range;   /* 2 per node: begin, end in perm */
+    int64_t* child;   /* 2 per node: left, right (-1: leaf) */
+} KdTree;
+
+static double coord(const float* pts, int32_t i, int a) { return (double)pts[3 * (int64_t)i + a]; }
+
+static void kd_select(const float* pts, int32_t* v, int64_t lo, int64_t hi, int64_t nth, int a) {
+    /* quickselect: v[nth] in sorted position by (coordinate a, index) */
+    while (hi - lo > 1) {
+        int32_t pv = v[lo + (hi - lo) / 2];
+        double pc = coord(pts, pv, a);
+        int64_t i = lo, j = hi - 1;
+        while (i <= j) {
+            while (coord(pts, v[i], a) < pc || (coord(pts, v[i], a) == pc && v[i] < pv)) ++i;
+            while (coord(pts, v[j], a) > pc || (coord(pts, v[j], a) == pc && v[j] > pv)) --j;
+            if (i <= j) {
+                int32_t t = v[i];
+                v[i] = v[j];
+                v[j] = t;
+                ++i;
+                --j;
+            }
+        }
+        if (nth <= j) hi = j + 1;
+        else if (nth >= i) lo = i;
+        else return;
+    }
+}
+
+static int64_t kd_build_node(KdTree* t, const float* pts, int64_t b, int64_t e) {
+    if (t->nnodes == t->cap) {
+        t->cap *= 2;
+        t->box = (float*)realloc(t->box, (size_t)t->cap * 6 * sizeof(float));
+        t->range = (int64_t*)realloc(t->range, (size_t)t->cap * 2 * sizeof(int64_t));
+        t->child = (int64_t*)realloc(t->child, (size_t)t->cap * 2 * sizeof(int64_t));
+    }
+    int64_t id = t->nnodes++;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = b; i < e; ++i)
+        for (int a = 0; a < 3; ++a) {
+            float v = pts[3 * (int64_t)t->perm[i] + a];
+            if (v < lo[a]) lo[a] = v;
+            if (v > hi[a]) hi[a] = v;
+        }
+    for (int a = 0; a < 3; ++a) {
+        t->box[6 * id + a] = lo[a];
+        t->box[6 * id + 3 + a] = hi[a];
+    }
+    t->range[2 * id] = b;
+    t->range[2 * id + 1] = e;
+    t->child[2 * id] = t->child[2 * id + 1] = -1;
+    if (e - b > KD_LEAF) {
+        int ax = 0;
+        for (int a = 1; a < 3; ++a)
+            if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+        int64_t mid = b + (e - b) / 2;
+        kd_select(pts, t->perm, b, e, mid, ax);
+        int64_t l = kd_build_node(t, pts, b, mid);
+        int64_t r = kd_build_node(t, pts, mid, e);
+        t->child[2 * id] = l;
+        t->child[2 * id + 1] = r;
+    }
+    return id;
+}
+
+static KdTree* kd_build(const float* pts, int64_t m) {
+    KdTree* t = (KdTree*)calloc(1, sizeof(KdTree));
+    t->perm = (int32_t*)malloc((size_t)(m > 0 ? m : 1) * sizeof(int32_t));
+    for (int64_t i = 0; i < m; ++i) t->perm[i] = (int32_t)i;
+    t->cap = 64;
+    t->box = (float*)malloc((size_t)t->cap * 6 * sizeof(float));
+    t->range = (int64_t*)malloc((size_t)t->cap * 2 * sizeof(int64_t));
+    t->child = (int64_t*)malloc((size_t)t->cap * 2 * sizeof(int64_t));
+    if (m > 0) kd_build_node(t, pts, 0, m);
+    return t;
+}
+
+static void kd_free(KdTree* t) {
+    if (!t) return;
+    free(t->perm);
+    free(t->box);
+    free(t->range);
+    free(t->child);
+    free(t);
+}
+
+static double kd_box_d2(const KdTree* t, int64_t node, const double q[3]) {
+    double g[3];
+    for (int a = 0; a < 3; ++a) {
+        double lo = (double)t->box[6 * node + a] - q[a], hi = q[a] - (double)t->box[6 * node + 3 + a];
+        g[a] = lo > 0.0 ? lo : (hi > 0.0 ? hi : 0.0);
+    }
+    return (g[0] * g[0] + g[1] * g[1]) + g[2] * g[2];
+}
+
+static void kd_knn_node(const KdTree* t, const float* pts, int64_t node, const double q[3], int k, Cand* h, int* n) {
+    if (t->child[2 * node] < 0) {
+        for (int64_t i = t->range[2 * node]; i < t->range[2 * node + 1]; ++i) {
+            const int32_t j = t->perm[i];
+            double dx = (double)pts[3 * (int64_t)j] - q[0], dy = (double)pts[3 * (int64_t)j + 1] - q[1],
+                   dz = (double)pts[3 * (int64_t)j + 2] - q[2];
+            double d2 = (dx * dx + dy * dy) + dz * dz;
+            if (*n < k) {
+                h[*n].d2 = d2;
+                h[*n].i = j;
+                ++*n;
+                if (*n == k)
+                    for (int s = k / 2 - 1; s >= 0; --s) heap_down(h, k, s);
+            } else if (d2 < h[0].d2 || (d2 == h[0].d2 && j < h[0].i)) {
+                h[0].d2 = d2;
+                h[0].i = j;
+                heap_down(h, k, 0);
+            }
+        }
+        return;
+    }
+    int64_t c0 = t->child[2 * node], c1 = t->child[2 * node + 1];
+    double b0 = kd_box_d2(t, c0, q), b1 = kd_box_d2(t, c1, q);
+    if (b1 < b0) {
+        int64_t tc = c0;
+        c0 = c1;
+        c1 = tc;
+        double tb = b0;
+        b0 = b1;
+        b1 = tb;
+    }
+    if (*n < k || b0 <= h[0].d2) kd_knn_node(t, pts, c0, q, k, h, n);
+    if (*n < k || b1 <= h[0].d2) kd_knn_node(t, pts, c1, q, k, h, n);
+}
+
+/* Exact k nearest through the tree, sorted ascending (the same array knn_brute gives). */
+static void knn_tree(const KdTree* t, const float* pts, const double q[3], int k, Cand* out) {
+    int n = 0;
+    kd_knn_node(t, pts, 0, q, k, out, &n);
+    qsort(out, (size_t)k, sizeof(Cand), cand_cmp);
+}
+
+/* Every point with float64 squared distance <= R2, in ascending index order (the order the
+ * brute-force scan produces, so float64 sums over them are unchanged). */
+static int cand_idx_cmp(const void* a, const void* b) {
+    const Cand* x = (const Cand*)a;
+    const Cand* y = (const Cand*)b;
+    return (x->i > y->i) - (x->i < y->i);
+}
+static void kd_range_node(const KdTree* t, const float* pts, int64_t node, const double q[3], double R2, Cand** c,
+                          int64_t* cnt, int64_t* cap) {
+    if (kd_box_d2(t, node, q) > R2) return;
+    if (t->child[2 * node] < 0) {
+        for (int64_t i = t->range[2 * node]; i < t->range[2 * node + 1]; ++i) {
+            const int32_t j = t->perm[i];
+            double dx = (double)pts[3 * (int64_t)j] - q[0], dy = (double)pts[3 * (int64_t)j + 1] - q[1],
+                   dz = (double)pts[3 * (int64_t)j + 2] - q[2];
+            if ((dx * dx + dy * dy) + dz * dz <= R2) {
+                if (*cnt == *cap) {
+                    *cap *= 2;
+                    *c = (Cand*)realloc(*c, (size_t)*cap * sizeof(Cand));
+                }
+                (*c)[*cnt].i = j;
+                (*c)[*cnt].d2 = 0.0;
+                ++*cnt;
+            }
+        }
+        return;
+    }
+    kd_range_node(t, pts, t->child[2 * node], q, R2, c, cnt, cap);
+    kd_range_node(t, pts, t->child[2 * node + 1], q, R2, c, cnt, cap);
+}
+
+/* 1: every k-NN and radius query scans all points (the checker); 0: the k-d tree. */
+static int g_knn_brute = 0;
+void oracle_set_knn_brute(int on) { g_knn_brute = on; }
+
 int oracle_knn(const float* pts, int64_t m, const double* qs, int64_t nq, int k, int32_t* idx, double* dist,
                int threads) {
     if (m < k) return ALB_ERR_TOO_FEW;
+    KdTree* tree = g_knn_brute ? NULL : kd_build(pts, m);
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 8)
 #endif
     for (int64_t i = 0; i < nq; ++i) {
         Cand* c = (Cand*)malloc((size_t)k * sizeof(Cand));
-        knn_brute(pts, m, qs + 3 * i, k, c);
+        if (tree) knn_tree(tree, pts, qs + 3 * i, k, c);
+        else knn_brute(pts, m, qs + 3 * i, k, c);
         for (int j = 0; j < k; ++j) {
             idx[i * k + j] = c[j].i;
             dist[i * k + j] = sqrt(c[j].d2);
         }
         free(c);
     }
+    kd_free(tree);
     return 0;
 }
 
@@ -851,6 +1039,7 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
     const size_t stride = (size_t)nb + 2 * hb + (size_t)nj * nb;
     double* priv = (double*)calloc((size_t)nthreads * stride, sizeof(double));
     int err = 0;
+    KdTree* tree = (g_knn_brute || nq == 0 || m == 0) ? NULL : kd_build(mpos, m);
 #ifdef _OPENMP
 #pragma omp parallel
 #endif
@@ -876,7 +1065,11 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
             if (R > 0.0) {
                 /* every record with float64 squared distance <= R^2 */
                 cnt = 0;
-                for (int64_t j = 0; j < m; ++j) {
+                if (tree) {
+                    kd_range_node(tree, mpos, 0, x, R * R, &c, &cnt, &ccap);
+                    qsort(c, (size_t)cnt, sizeof(Cand), cand_idx_cmp);
+                }
+                for (int64_t j = 0; j < m && !tree; ++j) {
                     double dx = (double)mpos[3 * j] - x[0], dy = (double)mpos[3 * j + 1] - x[1],
                            dz = (double)mpos[3 * j + 2] - x[2];
                     if ((dx * dx + dy * dy) + dz * dz <= R * R) {
@@ -890,7 +1083,8 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
                 }
                 r = R;
             } else {
-                knn_brute(mpos, m, x, k, c);
+                if (tree) knn_tree(tree, mpos, x, k, c);
+                else knn_brute(mpos, m, x, k, c);
                 r = sqrt(c[k - 1].d2);
             }
             if (rk_out) rk_out[q] = r;
@@ -976,6 +1170,7 @@ int oracle_gather(const AlbSceneParams* p, int channel, const float* mpos, const
             }
     }
     free(priv);
+    kd_free(tree);
     return err;
 }
 

@@ -94,6 +94,7 @@ def _load():
         lib.oracle_free.argtypes = [C.POINTER(_Trace)]
         lib.oracle_record_size.restype = C.c_int
         lib.oracle_knn.argtypes = [P, C.c_int64, P, C.c_int64, C.c_int, P, P, C.c_int]
+        lib.oracle_set_knn_brute.argtypes = [C.c_int]
         lib.oracle_gather.argtypes = [
             P, C.c_int, P, P, P, P, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P, P, P, P, P, C.c_int
         ]
@@ -101,6 +102,12 @@ def _load():
             raise RuntimeError("oracle record layout mismatch")
         _lib = lib
     return _lib
+
+
+def set_knn_brute(on: bool) -> None:
+    """Neighbour searches of the oracle scan every map point (True, the checker of the
+    tree) or descend its k-d tree (False, the default); both return the same neighbours."""
+    _load().oracle_set_knn_brute(1 if on else 0)
 
 
 def _p(a):

@@ -169,12 +169,13 @@ def config_from_sample(params: Dict[str, float], base=None):
 
 
 def run_hypercube(param_ranges: Dict[str, Tuple[float, float]], n_samples: int, run_config, seed: Optional[int] = None,
-                  base=None, streams: int = 8, device: int = 0) -> List[Dict]:
+                  base=None, streams: int = 8, device: int = 0, precise: bool = False) -> List[Dict]:
     """The hypercube sweep in one batched call: n_samples LatinHypercube(d) points scaled to
     ``param_ranges``, each simulated with the run_config's photon counts (forward batches x
     photons per batch, backward likewise) through alb_batch_run. Returns
     [{"params": dict, "waveform": {PhotonType: float32 array}}, ...] in sample order.
-    With ``seed`` the samples and every instance's Philox key are reproducible."""
+    With ``seed`` the samples and every instance's Philox key ((seed << 32) + sample index)
+    are reproducible. ``precise`` selects the float64-geometry tracer."""
     import secrets
 
     from scipy.stats import qmc
@@ -192,7 +193,7 @@ def run_hypercube(param_ranges: Dict[str, Tuple[float, float]], n_samples: int, 
     for i, p in enumerate(samples):
         key = ((int(seed) & 0xFFFFFFFF) << 32) + i if seed is not None else secrets.randbits(64)
         inst.append(Instance(config_from_sample(p, base), nf, nb, key, np.array(list(p.values()))))
-    w, _, st, _, _ = run_batch(inst, streams=streams, device=device)
+    w, _, st, _, _ = run_batch(inst, streams=streams, device=device, precise=precise)
     out = []
     for i, p in enumerate(samples):
         if st[i] != 0:

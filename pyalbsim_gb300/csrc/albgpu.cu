@@ -199,6 +199,8 @@ static int check_device(AlbCtx* ctx, const char* where) {
                            : h == ALB_ERR_REPLAY ? "a replay stream ran out of variates"
                            : h == ALB_ERR_TOO_FEW ? "a photon map holds fewer records than k"
                            : h == ALB_ERR_CAPACITY ? "a waveform bin index fell outside the waveform"
+                           : h == ALB_ERR_INVALID ? "a neighbour search admitted fewer than k finite points "
+                                                    "(NaN or infinite coordinates)"
                                                    : "device error";
         return fail(ctx, h, std::string(where) + ": " + what);
     }
@@ -1148,7 +1150,11 @@ extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* 
     launch_knn(map_dev(mi), dq, nq, k, di, dd, ctx->d_err, ctx->st);
     std::vector<int32_t> sorted_idx(nq * k);
     int rc = check_device(ctx, "knn");
-    if (rc) return rc;
+    if (rc) {
+        cudaFree(mi.a); cudaFree(mi.b); cudaFree(mi.box_lo); cudaFree(mi.box_hi);
+        ctx->ws.release(mark);
+        return rc;
+    }
     CK(cudaMemcpy(sorted_idx.data(), di, nq * k * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(dist, dd, nq * k * 8, cudaMemcpyDeviceToHost));
     std::vector<float4> sa(mi.n);  // the index may hold more slots than points

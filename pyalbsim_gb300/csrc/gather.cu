@@ -297,6 +297,9 @@ struct KnnResult {
     int nodes;     // internal nodes expanded
     int selects;   // candidate-buffer reductions
     int clipped;   // 1 if a buffer bound forced an inexact answer (mass ties)
+    int fail;      // 0, or why the search has no answer (s.ci is then not valid):
+                   // ALB_ERR_ITER_CAP (traversal guard) or ALB_ERR_INVALID (fewer than k
+                   // finite points admitted: a NaN or infinite query or map coordinates)
 };
 
 // float64 ranking of the band entries bi[0..nb) by (distance, tie key, map position); the
@@ -390,7 +393,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
     if (m.n_real < (uint64_t)k) return false;
     float thr = thr0;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
-    res.leaves = res.nodes = res.selects = res.clipped = 0;
+    res.leaves = res.nodes = res.selects = res.clipped = res.fail = 0;
     // A carried bound can only fail through a degenerate previous result (a clipped
     // boundary band); the search is then repeated without it.
     for (int attempt = 0; attempt < 2; ++attempt) {
@@ -419,7 +422,10 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         }
         int guard = 0;
         while (sp > 0) {
-            if (++guard > (1 << 22)) break;
+            if (++guard > (1 << 22)) {  // reported, never a silent partial answer
+                res.fail = ALB_ERR_ITER_CAP;
+                break;
+            }
             // the top 32 stack entries, one per lane (lane 0 = top)
             const int i = sp - 1 - l;
             uint32_t e = 0u;
@@ -513,8 +519,10 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 __syncwarp();
             }
         }
-        if (cnt >= k || thr0 == FLT_MAX) break;
+        if (res.fail || cnt >= k || thr0 == FLT_MAX) break;
     }
+    if (!res.fail && cnt < k) res.fail = ALB_ERR_INVALID;
+    if (res.fail) return true;
     double rk2;
     if (REFINE) {
         rk2 = select_refined(m, s, 0, cnt, k, qx, qy, qz, tie_rec, res.clipped);
@@ -714,7 +722,7 @@ ALB_DEVICE void warp_radius_visit(const MapDev& m, WarpSmem& s, double qx, doubl
     const double R2 = R * R;
     const float thr = __double2float_ru(R2) * (1.0f + 2.0f * kRelMargin);
     const float lo_band = __double2float_rd(R2) * (1.0f - 2.0f * kRelMargin);
-    res.leaves = res.nodes = res.selects = res.clipped = 0;
+    res.leaves = res.nodes = res.selects = res.clipped = res.fail = 0;
     res.rk2 = R2;
     res.rkf = (float)R;
     if (m.nlevels <= 0) return;  // an empty map contributes nothing
@@ -734,7 +742,7 @@ ALB_DEVICE void warp_radius_visit(const MapDev& m, WarpSmem& s, double qx, doubl
     uint64_t guard = 0;
     while (sp > 0) {
         if (++guard > boxes) {
-            res.clipped = 1;
+            res.fail = ALB_ERR_ITER_CAP;
             break;
         }
         --sp;
@@ -875,6 +883,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                         if (acc.hw_lo && m.fwi) heat_add(sc, m, acc, idx, c);
                     },
                     r);
+                if (r.fail) {
+                    if (l == 0) atomicCAS(err, 0, r.fail);
+                    failed = true;
+                    break;
+                }
                 st_leaves += r.leaves;
                 st_nodes += r.nodes;
                 st_inexact += r.clipped;
@@ -899,6 +912,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             if (!warp_knn<CHANNEL != ALB_SCATTER>(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0,
                                                    m.b, r)) {
                 if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
+                failed = true;
+                break;
+            }
+            if (r.fail) {  // no valid neighbour set: report it and stop this warp's work
+                if (l == 0) atomicCAS(err, 0, r.fail);
                 failed = true;
                 break;
             }
@@ -990,10 +1008,22 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const doubl
         double qx = qs[3 * qi], qy = qs[3 * qi + 1], qz = qs[3 * qi + 2];
         KnnResult r;
         const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+        int why = 0;
         if (!warp_knn<true>(m, s, k, qx, qy, qz, fx, fy, fz, (float)(qx - (double)fx), (float)(qy - (double)fy),
-                      (float)(qz - (double)fz), FLT_MAX, nullptr, r)) {
-            if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
-            return;
+                            (float)(qz - (double)fz), FLT_MAX, nullptr, r))
+            why = ALB_ERR_TOO_FEW;
+        else if (r.fail)
+            why = r.fail;
+        if (why) {
+            // a query without an answer gets index -1 and distance NaN in all its k slots,
+            // so no slot is left holding whatever the caller's buffer held before
+            if (l == 0) atomicCAS(err, 0, why);
+            for (int j = l; j < k; j += 32) {
+                out_idx[qi * k + j] = -1;
+                out_dist[qi * k + j] = __longlong_as_double(0x7ff8000000000000ll);
+            }
+            __syncwarp();
+            continue;
         }
         // float64 distances of the k neighbours, then rank-sort them (k <= kMaxK)
         for (int j = l; j < k; j += 32) {

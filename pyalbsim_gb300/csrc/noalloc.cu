@@ -71,16 +71,36 @@ __global__ void k_pack_points(const float* __restrict__ pts, uint32_t m, KnnScra
     }
 }
 
-// neighbour positions in the k-d ordered copy -> the caller's point indices
-__global__ void k_map_tags(int32_t* idx, uint64_t total, const KnnScratch* s) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
-        idx[i] = (int32_t)__float_as_uint(s->sorted[idx[i]].w);
+// neighbour positions in the k-d ordered copy -> the caller's point indices. A slot whose
+// position is not one of the P slots of the ordered copy, or whose tag is not one of the m
+// input points, is marked as failed (index -1, distance NaN) instead of being followed: the
+// search writes -1 for a query it could not answer, and this call cannot synchronise to
+// report the device-side status, so the marker is how a failure reaches the caller.
+__global__ void k_map_tags(int32_t* idx, double* dist, uint64_t total, uint32_t P, uint32_t m, const KnnScratch* s) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const int32_t j = idx[i];
+        uint32_t tag = 0xffffffffu;
+        if (j >= 0 && (uint32_t)j < P) tag = __float_as_uint(s->sorted[j].w);
+        if (tag < m) {
+            idx[i] = (int32_t)tag;
+        } else {
+            idx[i] = -1;
+            dist[i] = __longlong_as_double(0x7ff8000000000000ll);
+        }
+    }
 }
 
-KnnScratch* scratch_for_current_device(int* dev_out) {
+KnnScratch* scratch_for_current_device() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    *dev_out = dev;
+    const cudaError_t ge = cudaGetDevice(&dev);
+    if (ge != cudaSuccess) {
+        set_global_error(std::string("alb_knn_noalloc: no usable current device: ") + cudaGetErrorString(ge));
+        return nullptr;
+    }
+    if (dev < 0 || dev >= 64) {
+        set_global_error("alb_knn_noalloc: current device " + std::to_string(dev) + " is outside the 64 supported");
+        return nullptr;
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
@@ -116,12 +136,8 @@ extern "C" int alb_knn_noalloc(const float* points_dev, uint64_t m, const double
         return ALB_ERR_TOO_FEW;
     }
     if (q == 0) return ALB_OK;
-    int dev = 0;
-    KnnScratch* s = scratch_for_current_device(&dev);
-    if (!s) {
-        if (dev < 0 || dev >= 64) set_global_error("alb_knn_noalloc: no usable current device");
-        return ALB_ERR_CUDA;
-    }
+    KnnScratch* s = scratch_for_current_device();
+    if (!s) return ALB_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     // box tree shape of the padded point set
     const uint64_t P = (m + 31) / 32 * 32;
@@ -153,7 +169,8 @@ extern "C" int alb_knn_noalloc(const float* points_dev, uint64_t m, const double
         md.lvl_cnt[l] = lvl_cnt[l];
     }
     launch_knn(md, queries_dev, q, k, idx_dev, dist_dev, &s->err, st);
-    k_map_tags<<<(unsigned)std::min<uint64_t>((q * (uint64_t)k + 255) / 256, 65535), 256, 0, st>>>(idx_dev, q * (uint64_t)k, s);
+    k_map_tags<<<(unsigned)std::min<uint64_t>((q * (uint64_t)k + 255) / 256, 65535), 256, 0, st>>>(
+        idx_dev, dist_dev, q * (uint64_t)k, (uint32_t)P, (uint32_t)m, s);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

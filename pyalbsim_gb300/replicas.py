@@ -18,8 +18,12 @@ def rank_info() -> Tuple[int, int, int]:
 
 
 def replica_seed(base: int, rank: int, step: int = 0) -> int:
-    """Philox key of a rank's step: distinct per rank and per step, reproducible."""
-    return base + rank + 1000 * step
+    """Philox key of a rank's step: base, rank and step in separate bit fields of the 64-bit
+    key (base above bit 32, rank in bits 20..31, step below bit 20), so two different
+    (base, rank, step) triples never share a stream."""
+    if not (0 <= rank < (1 << 12) and 0 <= step < (1 << 20) and 0 <= base < (1 << 32)):
+        raise ValueError("replica_seed: base < 2^32, rank < 2^12 and step < 2^20 are required")
+    return (base << 32) | (rank << 20) | step
 
 
 def max_over_ranks(value: float, device: str = "cpu") -> float:

@@ -21,6 +21,18 @@ from pyalbsim_gb300.config.water import FournierForandConfig
 from pyalbsim_gb300.utils.parameter_profile import ExponentialParameter, LinearParameter
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def reference_src():
+    """Directory holding the reference's importable ``alb_sim`` package, or None: the
+    ``ALB_REFERENCE_SRC`` environment variable when it is set, else the copy installed into
+    ``baseline/_ref`` by ``python -m pip install --no-deps --target baseline/_ref <reference>``."""
+    env = os.environ.get("ALB_REFERENCE_SRC")
+    if env:
+        return env if os.path.isdir(os.path.join(env, "alb_sim")) else None
+    local = os.path.join(REPO, "baseline", "_ref")
+    return local if os.path.isdir(os.path.join(local, "alb_sim")) else None
 
 
 def load(name):

@@ -1,7 +1,8 @@
 """Generate the golden fixtures under tests/golden/ by running the reference simulator.
 
-Run in a container where the reference is importable (default path below, or
-``ALB_REFERENCE_SRC``). The GPU tests never run this script: the fixtures it writes
+Run where the reference is importable: ``ALB_REFERENCE_SRC`` names the directory that holds
+its ``alb_sim`` package, else the copy installed into ``baseline/_ref`` (``python -m pip
+install --no-deps --target baseline/_ref <reference checkout>``) is used. The GPU tests never run this script: the fixtures it writes
 are committed. Nothing here restates the reference's physics; the script only drives the
 reference's own objects and records what they do:
 
@@ -21,8 +22,9 @@ Fixtures:
                        waveforms of a small reference run
   knn.npz              scipy KDTree k-nearest-neighbour answers on clustered maps
   stats_small.npz      per-bin mean / standard error over independent reference runs
+  stats_cfg0.npz       the same for 32 run_linear calls at the config-0 geometry
 
-Usage: python tests/golden/make_golden.py [kat|replay|knn|stats|fd_ref|all]
+Usage: python tests/golden/make_golden.py [kat|replay|knn|stats|stats_cfg0|fd_ref|all]
 """
 
 from __future__ import annotations
@@ -35,8 +37,11 @@ from types import SimpleNamespace
 
 import numpy as np
 
-REF_SRC = os.environ.get("ALB_REFERENCE_SRC", "/root/reference/src")
 OUT_DIR = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = os.environ.get("ALB_REFERENCE_SRC") or os.path.join(
+    os.path.dirname(os.path.dirname(OUT_DIR)), "baseline", "_ref")
+if not os.path.isdir(os.path.join(REF_SRC, "alb_sim")):
+    sys.exit(f"make_golden: no alb_sim package under {REF_SRC}; set ALB_REFERENCE_SRC")
 
 sys.path.insert(0, REF_SRC)
 sys.modules.setdefault("multiprocess", multiprocessing)
@@ -753,6 +758,46 @@ def make_stats(runs=32, nf=3000, nb=750):
     print("stats written")
 
 
+def _stats_cfg0_worker(args):
+    seed, nf, nb = args
+    import contextlib
+    import io
+
+    from alb_sim.config.run import RunConfig
+    from alb_sim.execution.linear import run_linear
+
+    rc = RunConfig(photons_per_batch_forward=nf, photons_per_batch_backward=nb, batches_forward=1,
+                   batches_backward=1)
+    with contextlib.redirect_stdout(io.StringIO()):
+        w = run_linear(config0_geometry(), rc, rng=np.random.default_rng(seed))
+    return np.stack([w[t] for t in TYPES]).astype(np.float64)
+
+
+def make_stats_cfg0(runs=32, nf=8000, nb=2000):
+    """Independent runs of the reference's own ``run_linear`` at the config-0 geometry
+    (seeds 0 .. runs-1, one forward and one backward batch each). Only the window of bins
+    that any run populates is stored (as float32, the reference's waveform type)."""
+    with multiprocessing.get_context("spawn").Pool(os.cpu_count()) as pool:
+        waves = pool.map(_stats_cfg0_worker, [(r, nf, nb) for r in range(runs)])
+    w = np.stack(waves)
+    nz = np.nonzero(np.any(w != 0, axis=(0, 1)))[0]
+    lo, hi = int(nz[0]), int(nz[-1]) + 1
+    w = w[:, :, lo:hi] / (nf * nb)  # reference units scale with N_f * N_b
+    np.savez_compressed(
+        os.path.join(OUT_DIR, "stats_cfg0.npz"),
+        mean=w.mean(0),
+        se=w.std(0, ddof=1) / np.sqrt(runs),
+        per_run=w.astype(np.float32),
+        bin0=lo,
+        nbins=int(np.shape(waves[0])[1]),
+        runs=runs,
+        n_fwd=nf,
+        n_bwd=nb,
+        **config_fields(config0_geometry()),
+    )
+    print("stats_cfg0 written", lo, hi)
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
     if what in ("kat", "all"):
@@ -769,3 +814,5 @@ if __name__ == "__main__":
         make_fd_ref()
     if what in ("stats", "all"):
         make_stats()
+    if what in ("stats_cfg0", "all"):
+        make_stats_cfg0()

@@ -12,6 +12,7 @@ import pytest
 
 from pyalbsim_gb300 import config as cfgmod
 from pyalbsim_gb300.build import INCLUDE, build_library
+from fixtures import reference_src
 
 HEADER = os.path.join(INCLUDE, "albgpu.h")
 
@@ -83,8 +84,9 @@ def test_config_validation_like_reference():
     assert isinstance(layer.salinity, float) and layer.num_sublayers == 60
 
 
-# reference sources for the config-field comparison (present only where the fixtures are made)
-REF_SRC = os.environ.get("ALB_REFERENCE_SRC", "/root/reference/src")
+# reference sources for the config-field comparison (present only where the reference is
+# installed or named by ALB_REFERENCE_SRC; the comparison is skipped elsewhere)
+REF_SRC = reference_src() or ""
 
 
 # Fields with no counterpart in the reference, appended after its own and defaulting to
@@ -106,7 +108,7 @@ def _drop_extensions(v):
     return v
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
 def test_config_fields_and_defaults_equal_reference():
     sys.path.insert(0, REF_SRC)
     import importlib
@@ -139,7 +141,7 @@ def test_config_fields_and_defaults_equal_reference():
                 assert rv == ov, (name, k)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
 def test_scene_accepts_reference_config_objects():
     sys.path.insert(0, REF_SRC)
     from alb_sim.config.simulation import SimulationConfig as RefCfg
@@ -251,15 +253,17 @@ def test_engine_closes_its_context(monkeypatch):
     assert closed == [True, True]
 
 
+INTEGRATION_GUIDE = os.path.join(os.path.dirname(INCLUDE), "INTEGRATION.md")
+
+
 def test_integration_examples_compile_and_name_real_entry_points():
-    """The Python examples in INTEGRATION.md are valid Python, and every ``lib.alb_*`` they
-    call is an entry point the header declares."""
-    path = os.path.join(os.path.dirname(INCLUDE), "INTEGRATION.md")
-    text = open(path).read()
+    """The Python examples of the integration guide at the repository root are valid
+    Python, and every ``lib.alb_*`` they call is an entry point the header declares."""
+    text = open(INTEGRATION_GUIDE).read()
     blocks = re.findall(r"```python\n(.*?)```", text, flags=re.S)
     assert blocks
     declared = set(declared_functions())
     for b in blocks:
-        compile(b, "INTEGRATION.md", "exec")
+        compile(b, "integration-guide example", "exec")
         used = set(re.findall(r"\blib\.(alb_[a-z0-9_]+)", b))
         assert used <= declared, used - declared

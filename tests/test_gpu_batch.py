@@ -119,6 +119,34 @@ def test_run_hypercube_matches_single_instance_runs(gpu_available):
         assert got.sum() > 0
 
 
+def test_run_hypercube_samples_match_the_oracle(gpu_available):
+    """The sweep driver pinned to the oracle: samples of the reference notebook's seven
+    fields, run in one batched call with the float64-geometry tracer, equal the oracle's run
+    of the same configuration on the same Philox streams (relative L1 <= 1e-5 per channel)."""
+    pytest.importorskip("scipy")
+    from oracle.oracle import oracle_run
+    from pyalbsim_gb300.config import HeatmapConfig, RunConfig
+    from pyalbsim_gb300.scene import build_scene
+
+    ranges = {"height": (0.5, 7.5), "absorption": (0.005, 0.05), "scattering": (1.0, 5.0),
+              "floor_albedo": (0.05, 0.3), "surface_roughness": (0.01, 0.1),
+              "field_of_view": (5e-3, 40e-3), "aperture_radius": (0.001, 0.2)}
+    nf, nb = 1500, 400
+    rc = RunConfig(photons_per_batch_forward=nf, photons_per_batch_backward=nb, batches_forward=1,
+                   batches_backward=1)
+    base = dataclasses.replace(batch.config_from_sample({}, base=None), heatmap=HeatmapConfig(enabled=False))
+    res = batch.run_hypercube(ranges, 2, rc, seed=13, base=base, streams=2, precise=True)
+    for i, r in enumerate(res):
+        cfg = batch.config_from_sample(r["params"], base)
+        orc = oracle_run(build_scene(cfg), nf, nb, seed=(13 << 32) + i)["waveform"]
+        got = np.stack([r["waveform"][t] for t in r["waveform"]]).astype(np.float64)
+        assert orc.sum() > 0
+        for c in range(4):
+            den = np.abs(orc[c]).sum()
+            if den:
+                assert np.abs(got[c] - orc[c]).sum() / den < 1e-5, (i, c)
+
+
 def test_batch_jacobian_mask_runs_masked_instances_plain(gpu_available):
     """With the adjoint on, instances without a Jacobian buffer run plain on the same
     contexts; every waveform still equals its single run."""

@@ -65,3 +65,15 @@ def test_reference_arm_only_runs_on_rank_zero():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2"],
                        env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_replica_seeds_do_not_collide_across_base_rank_and_step():
+    """Adjacent base seeds, ranks and steps give distinct Philox keys (a sum of the three
+    would give (base 0, rank 1) and (base 1, rank 0) the same key)."""
+    from pyalbsim_gb300.replicas import replica_seed
+
+    keys = {replica_seed(b, r, s) for b in range(4) for r in range(4) for s in range(4)}
+    assert len(keys) == 64
+    assert replica_seed(0, 1) != replica_seed(1, 0)
+    with pytest.raises(ValueError):
+        replica_seed(1, 1 << 12)

@@ -72,6 +72,63 @@ def test_knn_noalloc_matches_allocating_knn_two_calls():
         eng.close()
 
 
+def test_knn_noalloc_matches_scipy_at_its_limits():
+    """m = 4096 points and k = 256 (the entry point's maxima) against scipy's KDTree on the
+    same float32 points: the same neighbour sets and float64 distances, two calls in a row."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from scipy.spatial import cKDTree
+
+    from pyalbsim_gb300._native import load_library
+
+    lib = load_library()
+    rng = np.random.default_rng(4096)
+    pts = _points(rng, 4096)
+    qs = _queries(rng, pts, 300)
+    ref_d, ref_i = cKDTree(pts.astype(np.float64)).query(qs, k=256)
+    for _ in range(2):
+        d, i = _noalloc(lib, torch, pts, qs, 256)
+        np.testing.assert_allclose(d, ref_d, rtol=1e-12, atol=0.0)
+        for a, b, dd in zip(i, ref_i, d):
+            strict = dd < dd[-1]
+            assert set(a[strict]) == set(b[strict])
+
+
+def test_knn_noalloc_marks_a_query_without_an_answer():
+    """A query with a NaN coordinate has no nearest neighbours: the call cannot report the
+    device-side status synchronously, so all k slots of that query come back as index -1
+    and distance NaN; the other queries of the same call are answered as usual."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from scipy.spatial import cKDTree
+
+    from pyalbsim_gb300._native import load_library
+
+    lib = load_library()
+    rng = np.random.default_rng(11)
+    pts = _points(rng, 1000)
+    qs = _queries(rng, pts, 64)
+    qs[5, 1] = np.nan
+    k = 16
+    d_pts = torch.from_numpy(pts.reshape(-1)).cuda()
+    d_q = torch.from_numpy(qs.reshape(-1)).cuda()
+    d_idx = torch.full((len(qs) * k,), 12345, dtype=torch.int32, device="cuda")
+    d_dist = torch.zeros(len(qs) * k, dtype=torch.float64, device="cuda")
+    rc = lib.alb_knn_noalloc(C.c_void_p(d_pts.data_ptr()), len(pts), C.c_void_p(d_q.data_ptr()), len(qs), k,
+                             C.c_void_p(d_idx.data_ptr()), C.c_void_p(d_dist.data_ptr()), None)
+    assert rc == 0  # asynchronous: the failure is in the output
+    torch.cuda.synchronize()
+    idx = d_idx.cpu().numpy().reshape(-1, k)
+    dist = d_dist.cpu().numpy().reshape(-1, k)
+    assert np.all(idx[5] == -1) and np.all(np.isnan(dist[5]))
+    ok = np.arange(len(qs)) != 5
+    ref_d, _ = cKDTree(pts.astype(np.float64)).query(qs[ok], k=k)
+    assert np.all(idx[ok] >= 0)
+    np.testing.assert_allclose(dist[ok], ref_d, rtol=1e-12, atol=0.0)
+
+
 def test_knn_noalloc_rejects_oversize_input():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
