@@ -396,8 +396,9 @@ def gradients_measure(nf: int):
     depth 12 m, a 0.08, b 0.30, g 0.90 (HG), albedo 0.18, GGX alpha 0.08, differentiated
     with respect to all six parameters at the point 10% above, nf forward + nf/4 backward
     photons (Philox seed 3), the large scene's geometry. One gradient = one adjoint run (five
-    columns) + two depth runs (common-random-number central difference). Baseline: central
-    differences of plain runs (12 runs per gradient + 1 for the value). Accuracy is measured
+    columns) + one depth run (common-random-number forward difference against the adjoint
+    run's own waveform). Baseline: central differences of plain runs (12 runs per gradient +
+    1 for the value). Accuracy is measured
     separately, in expectation over seeds (``gradient_check_measure``): on one seed a central
     difference of a, b or the depth jumps with every integrator step and neighbour set that
     its step moves, so a single-seed comparison says nothing about either estimate."""
@@ -468,17 +469,36 @@ def gradients_measure(nf: int):
 CHANNEL_NAMES = ("bottom", "scatter", "surface_reflection", "transmission_up")
 
 
-def gradient_check_measure(seeds: int = 32, photons: int = 1_000_000):
-    """Accuracy of the adjoint columns: ``adjoint.difference_check`` on the small scene with
-    an HG layer (5 m water, a 0.05, b 0.20, g 0.90, albedo 0.15, GGX alpha 0.05), 1e6 + 2.5e5
-    photons per run, Philox seeds 100.., relative half-steps a, b 5%, g 2%, albedo and
-    roughness 1e-3. Per parameter and reached channel: the mean relative difference between
-    the column's total and the common-random-number central difference, with its paired
-    standard error over the seeds."""
+def _check_table(out):
+    table = {}
+    for name, r in out.items():
+        table[name] = {
+            CHANNEL_NAMES[c]: {"rel_diff": round(r["rel_diff"][c], 5), "se": round(r["rel_diff_se"][c], 5)}
+            for c in range(4) if np.isfinite(r["rel_diff"][c])
+        }
+    return table
+
+
+def gradient_check_measure(seeds: int = 128, photons: int = 1_000_000, config3_seeds: int = 16):
+    """Accuracy of the gradient columns against common-random-number central differences, in
+    expectation over seeds (paired standard errors), three ways:
+
+    * ``by_parameter``: ``adjoint.difference_check`` on the small scene with an HG layer
+      (5 m water, a 0.05, b 0.20, g 0.90, albedo 0.15, GGX alpha 0.05), 1e6 + 2.5e5 photons
+      per run, Philox seeds 100.., relative half-steps a, b 5%, g 2%, albedo and roughness
+      1e-3;
+    * ``config3``: the same at the adjoint workload's geometry and point (the large scene,
+      HG, depth 12 m, a 0.08, b 0.30, g 0.90, albedo 0.18, GGX alpha 0.08, each +10%, a 200 ns
+      window at the surface return), relative half-steps 1e-3 for every parameter;
+    * ``depth_forward_vs_central``: the forward depth difference the gradients use against
+      the central one, small scene, the bias of the O(h) step."""
+    import dataclasses
+
     import torch
 
-    from pyalbsim_gb300.adjoint import CHECK_STEPS, PARAMS, difference_check
-    from pyalbsim_gb300.workloads import small
+    from pyalbsim_gb300.adjoint import CHECK_STEPS, PARAMS, depth_difference_bias, difference_check, with_parameters
+    from pyalbsim_gb300.batch import surface_gate
+    from pyalbsim_gb300.workloads import large, small
 
     cfg = small(hg=0.9)
     nb = photons // 4
@@ -488,27 +508,38 @@ def gradient_check_measure(seeds: int = 32, photons: int = 1_000_000):
     out = difference_check(cfg, photons, nb, seeds=list(range(100, 100 + seeds)))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    table = {}
-    for name, r in out.items():
-        table[name] = {
-            CHANNEL_NAMES[c]: {"rel_diff": round(r["rel_diff"][c], 5), "se": round(r["rel_diff_se"][c], 5)}
-            for c in range(4) if np.isfinite(r["rel_diff"][c])
-        }
-    return {
-        "by_parameter": table, "seeds": seeds, "photons_per_run": photons + nb, "wall_s": wall,
+    result = {
+        "by_parameter": _check_table(out), "seeds": seeds, "photons_per_run": photons + nb, "wall_s": wall,
         "steps": {PARAMS[i]: h for i, h in CHECK_STEPS.items()},
         "config": "small scene: 400 m, 5 m water a=0.05 b=0.20 HG g=0.90, albedo 0.15, GGX alpha 0.05, "
                   "FOV 20 mrad, 0.1 ns bins, k = 100; fast tracer; rel_diff = mean(column total - CRN "
                   "central difference) / |mean difference| over seeds, se its paired standard error",
     }
+    truth = np.array([12.0, 0.08, 0.30, 0.90, 0.18, float(np.sqrt(0.08))])
+    c3 = with_parameters(large(hg=0.9), 1.1 * truth)
+    c3 = dataclasses.replace(c3, waveform_gate=surface_gate(c3))
+    steps3 = {i: 1e-3 for i in range(1, 6)}
+    t0 = time.perf_counter()
+    out3 = difference_check(c3, photons, nb, seeds=list(range(300, 300 + config3_seeds)), steps=steps3)
+    result["config3"] = {"by_parameter": _check_table(out3), "seeds": config3_seeds,
+                         "photons_per_run": photons + nb, "steps": {PARAMS[i]: h for i, h in steps3.items()},
+                         "wall_s": time.perf_counter() - t0}
+    t0 = time.perf_counter()
+    db = depth_difference_bias(cfg, photons, nb, seeds=list(range(500, 500 + 32)))
+    result["depth_forward_vs_central"] = {
+        CHANNEL_NAMES[c]: {"rel_bias": round(db["rel_bias"][c], 5), "se": round(db["rel_bias_se"][c], 5)}
+        for c in range(4) if np.isfinite(db["rel_bias"][c])}
+    result["depth_forward_vs_central"].update(step_m=db["step_m"], seeds=32, wall_s=time.perf_counter() - t0)
+    return result
 
 
 def batched_gradients_measure(n_targets: int = 16, photons: int = 1_000_000, streams: int = 4):
     """Batched form: six-parameter gradients of n_targets Latin-hypercube instances (seed 4)
     at 1e6 + 2.5e5 photons, small scene with an HG layer and a 400 ns window. One
-    alb_batch_run holds, per target, the adjoint instance and the depth pair. Baseline: the
-    plain single-instance run of every target through the engine, one after another (their
-    mean time), 13 runs per central-difference gradient."""
+    alb_batch_run holds, per target, the adjoint instance and one plain instance at depth + h
+    (the depth column's forward difference). Baseline: the plain single-instance run of every
+    target through the engine, one after another (their mean time), 13 runs per
+    central-difference gradient."""
     import torch
 
     from pyalbsim_gb300.adjoint import with_parameters
@@ -526,14 +557,13 @@ def batched_gradients_measure(n_targets: int = 16, photons: int = 1_000_000, str
         out = []
         for i, p in enumerate(pts):
             out.append(Instance(with_parameters(base, p), photons, nb, 3000 + i, p))
-            for s in (1.0, -1.0):
-                q = p.copy()
-                q[0] += s * max(0.01 * p[0], 0.01)
-                out.append(Instance(with_parameters(base, q), photons, nb, 3000 + i, q))
+            q = p.copy()
+            q[0] += max(0.01 * p[0], 0.01)
+            out.append(Instance(with_parameters(base, q), photons, nb, 3000 + i, q))
         return out
 
-    mask = [k % 3 == 0 for k in range(3 * n_targets)]  # Jacobians for the adjoint instances only
-    run_batch(instances()[:6], streams=streams, adjoint=True, jacobian_mask=mask[:6])  # warm-up
+    mask = [k % 2 == 0 for k in range(2 * n_targets)]  # Jacobians for the adjoint instances only
+    run_batch(instances()[:4], streams=streams, adjoint=True, jacobian_mask=mask[:4])  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     _, _, st, _, _ = run_batch(instances(), streams=streams, adjoint=True, jacobian_mask=mask)
@@ -565,7 +595,8 @@ def batched_gradients_measure(n_targets: int = 16, photons: int = 1_000_000, str
         "fd_baseline": {"value": 1.0 / (13 * t_plain), "unit": "waveform-gradients/s", "runs_per_gradient": 13},
         "speedup_vs_fd": rate * 13 * t_plain,
         "config": "small scene (400 m, 0.1 ns bins), HG layer, 400 ns window, k = 100; Latin-hypercube "
-                  "parameters (seed 4) +10%; per target one adjoint instance + depth pair, fast tracer",
+                  "parameters (seed 4) +10%; per target one adjoint instance + one depth + h instance "
+                  "(forward difference), fast tracer",
     }
 
 

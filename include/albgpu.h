@@ -288,7 +288,8 @@ int alb_batch_run(AlbBatchInstance* instances, uint64_t n, const AlbBatchOptions
 /* Device-side counters: [0] events and [1] photons of the last trace, [2] kernels launched
  * by this library, [4 + 4c .. 7 + 4c] gather counters of channel c (leaves, nodes, selects,
  * queries), [24 + c] inexact queries of channel c, [28] events and [29] photons of the last
- * forward trace. n entries are written (at most 32). */
+ * forward trace, [30] neighbour searches of the last trace redone because their first,
+ * guessed threshold did not hold. n entries are written (at most 32). */
 int alb_stats(AlbCtx* ctx, int64_t* out, int n);
 
 /* Accumulated device time (ms, CUDA events on the context's stream) and call counts per

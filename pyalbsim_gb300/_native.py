@@ -481,7 +481,8 @@ class NativeContext:
         out = np.zeros(32, np.int64)
         self._check(self.lib.alb_stats(self.h, _ptr(out), 32))
         st = {"events": int(out[0]), "photons": int(out[1]), "launches": int(out[2]),
-              "forward_events": int(out[28]), "forward_photons": int(out[29])}
+              "forward_events": int(out[28]), "forward_photons": int(out[29]),
+              "search_retries": int(out[30])}
         for c, name in enumerate(("bottom", "scatter", "surface_reflection", "transmission_up")):
             lv, nd, se, nq = (int(x) for x in out[4 + 4 * c: 8 + 4 * c])
             st[f"gather_{name}"] = {

@@ -8,8 +8,10 @@ layer's floor.
 Columns a, b, g, albedo and roughness come from the device adjoint (path scores carried by
 every record and query, accumulated in the same gather as the waveform). The depth moves
 the seafloor plane and with it the discrete integrator step at which a photon returns, so
-its column is a central difference with common random numbers: the same Philox streams
-traced at depth +- h.
+its column is a difference with common random numbers (the same Philox streams traced at
+another depth): by default a forward difference against the adjoint run's own waveform,
+one extra run at depth + h (its O(h) bias against the central difference is measured by
+``depth_difference_bias``); ``depth_difference="central"`` traces depth +- h instead.
 
 ``WaveformFunction`` wraps one simulation as a ``torch.autograd.Function``: forward returns
 the float64 waveform [channels, nbins]; backward contracts the incoming gradient with the
@@ -88,11 +90,16 @@ def simulate_with_jacobian(
     options: Optional[GpuRunOptions] = None,
     depth_step: Optional[float] = None,
     with_depth: bool = True,
+    depth_difference: str = "forward",
 ) -> Tuple[np.ndarray, np.ndarray]:
     """One simulation: (waveform float64 [4, nbins], Jacobian float64 [6, 4, nbins]).
 
-    depth_step (m): half-width of the depth difference, default max(1% of the depth, 1 cm).
-    with_depth=False leaves the depth column at zero and skips its two extra runs."""
+    depth_step (m): step of the depth difference, default max(1% of the depth, 1 cm).
+    depth_difference: "forward" ((w(d + h) - w(d)) / h, one extra run) or "central"
+    ((w(d + h) - w(d - h)) / 2h, two extra runs). with_depth=False leaves the depth column
+    at zero and skips the extra runs."""
+    if depth_difference not in ("forward", "central"):
+        raise ValueError("depth_difference must be 'forward' or 'central'")
     options = options or GpuRunOptions()
     w, j5 = _run(cfg, n_fwd, n_bwd, seed, options, adjoint=True)
     jac = np.zeros((6,) + w.shape)
@@ -100,14 +107,18 @@ def simulate_with_jacobian(
     if with_depth:
         p = parameters_of(cfg)
         h = depth_step if depth_step is not None else max(0.01 * p[0], 0.01)
-        plus, minus = p.copy(), p.copy()
+        plus = p.copy()
         plus[0] += h
-        minus[0] -= h
         wp, _ = _run(with_parameters(cfg, plus), n_fwd, n_bwd, seed, options, adjoint=False)
-        wm, _ = _run(with_parameters(cfg, minus), n_fwd, n_bwd, seed, options, adjoint=False)
         # the simulated time span follows the depth; bins share t = 0 and their width, so
         # the shifted runs are cut or zero-padded to this run's bins
-        jac[0] = (_fit(wp, w.shape[1]) - _fit(wm, w.shape[1])) / (2.0 * h)
+        if depth_difference == "forward":
+            jac[0] = (_fit(wp, w.shape[1]) - w) / h
+        else:
+            minus = p.copy()
+            minus[0] -= h
+            wm, _ = _run(with_parameters(cfg, minus), n_fwd, n_bwd, seed, options, adjoint=False)
+            jac[0] = (_fit(wp, w.shape[1]) - _fit(wm, w.shape[1])) / (2.0 * h)
     return w, jac
 
 
@@ -156,6 +167,48 @@ class WaveformFunction:
 
             cls._impl = _Fn
         return cls._impl.apply(params, cfg, n_fwd, n_bwd, seed, options)
+
+
+def depth_difference_bias(cfg, n_fwd: int, n_bwd: int, seeds: Sequence[int], depth_step: Optional[float] = None,
+                          streams: int = 4, runner=None) -> dict:
+    """The forward depth difference against the central one, in expectation over seeds.
+
+    Per seed, three plain runs with the seed's streams at depth d - h, d, d + h (h as in
+    ``simulate_with_jacobian``). Per channel: the mean over seeds of the channel totals'
+    forward difference and central difference, and rel_bias = mean(forward - central) /
+    |mean(central)| with its paired standard error (NaN where the central difference is
+    zero). runner(configs, seeds) -> waveforms replaces the device batch (tests)."""
+    p0 = parameters_of(cfg)
+    h = depth_step if depth_step is not None else max(0.01 * p0[0], 0.01)
+    configs, run_seeds = [], []
+    for s in seeds:
+        for dz in (-h, 0.0, h):
+            q = p0.copy()
+            q[0] += dz
+            configs.append(with_parameters(cfg, q))
+            run_seeds.append(s)
+    if runner is None:
+        from pyalbsim_gb300.batch import Instance, run_batch
+
+        inst = [Instance(c, n_fwd, n_bwd, s, None) for c, s in zip(configs, run_seeds)]
+        waves, _, status, _, _ = run_batch(inst, streams=streams)
+        if np.any(status != 0):
+            raise RuntimeError(f"depth difference check: {int((status != 0).sum())} runs failed")
+    else:
+        waves = runner(configs, run_seeds)
+    nb = waves[1].shape[1]
+    fwd, cen = [], []
+    for k in range(len(seeds)):
+        wm, w0, wp = (_fit(waves[3 * k + j], nb).sum(axis=1) for j in range(3))
+        fwd.append((wp - w0) / h)
+        cen.append((wp - wm) / (2.0 * h))
+    fwd, cen = np.array(fwd), np.array(cen)
+    cm = cen.mean(axis=0)
+    den = np.where(cm != 0, np.abs(cm), np.nan)
+    d = fwd - cen
+    se = d.std(axis=0, ddof=1) / np.sqrt(len(seeds)) if len(seeds) > 1 else np.full(4, np.nan)
+    return {"forward": fwd.mean(axis=0).tolist(), "central": cm.tolist(), "step_m": h,
+            "rel_bias": (d.mean(axis=0) / den).tolist(), "rel_bias_se": (se / den).tolist()}
 
 
 # Relative half-steps of the central differences in ``difference_check``: a, b and g move

@@ -716,6 +716,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
     }
     // slots 28/29 keep the last forward trace's events and photons across the backward trace
     CK(cudaMemsetAsync(ctx->d_stats, 0, 28 * 8, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_stats + 30, 0, 8, ctx->st));
     if (pass == ALB_FORWARD) {
         ctx->maps_built = false;
         uint64_t before[ALB_CHANNELS];
@@ -832,6 +833,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             q.rk_out = ctx->keep_ids ? ctx->qrk[k][g == 3 ? 1 : 0] : nullptr;
             q.stats = ctx->d_stats + 4 + 4 * c;  // per channel: leaves, nodes, selects, queries
             q.inexact = ctx->d_stats + 24 + c;
+            q.retries = ctx->d_stats + 30;
             if (ctx->sort_q) {
                 PhaseTimer ps(ctx, 3);
                 sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);

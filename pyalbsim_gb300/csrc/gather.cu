@@ -46,6 +46,7 @@ struct WarpSmem {
     double bd[kBand];    // near-tie band: float64 distances
     uint32_t bi[kBand];  // map positions
     uint64_t bt[kBand];  // tie keys from the record's content (or 0)
+    float prev_rk2;      // squared k-th distance of the warp's previous query (kept out of registers)
 };
 
 // Lower bound of the squared distance from the float64 query (qx + lx, ...) to a box:
@@ -297,6 +298,7 @@ struct KnnResult {
     int nodes;     // internal nodes expanded
     int selects;   // candidate-buffer reductions
     int clipped;   // 1 if a buffer bound forced an inexact answer (mass ties)
+    int retried;   // 1 if an optimistic first threshold did not hold and the search was redone
     int fail;      // 0, or why the search has no answer (s.ci is then not valid):
                    // ALB_ERR_ITER_CAP (traversal guard) or ALB_ERR_INVALID (fewer than k
                    // finite points admitted: a NaN or infinite query or map coordinates)
@@ -374,8 +376,14 @@ ALB_DEVICE double select_refined(const MapDev& m, WarpSmem& s, int off, int n, i
 
 // Full k-NN search for one query. Returns false when the map has fewer than k records; the
 // k nearest map positions are then in s.ci[0 .. k).
-// thr0: an upper bound of the squared k-th distance that already includes the band margin
-// (FLT_MAX when none is known).
+// thr_safe: an upper bound of the squared k-th distance that already includes the band margin
+// (FLT_MAX when none is known). thr0 <= thr_safe: the first search's threshold, which may be
+// an optimistic guess. A search under a guess is accepted only when its own answer proves it
+// complete: at least k candidates, and the k-th with its band margin within the guess (every
+// point that can rank among the k nearest then had a distance below the admission
+// threshold, and every box holding one was opened). Otherwise the search is repeated under
+// thr_safe, and under no bound at all if that fails too. Either way the answer is the one a
+// search from no bound gives.
 // The query is (fx + lx, fy + ly, fz + lz) = (qx, qy, qz) exactly, |l*| <= half an ulp of f*.
 // Points at exactly the same float64 distance rank by a key taken from their record content
 // (time, then a hash of direction, time and energy; when tie_rec is given) and then by map
@@ -387,17 +395,28 @@ ALB_DEVICE double select_refined(const MapDev& m, WarpSmem& s, int off, int n, i
 // float32 screening distance and only a crowded final band is refined.
 template <bool REFINE>
 ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz, float fx,
-                         float fy, float fz, float lx, float ly, float lz, float thr0, const float4* tie_rec,
-                         KnnResult& res) {
+                         float fy, float fz, float lx, float ly, float lz, float thr0, float thr_safe,
+                         const float4* tie_rec, KnnResult& res) {
     const int l = lane_id();
     if (m.n_real < (uint64_t)k) return false;
     float thr = thr0;  // admission threshold (float32 squared distance, with margin)
     int cnt = 0;
-    res.leaves = res.nodes = res.selects = res.clipped = res.fail = 0;
-    // A carried bound can only fail through a degenerate previous result (a clipped
-    // boundary band); the search is then repeated without it.
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        thr = attempt ? FLT_MAX : thr0;
+    float kth_known = -1.f;  // the float32 k-th of the accepted search (!REFINE), when computed
+    res.leaves = res.nodes = res.selects = res.clipped = res.retried = res.fail = 0;
+    // Thresholds in turn: the first guess, the safe bound, no bound. A carried safe bound can
+    // only fail through a degenerate previous result (a clipped boundary band).
+    float start = thr0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        if (attempt == 1) {
+            if (!(thr_safe > thr0)) continue;  // the guess was the safe bound itself
+            start = thr_safe;
+            res.retried = 1;
+        }
+        if (attempt == 2) {
+            if (start == FLT_MAX) break;
+            start = FLT_MAX;
+        }
+        thr = start;
         cnt = 0;
         int sp = 0;
         // roots
@@ -519,7 +538,16 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 __syncwarp();
             }
         }
-        if (res.fail || cnt >= k || thr0 == FLT_MAX) break;
+        if (res.fail || start == FLT_MAX) break;
+        if (cnt < k) continue;
+        if (REFINE || start >= thr_safe) break;
+        // a guess: accepted when the k-th with its band margin lies within it
+        ++res.selects;
+        const float kth = warp_kth32(s, 0, cnt, k);
+        if (kth * (1.0f + 2.0f * kRelMargin) <= start) {
+            kth_known = kth;
+            break;
+        }
     }
     if (!res.fail && cnt < k) res.fail = ALB_ERR_INVALID;
     if (res.fail) return true;
@@ -529,7 +557,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
     } else {
         // float32 k-th; entries clearly below it are in, the band within the screening
         // margin around it is resolved exactly (refined keys when it is crowded)
-        const float kth = warp_kth32(s, 0, cnt, k);
+        const float kth = kth_known >= 0.f ? kth_known : warp_kth32(s, 0, cnt, k);
         const float blo = kth * (1.0f - 2.0f * kRelMargin), bhi = kth * (1.0f + 2.0f * kRelMargin);
         int n_in = 0, n_band = 0;
 #pragma unroll 1
@@ -896,7 +924,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 __syncwarp();
                 continue;
             }
-            float thr0 = FLT_MAX;
+            float thr_safe = FLT_MAX, thr0 = FLT_MAX;
             if (have_prev) {
                 // the float32 screening error (below 2^-21) is far inside the 2^-14 inflation
                 unsigned mx = 0u;
@@ -906,11 +934,18 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                     mx = max(mx, __float_as_uint(d));  // non-negative floats order like their bits
                 }
                 const float t = __uint_as_float(__reduce_max_sync(0xffffffffu, mx)) * (1.f + 1.f / 16384.f);
-                if (t < 1.0e37f) thr0 = t;
+                if (t < 1.0e37f) thr_safe = t;
+                // The safe bound is the farthest of the previous query's neighbours, about
+                // twice the k-th distance here (the sorted queries are about one k-th
+                // distance apart): eight times the ball. Consecutive k-th distances differ by
+                // less than 20% for 99.7% of the scatter map's sorted queries, so the first
+                // search uses (1.2 r_prev)^2 and is redone under the safe bound when that
+                // does not hold. Planar maps keep the safe bound.
+                thr0 = (CHANNEL == ALB_SCATTER) ? fminf(thr_safe, s.prev_rk2 * 1.44f) : thr_safe;
             }
             KnnResult r;
             if (!warp_knn<CHANNEL != ALB_SCATTER>(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0,
-                                                   m.b, r)) {
+                                                   thr_safe, m.b, r)) {
                 if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
                 failed = true;
                 break;
@@ -921,11 +956,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 break;
             }
             have_prev = true;
+            if (l == 0) s.prev_rk2 = (float)r.rk2;  // read after the next query's __syncwarp
             if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
             st_leaves += r.leaves;
             st_nodes += r.nodes;
             st_selects += r.selects;
             st_inexact += r.clipped;
+            if (r.retried && l == 0 && q.retries) atomicAdd(q.retries, 1ull);  // rare: no register kept
             ++st_queries;
             const float Es = qa.w, ts = qb.w;
             const float rk = r.rkf;
@@ -1010,7 +1047,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_knn(MapDev m, const doubl
         const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
         int why = 0;
         if (!warp_knn<true>(m, s, k, qx, qy, qz, fx, fy, fz, (float)(qx - (double)fx), (float)(qy - (double)fy),
-                            (float)(qz - (double)fz), FLT_MAX, nullptr, r))
+                            (float)(qz - (double)fz), FLT_MAX, FLT_MAX, nullptr, r))
             why = ALB_ERR_TOO_FEW;
         else if (r.fail)
             why = r.fail;

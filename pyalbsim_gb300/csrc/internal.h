@@ -89,6 +89,7 @@ struct QueryDev {
     double* rk_out;    // optional per-query k-th neighbour distance
     unsigned long long* stats;    // optional [leaves, nodes, selects, queries] accumulators
     unsigned long long* inexact;  // optional count of answers a buffer bound made inexact (mass ties)
+    unsigned long long* retries;  // optional count of searches redone because a first guess did not hold
 };
 
 // Waveform / heatmap accumulators (128-bit fixed point, lo and hi words).

@@ -3,10 +3,10 @@
 Each target waveform is fitted by Adam over the six parameters (depth, a, b, HG g,
 seafloor albedo, roughness) from a common initial guess. Every iteration runs all targets
 in one ``alb_batch_run``. Per target there is an adjoint instance at its current
-parameters, which gives the waveform and five Jacobian columns, and two plain instances at
-depth +- h, which give the depth column by a common-random-number difference. All three
-share the iteration's Philox key, which changes from iteration to iteration (a stochastic
-gradient).
+parameters, which gives the waveform and five Jacobian columns, and a plain instance at
+depth + h, which gives the depth column by a common-random-number forward difference
+(``depth_difference="central"``: two plain instances at depth +- h). All share the
+iteration's Philox key, which changes from iteration to iteration (a stochastic gradient).
 
 The loss compares the scaled simulated waveform s w with the target counts c, where c is
 the target waveform scaled to ``peak`` counts with Poisson shot noise and s is the same
@@ -85,9 +85,13 @@ def fit(
     depth_grid: Optional[Sequence[float]] = None,
     fixed: Optional[Sequence[bool]] = None,
     prior_sigma: Optional[Sequence[Optional[float]]] = None,
+    depth_difference: str = "forward",
 ) -> Dict:
     """Fit every row of ``targets`` (n x 6). Returns final parameters, depth errors and the
     per-iteration mean data loss.
+
+    depth_difference: "forward" (one plain instance at depth + depth_step per target) or
+    "central" (two, at depth +- depth_step) for the depth column of the gradient.
 
     loss: "log" (squared difference of log(1 + counts)), "mse", or "poisson" (the negative
     log-likelihood of the Poisson counts, sum(lambda - counts ln lambda), lambda the scaled
@@ -115,6 +119,8 @@ def fit(
 
     theta0 = np.array(initial if initial is not None else INITIAL, dtype=np.float64)
     u = np.zeros((n, 6))
+    if depth_difference not in ("forward", "central"):
+        raise ValueError("depth_difference must be 'forward' or 'central'")
     free = np.ones(6) if fixed is None else 1.0 - np.asarray(fixed, dtype=np.float64)
     if free.shape != (6,):
         raise ValueError("fixed needs six entries")
@@ -169,11 +175,12 @@ def fit(
     for it in range(iters):
         theta = _clip(theta0 * np.exp(u))
         key = (seed << 40) + (1 << 32) + (it if resample else 0)
-        per = 3 if free[0] else 1  # the depth pair only while the depth is free
+        shifts = ((1.0,) if depth_difference == "forward" else (1.0, -1.0)) if free[0] else ()
+        per = 1 + len(shifts)  # the depth runs only while the depth is free
         inst = []
         for i in range(n):
             inst.append(Instance(with_parameters(base, theta[i]), photons, nb, key, theta[i]))
-            for sgn in ((1.0, -1.0) if free[0] else ()):
+            for sgn in shifts:
                 q = theta[i].copy()
                 q[0] += sgn * depth_step
                 inst.append(Instance(with_parameters(base, q), photons, nb, key, q))
@@ -189,8 +196,11 @@ def fit(
             grads[i, 1:] = np.einsum("pcb,cb->p", jac[k], dl_dw)
             if free[0]:
                 lp = loss_and_grad(w[k + 1], i)[0]
-                lm = loss_and_grad(w[k + 2], i)[0]
-                grads[i, 0] = (lp - lm) / (2.0 * depth_step)
+                if depth_difference == "forward":
+                    grads[i, 0] = (lp - losses[i]) / depth_step
+                else:
+                    lm = loss_and_grad(w[k + 2], i)[0]
+                    grads[i, 0] = (lp - lm) / (2.0 * depth_step)
         gu = (grads * theta + u * inv_var) * free  # d (L + prior) / d u for theta = theta0 e^u
         m_ = b1 * m_ + (1 - b1) * gu
         v_ = b2 * v_ + (1 - b2) * gu * gu

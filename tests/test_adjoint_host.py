@@ -208,7 +208,7 @@ def test_depth_column_is_the_aligned_central_difference(monkeypatch):
     monkeypatch.setattr(adj, "_run", fake_run)
     cfg = _hg_cfg(0.9)
     D = adj.parameters_of(cfg)[0]
-    w, jac = adj.simulate_with_jacobian(cfg, 10, 10, 7, depth_step=0.5)
+    w, jac = adj.simulate_with_jacobian(cfg, 10, 10, 7, depth_step=0.5, depth_difference="central")
     n = w.shape[1]
     n_minus = 100 + int(round(10 * (D - 0.5 - 2.0)))  # the shallower run's span
     t = np.arange(n, dtype=np.float64)
@@ -218,6 +218,51 @@ def test_depth_column_is_the_aligned_central_difference(monkeypatch):
     assert [c[1] for c in calls] == [True, False, False] and len({c[2] for c in calls}) == 1
     _, jac2 = adj.simulate_with_jacobian(cfg, 10, 10, 7, with_depth=False)
     assert not jac2[0].any() and len(calls) == 4
+
+
+def test_depth_column_forward_difference_reuses_the_adjoint_run(monkeypatch):
+    """The default depth column is (W(D + h) - W(D)) / h on this run's bins: one extra plain
+    run, the adjoint run's own waveform as W(D)."""
+    calls = []
+
+    def fake_run(cfg, nf, nb, seed, options, adjoint):
+        d = adj.parameters_of(cfg)[0]
+        calls.append((round(d, 6), adjoint, seed))
+        nbins = 100 + int(round(10 * (d - 2.0)))
+        w = np.tile(np.arange(nbins, dtype=np.float64) * d, (4, 1))
+        return w, (np.ones((5, 4, nbins)) if adjoint else None)
+
+    monkeypatch.setattr(adj, "_run", fake_run)
+    cfg = _hg_cfg(0.9)
+    D = adj.parameters_of(cfg)[0]
+    w, jac = adj.simulate_with_jacobian(cfg, 10, 10, 7, depth_step=0.5)
+    t = np.arange(w.shape[1], dtype=np.float64)
+    np.testing.assert_allclose(jac[0, 2], (t * (D + 0.5) - t * D) / 0.5)
+    assert [c[1] for c in calls] == [True, False] and calls[1][0] == round(D + 0.5, 6)
+    with pytest.raises(ValueError):
+        adj.simulate_with_jacobian(cfg, 10, 10, 7, depth_difference="backward")
+
+
+def test_depth_difference_bias_on_a_quadratic():
+    """depth_difference_bias: for totals quadratic in the depth, c2 d^2, the forward
+    difference exceeds the central one by c2 h, the O(h) bias it reports."""
+    cfg = _hg_cfg(0.9)
+    D = adj.parameters_of(cfg)[0]
+    h = 0.2
+
+    def runner(configs, seeds):
+        out = []
+        for c in configs:
+            d = adj.parameters_of(c)[0]
+            w = np.zeros((4, 50))
+            w[0, 0] = 3.0 * d * d
+            out.append(w)
+        return out
+
+    r = adj.depth_difference_bias(cfg, 10, 10, [1, 2, 3], depth_step=h, runner=runner)
+    np.testing.assert_allclose(r["central"][0], 6.0 * D)
+    np.testing.assert_allclose(r["forward"][0], 6.0 * D + 3.0 * h)
+    np.testing.assert_allclose(r["rel_bias"][0], 3.0 * h / (6.0 * D))
 
 
 def _oracle_runner(nf, nb):

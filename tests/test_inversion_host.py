@@ -101,6 +101,9 @@ def test_fixed_depth_skips_the_depth_pair(fake, monkeypatch):
     assert calls == [2, 2, 2, 2]  # the targets, then one adjoint instance per target and iteration
     calls.clear()
     inversion.fit(target, iters=2, photons=100, base=object())
+    assert calls == [2, 4, 4]  # forward depth difference: one shifted instance per target
+    calls.clear()
+    inversion.fit(target, iters=2, photons=100, base=object(), depth_difference="central")
     assert calls == [2, 6, 6]
 
 
