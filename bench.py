@@ -280,6 +280,10 @@ def main():
     ap.add_argument("--no-gradients", action="store_true")
     ap.add_argument("--grad-photons", type=float, default=1e7)
     ap.add_argument("--precise", action="store_true", help="float64-geometry tracer instead of the float32 one")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-every", type=int, default=32,
+                    help="run every n-th instance of the 4096-instance sweep (1 = the whole sweep)")
+    ap.add_argument("--sweep-only", action="store_true", help="print only the sweep measurement")
     args = ap.parse_args()
     args.workload_label = (
         "large single instance: 400 m, 20 m water a=0.10 b=0.40 FF, GGX alpha 0.10, albedo 0.20, "
@@ -288,6 +292,9 @@ def main():
     )
     if args.impl == "reference":
         return run_reference(args)
+    if args.sweep_only:
+        print(json.dumps({"batched_sweep": sweep_measure(args.sweep_every)}), flush=True)
+        return None
 
     import torch
 
@@ -382,6 +389,8 @@ def main():
         line["cpu_baseline"] = cpu_baseline_port(cfg, args.cpu_sample, threads)
         if not args.no_e2e:
             line["e2e"] = measured(e2e_measure, cfg, nf, nb)
+        if not args.no_sweep:
+            line["batched_sweep"] = measured(sweep_measure, args.sweep_every)
         if not args.no_gradients:
             line["gradients"] = measured(gradients_measure, int(args.grad_photons))
             line["gradients_batched"] = measured(batched_gradients_measure)
@@ -598,6 +607,34 @@ def batched_gradients_measure(n_targets: int = 16, photons: int = 1_000_000, str
                   "parameters (seed 4) +10%; per target one adjoint instance + one depth + h instance "
                   "(forward difference), fast tracer",
     }
+
+
+def sweep_measure(every: int = 32, streams: int = 8):
+    """The batched Latin-hypercube sweep (4096 instances, seed 2: depth 1-40 m, a, b, g,
+    albedo, GGX alpha, FOV 10-60 mrad; photons log-uniform in [1e5, 1e7] per instance, a
+    quarter as many backward; 400 m, 0.1 ns bins, k-NN, HG water) through one
+    ``alb_batch_run``: every ``every``-th instance (all 4096 with every=1). Wall time,
+    traced photons per wall second, failed instances. Also the concurrency gain on small
+    instances: 64 instances of 1e5 photons on one worker against ``streams`` workers."""
+    import torch
+
+    from pyalbsim_gb300.batch import hypercube_instances, run_batch
+    from pyalbsim_gb300.workloads import small
+
+    base = small(hg=0.9)
+    inst = hypercube_instances(base, 4096, seed=2)[::every]
+    run_batch(inst[:2], streams=2)  # warm-up
+    torch.cuda.synchronize()
+    _, _, st, _, wall = run_batch(inst, streams=streams)
+    photons = sum(x.n_forward + x.n_backward for x in inst)
+    out = {"instances": len(inst), "of": 4096, "photons": int(photons), "wall_s": wall,
+           "value": photons / wall, "unit": "photons/s", "failed": int((st != 0).sum()), "streams": streams}
+    smalls = hypercube_instances(base, 64, seed=7, photons=(1e5, 1e5 + 1))
+    t1 = run_batch(smalls, streams=1)[4]
+    tn = run_batch(smalls, streams=streams)[4]
+    out["small_instances"] = {"instances": 64, "photons_each": int(smalls[0].n_forward), "wall_s_1_worker": t1,
+                              f"wall_s_{streams}_workers": tn, "gain": t1 / tn}
+    return out
 
 
 def e2e_measure(cfg, nf, nb):

@@ -29,6 +29,10 @@ constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
 constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
 constexpr int kBand = 32;         // near-tie entries resolved in float64
+// Squared widening of the previous query's k-th distance that the scatter-map search first
+// admits within (1.2^2): consecutive sorted queries' k-th distances differ by less than 20%
+// for 99.7% of them; a guess that does not hold is detected and the search redone.
+constexpr float kGuessWiden2 = 1.44f;
 // Admission margin of the float32 screening distance (its error is below 2^-22 relative).
 constexpr float kRelMargin = 9.5367431640625e-07f;  // 2^-20
 
@@ -513,8 +517,18 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                     if (d > thr) d = FLT_MAX;
                 }
                 uint32_t cc = (uint32_t)c;
-                int nv = __popc(__ballot_sync(0xffffffffu, d < FLT_MAX));
-                if (nv <= 16) {
+                const unsigned vm = __ballot_sync(0xffffffffu, d < FLT_MAX);
+                int nv = __popc(vm);
+                if (!REFINE && start < thr_safe) {
+                    // Under a guessed threshold the search rarely shrinks its threshold, so
+                    // the order of the boxes does not change which leaves are opened:
+                    // push the children as they come, without ordering them.
+                    if (d < FLT_MAX) {
+                        const int pos = sp + __popc(vm & lanemask_lt());
+                        s.stk[pos] = ((uint32_t)cl << 29) | cc;
+                        s.stk_d[pos] = d;
+                    }
+                } else if (nv <= 16) {
                     // few children within the threshold: extract them nearest first
                     // (non-negative floats order like their bit patterns)
                     unsigned key = __float_as_uint(d);
@@ -941,7 +955,7 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 // less than 20% for 99.7% of the scatter map's sorted queries, so the first
                 // search uses (1.2 r_prev)^2 and is redone under the safe bound when that
                 // does not hold. Planar maps keep the safe bound.
-                thr0 = (CHANNEL == ALB_SCATTER) ? fminf(thr_safe, s.prev_rk2 * 1.44f) : thr_safe;
+                thr0 = (CHANNEL == ALB_SCATTER) ? fminf(thr_safe, s.prev_rk2 * kGuessWiden2) : thr_safe;
             }
             KnnResult r;
             if (!warp_knn<CHANNEL != ALB_SCATTER>(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0,

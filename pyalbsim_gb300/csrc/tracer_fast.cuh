@@ -286,6 +286,14 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
                 const float a = water_alpha_f(sc, ph.py);
                 if (sc.adjoint) score_tau(sc, ph.sc, layer_of_f(sc, ph.py), a * len);
                 ph.tau = fmaf(a, len, ph.tau);
+            } else if (!(ph.py > ys)) {
+                // A transmitted photon is in the air. Near the surface a float32 height is
+                // quantised to ulp(ys) (3e-5 m at 400 m), as coarse as a grazing photon's
+                // vertical step, so the crossing fraction can round to 1 and leave no
+                // remaining step: the photon would sit on the surface, count as in water and
+                // exit a second time (a second transmission record, 1.5% of the photons at
+                // 400 m with 0.05 ns bins). Place it just above the surface instead.
+                ph.py = nextafterf(ys, 1.0e30f);
             }
         } else {
             // handle_seafloor

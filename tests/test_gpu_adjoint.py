@@ -153,11 +153,23 @@ def test_depth_column_shifts_the_bottom_return(gpu_available):
 
 
 def test_forward_depth_column_shifts_the_bottom_return(gpu_available):
-    """The default forward difference (one extra run) spans half the depth interval of the
-    central one, so one seed carries twice its noise: the centroid rate averaged over six
-    seeds meets the same bar."""
+    """The default forward difference (one extra run), averaged over six seeds.
+
+    The simulated time span follows the depth (the reference sets its step count from it):
+    at this scene it gains a step every ~0.2 m (at 2.05 m, just above the scene's 2 m), and
+    a longer span admits late photons, a jump in the waveform that a difference across it
+    includes. The depth is therefore set to 1.9 m, whose interval [1.9, 1.95] m keeps one
+    span. There the centroid is convex in the depth: small-step differences of the oracle
+    (h = 0.01 m, 10 seeds) give 11.8 +- 0.4 bins/m central and 12.2 +- 0.5 forward, against
+    the 8.9 bins/m of a pure time shift (the return also changes shape), and 9.8 central at
+    h = 0.05 m. The bar is the pure shift's rate times [0.8, 1.6], which holds the measured
+    rates and rejects a column of the wrong sign or scale."""
     cfg = CFGS["hg"]()
+    p = adj.parameters_of(cfg)
+    p[0] = 1.9
+    cfg = adj.with_parameters(cfg, p)
     scene = build_scene(cfg)
+    assert build_scene(adj.with_parameters(cfg, p + np.array([0.05, 0, 0, 0, 0, 0]))).steps == scene.steps
     nf, nb = 200000, 50000
     rates = []
     for seed in range(20, 26):
@@ -165,7 +177,7 @@ def test_forward_depth_column_shifts_the_bottom_return(gpu_available):
         rates.append(_centroid_rate(w, jac))
     bin_s = scene.dt * scene.sample_multiplier
     expect = 2.0 / (scene.layers[-1].speed32 * bin_s)
-    assert 0.8 * expect < np.mean(rates) < 1.3 * expect, (rates, expect)
+    assert 0.8 * expect < np.mean(rates) < 1.6 * expect, (rates, expect)
 
 
 def test_torch_gradient_equals_c_adjoint(gpu_available):
