@@ -89,6 +89,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+# Flop-equivalents per interaction event of the tracer (FMA = 2, special-function op = 1),
+# the convention its FP32 roofline is quoted in.
+F_EVENT = 64
+
+
+def fp32_peak_tflops():
+    """FP32 peak of the GPU: SMs x 128 FP32 lanes x 2 flop per FMA x the maximum SM clock
+    (MEASURED_PEAKS.json's sm_max_mhz when present). Derived, not measured: the measured-peak
+    file carries no FP32 figure."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            mhz = float(json.load(fh).get("sm_max_mhz", mhz))
+    except Exception:
+        pass
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, f"derived: {sms} SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz"
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -376,6 +397,7 @@ def main():
             "value": world * (gstats["forward_events"] + gstats["events"]) / (ms_step / 1e3), "unit": "events/s",
             "per_step": gstats["forward_events"] + gstats["events"]},
         "last_step_counters": gstats,
+        "tracer_roofline": tracer_roofline(gstats, phases, args.steps),
         "clocks": clk.summary(),
         "waveform_total": float(wf.sum()),
     }
@@ -398,6 +420,17 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def tracer_roofline(gstats, phases, steps):
+    """FP32 roofline of the forward trace: the last step's interaction events x F_EVENT over
+    the forward trace's CUDA-event time per step, against the FP32 peak."""
+    fwd_ms = phases["trace_fwd"][0] / steps
+    peak, source = fp32_peak_tflops()
+    achieved = gstats["forward_events"] * F_EVENT / (fwd_ms / 1e3) / 1e12 if fwd_ms > 0 else 0.0
+    return {"bound": "fp32", "kernel": "k_trace_fast<0> (forward trace)", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "events_per_s": gstats["forward_events"] / (fwd_ms / 1e3),
+            "flop_per_event": F_EVENT, "peak_source": source}
 
 
 def gradients_measure(nf: int):
