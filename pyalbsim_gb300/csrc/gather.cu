@@ -30,9 +30,10 @@ constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
 constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
 constexpr int kBand = 32;         // near-tie entries resolved in float64
 // Squared widening of the previous query's k-th distance that the scatter-map search first
-// admits within (1.2^2): consecutive sorted queries' k-th distances differ by less than 20%
-// for 99.7% of them; a guess that does not hold is detected and the search redone.
-constexpr float kGuessWiden2 = 1.44f;
+// admits within (1.1^2): consecutive sorted queries' k-th distances differ by less than 10%
+// for 97% of them; a guess that does not hold is detected and the search redone (measured
+// at 1e7 photons: 1.1^2 gave the fastest scatter gather of 1.1^2, 1.15^2 and 1.2^2).
+constexpr float kGuessWiden2 = 1.21f;
 // Admission margin of the float32 screening distance (its error is below 2^-22 relative).
 constexpr float kRelMargin = 9.5367431640625e-07f;  // 2^-20
 
@@ -444,29 +445,40 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
             __syncwarp();
         }
         int guard = 0;
-        while (sp > 0) {
+        // Under a guessed threshold, the leaves of an expanded leaf parent are visited straight
+        // from its ballot (lmask, leaf index lbase + bit) instead of through the stack.
+        unsigned lmask = 0u;
+        uint32_t lbase = 0u;
+        while (sp > 0 || lmask) {
             if (++guard > (1 << 22)) {  // reported, never a silent partial answer
                 res.fail = ALB_ERR_ITER_CAP;
                 break;
             }
-            // the top 32 stack entries, one per lane (lane 0 = top)
-            const int i = sp - 1 - l;
-            uint32_t e = 0u;
-            bool ok = false;
-            if (i >= 0) {
-                e = s.stk[i];
-                ok = s.stk_d[i] <= thr;
-            }
-            const unsigned okm = __ballot_sync(0xffffffffu, ok);
-            if (!okm) {  // 32 entries beyond the threshold
-                sp = sp > 32 ? sp - 32 : 0;
+            uint32_t etop;
+            if (lmask) {
+                const int b = __ffs(lmask) - 1;
+                lmask &= lmask - 1u;
+                etop = lbase + (uint32_t)b;  // a leaf: level bits 0
+            } else {
+                // the top 32 stack entries, one per lane (lane 0 = top)
+                const int i = sp - 1 - l;
+                uint32_t e = 0u;
+                bool ok = false;
+                if (i >= 0) {
+                    e = s.stk[i];
+                    ok = s.stk_d[i] <= thr;
+                }
+                const unsigned okm = __ballot_sync(0xffffffffu, ok);
+                if (!okm) {  // 32 entries beyond the threshold
+                    sp = sp > 32 ? sp - 32 : 0;
+                    __syncwarp();
+                    continue;
+                }
+                const int f = __ffs(okm) - 1;
+                etop = __shfl_sync(0xffffffffu, e, f);
+                sp -= f + 1;
                 __syncwarp();
-                continue;
             }
-            const int f = __ffs(okm) - 1;
-            const uint32_t etop = __shfl_sync(0xffffffffu, e, f);
-            sp -= f + 1;
-            __syncwarp();
             if ((etop >> 29) == 0) {
                 // a leaf: admit its points within the threshold
                 ++res.leaves;
@@ -522,8 +534,13 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 if (!REFINE && start < thr_safe) {
                     // Under a guessed threshold the search rarely shrinks its threshold, so
                     // the order of the boxes does not change which leaves are opened:
-                    // push the children as they come, without ordering them.
-                    if (d < FLT_MAX) {
+                    // children are taken as they come, without ordering them; leaves go
+                    // straight to the visit.
+                    if (cl == 0) {
+                        lmask = vm;
+                        lbase = (uint32_t)(node * 32u);
+                        nv = 0;
+                    } else if (d < FLT_MAX) {
                         const int pos = sp + __popc(vm & lanemask_lt());
                         s.stk[pos] = ((uint32_t)cl << 29) | cc;
                         s.stk_d[pos] = d;
