@@ -836,8 +836,9 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             q.retries = ctx->d_stats + 30;
             if (ctx->sort_q) {
                 PhaseTimer ps(ctx, 3);
-                sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
+                const int src = sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
                 ps.stop();
+                if (src != 0) return fail(ctx, ALB_ERR_CUDA, "query sort: device memory allocation failed");
                 q.perm = ctx->qperm[k];
             }
             PhaseTimer pg(ctx, 4 + c);
@@ -1300,11 +1301,13 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        for (uint64_t t = next.fetch_add(1); t < n; t = next.fetch_add(1)) {
+        bool alone = false;  // the retry of an instance that ran out of memory beside others
+        for (uint64_t t = next.fetch_add(1); t < n; t = alone ? t : next.fetch_add(1)) {
             AlbBatchInstance& I = inst[order[t]];
             I.device_ms = 0.f;
             int rc = ALB_OK;
             std::string msg;
+            bool shared = false;  // other instances were running when this one started
             {
                 std::unique_lock<std::mutex> g(mem_mu);
                 const double need = need_of(I);
@@ -1318,9 +1321,10 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                     mem_cv.notify_all();
                 }
                 const double grow = std::max(0.0, need - held);
-                mem_cv.wait(g, [&] { return held_total + grow <= budget || running == 0; });
+                mem_cv.wait(g, [&] { return alone ? running == 0 : (held_total + grow <= budget || running == 0); });
                 held_total += grow;
                 held += grow;
+                shared = running > 0;
                 ++running;
             }
             if (!ctx) {
@@ -1391,6 +1395,10 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                     mem_cv.notify_all();
                 }
             }
+            // Device memory is admitted on an estimate: an instance that failed for memory
+            // (an allocation or a map build) while others were running is run once more, alone.
+            const bool memory = rc == ALB_ERR_CUDA || rc == ALB_ERR_CAPACITY;
+            alone = memory && shared && !alone && cudaGetLastError() != cudaErrorIllegalAddress;
         }
         if (ctx) alb_destroy(ctx);
         {

@@ -252,19 +252,22 @@ __global__ void k_scan_add(uint32_t* data, uint64_t n, const uint32_t* sums) {
     if (i < n) data[i] += sums[i / kScanTile];
 }
 
-static void exclusive_scan(Workspace& ws, uint32_t* data, uint64_t n, cudaStream_t st) {
+// Returns -1 when a temporary could not be allocated (nothing is launched on it).
+static int exclusive_scan(Workspace& ws, uint32_t* data, uint64_t n, cudaStream_t st) {
     uint64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles <= 1) {
         k_scan_tile<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
         note_launch();
-        return;
+        return 0;
     }
     uint32_t* sums = ws.take_u32(tiles);
+    if (!sums) return -1;
     k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, st>>>(data, n, sums);
     note_launch();
-    exclusive_scan(ws, sums, tiles, st);
+    if (exclusive_scan(ws, sums, tiles, st) != 0) return -1;
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(data, n, sums);
     note_launch();
+    return 0;
 }
 
 int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
@@ -273,12 +276,19 @@ int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*&
     const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
     size_t mark = ws.mark();
     uint32_t* hist = ws.take_u32((uint64_t)ntiles * 256);
+    if (!hist) {
+        ws.release(mark);
+        return -1;
+    }
     int passes = 0;
     for (int shift = 0; shift < 64; shift += 8) {
         if (((varying_bits >> shift) & 255ull) == 0ull) continue;  // digit constant over all keys
         k_rs_hist<<<ntiles, kRsThreads, 0, st>>>(keys, n, shift, hist, ntiles);
         note_launch();
-        exclusive_scan(ws, hist, (uint64_t)ntiles * 256, st);
+        if (exclusive_scan(ws, hist, (uint64_t)ntiles * 256, st) != 0) {
+            ws.release(mark);
+            return -1;
+        }
         k_rs_scatter<<<ntiles, kRsThreads, 0, st>>>(keys, vals, keys_alt, vals_alt, n, shift, hist, ntiles);
         note_launch();
         std::swap(keys, keys_alt);
@@ -1392,6 +1402,7 @@ int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st) {
     m.nboxes = off;
     m.box_lo = (float4*)ws.alloc_persistent(m.box_lo, m.box_cap, off);
     m.box_hi = (float4*)ws.alloc_persistent(m.box_hi, m.box_cap_hi, off);
+    if (!m.box_lo || !m.box_hi) return -1;
     uint64_t nl = m.lvl_cnt[0];
     k_leaf_boxes<<<(unsigned)((nl * 32 + 255) / 256), 256, 0, st>>>(m.a, n, m.box_lo, m.box_hi, nl);
     note_launch();
@@ -1407,6 +1418,7 @@ int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st) {
 
 int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st) {
     unsigned* box = ws.scratch_box();
+    if (!box) return -1;
     unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
     cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 4096);
@@ -1459,7 +1471,7 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     }
     if (n >= (1ull << 32)) return -1;  // record ids are 32-bit
     float lo[3], hi[3];
-    compute_bbox(ws, rec.a, n, lo, hi, st);
+    if (compute_bbox(ws, rec.a, n, lo, hi, st) != 0) return -1;
     m.grid = make_key_grid(lo, hi);
     cudaStreamSynchronize(st);
     if (n > m.a_cap) release_map_index(m);  // else every array is reused in place
@@ -1479,8 +1491,7 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     k_finalize<<<blocks, 256, 0, st>>>(m.a, m.b, rec.fwi ? m.fwi : nullptr, rec.fwi ? m.sfi : nullptr,
                                        rec.id ? m.id : nullptr, rec.sco ? m.sco : nullptr, rec, n);
     note_launch();
-    build_box_tree(ws, m, st);
-    return 0;
+    return build_box_tree(ws, m, st);
 }
 
 // Single-cell index build into caller-provided device memory (no allocation): the k-d
@@ -1523,6 +1534,10 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, 
     uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals2 = ws.take_u32(n);
     unsigned long long* oa = (unsigned long long*)ws.scratch_box();
+    if (!keys || !keys2 || !vals2 || !oa) {  // nothing launched on a failed allocation
+        ws.release(mark);
+        return -1;
+    }
     unsigned long long init[2] = {0ull, ~0ull};
     cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
@@ -1533,7 +1548,10 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, 
     cudaStreamSynchronize(st);
     uint64_t* k0 = keys;
     uint32_t* v0 = vals;
-    radix_sort_pairs(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st);
+    if (radix_sort_pairs(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st) < 0) {
+        ws.release(mark);
+        return -1;
+    }
     if (v0 != perm) cudaMemcpyAsync(perm, v0, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
     ws.release(mark);
     return 0;
