@@ -552,16 +552,23 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
     bool want_sco = ctx->sc.adjoint != 0;
     if (r.cap >= need && (!want_id || r.id) && (!want_hm || r.fwi) && (!want_sco || r.sco)) return ALB_OK;
     uint64_t cap = std::max<uint64_t>(need + need / 16, 1024);
-    float4 *a, *b, *fwi = nullptr, *sfi = nullptr, *sco = nullptr;
-    uint32_t* id = nullptr;
-    CK(cudaMalloc(&a, cap * 16));
-    CK(cudaMalloc(&b, cap * 16));
-    if (want_hm) {
-        CK(cudaMalloc(&fwi, cap * 16));
-        CK(cudaMalloc(&sfi, cap * 16));
+    if (!keep) {  // nothing to copy: release the old store first, so the peak is one store
+        CK(cudaStreamSynchronize(ctx->st));
+        cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
+        r = RecordStore{};
     }
-    if (want_id) CK(cudaMalloc(&id, cap * 4));
-    if (want_sco) CK(cudaMalloc(&sco, cap * 16));
+    float4 *a = nullptr, *b = nullptr, *fwi = nullptr, *sfi = nullptr, *sco = nullptr;
+    uint32_t* id = nullptr;
+    // every allocation is checked, and a failure frees what this call had taken
+    bool ok = cudaMalloc(&a, cap * 16) == cudaSuccess && cudaMalloc(&b, cap * 16) == cudaSuccess;
+    if (ok && want_hm) ok = cudaMalloc(&fwi, cap * 16) == cudaSuccess && cudaMalloc(&sfi, cap * 16) == cudaSuccess;
+    if (ok && want_id) ok = cudaMalloc(&id, cap * 4) == cudaSuccess;
+    if (ok && want_sco) ok = cudaMalloc(&sco, cap * 16) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cudaFree(a); cudaFree(b); cudaFree(fwi); cudaFree(sfi); cudaFree(id); cudaFree(sco);
+        return fail(ctx, ALB_ERR_CUDA, "photon-map store: out of device memory");
+    }
     if (keep) {
         CK(cudaMemcpyAsync(a, r.a, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
         CK(cudaMemcpyAsync(b, r.b, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
@@ -610,9 +617,12 @@ static int restore_records(AlbCtx* ctx, int c, uint64_t need) {
 static int ensure_queries(AlbCtx* ctx, int k, uint64_t need) {
     if (ctx->qcap[k] >= need && (!ctx->keep_ids || ctx->qid[k]) && (!ctx->sc.adjoint || ctx->qs[k])) return ALB_OK;
     uint64_t cap = std::max<uint64_t>(need + need / 4, 1024);
+    CK(cudaStreamSynchronize(ctx->st));
     cudaFree(ctx->qa[k]); cudaFree(ctx->qb[k]); cudaFree(ctx->qc[k]); cudaFree(ctx->qid[k]); cudaFree(ctx->qperm[k]);
     cudaFree(ctx->qrk[k][0]); cudaFree(ctx->qrk[k][1]); cudaFree(ctx->qs[k]);
+    ctx->qa[k] = ctx->qb[k] = ctx->qc[k] = nullptr; ctx->qperm[k] = nullptr;
     ctx->qid[k] = nullptr; ctx->qrk[k][0] = ctx->qrk[k][1] = nullptr; ctx->qs[k] = nullptr;
+    ctx->qcap[k] = 0;
     CK(cudaMalloc(&ctx->qa[k], cap * 16));
     CK(cudaMalloc(&ctx->qb[k], cap * 16));
     CK(cudaMalloc(&ctx->qc[k], cap * 16));
@@ -1288,6 +1298,7 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
     std::condition_variable mem_cv;
     double held_total = 0.0, rpp_seen = 0.0;
     int running = 0;
+    int exclusive = 0;  // workers waiting to rerun an instance alone; the others hold no memory then
     auto need_of = [&](const AlbBatchInstance& I) {
         const double rpp = rpp_seen > 0.0 ? 1.5 * rpp_seen : 200.0;
         return (double)I.n_forward * rpp * bytes_per_record + 64.0 * 1048576.0;
@@ -1311,7 +1322,7 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
             {
                 std::unique_lock<std::mutex> g(mem_mu);
                 const double need = need_of(I);
-                if (ctx && held > (double)(1 << 30) && 4.0 * need < held) {  // shrink for the small tail
+                auto drop_ctx = [&]() {  // release this worker's context and its device memory
                     g.unlock();
                     alb_destroy(ctx);
                     ctx = nullptr;
@@ -1319,13 +1330,26 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                     held_total -= held;
                     held = 0.0;
                     mem_cv.notify_all();
+                };
+                while (true) {
+                    if (!alone && exclusive > 0) {  // another worker reruns an instance alone
+                        if (ctx) drop_ctx();
+                        mem_cv.wait(g, [&] { return exclusive == 0; });
+                        continue;
+                    }
+                    if (ctx && held > (double)(1 << 30) && 4.0 * need < held) drop_ctx();  // small tail
+                    const double grow = std::max(0.0, need - held);
+                    mem_cv.wait(g, [&] {
+                        if (!alone && exclusive > 0) return true;
+                        return alone ? running == 0 : (held_total + grow <= budget || running == 0);
+                    });
+                    if (!alone && exclusive > 0) continue;
+                    held_total += grow;
+                    held += grow;
+                    shared = running > 0;
+                    ++running;
+                    break;
                 }
-                const double grow = std::max(0.0, need - held);
-                mem_cv.wait(g, [&] { return alone ? running == 0 : (held_total + grow <= budget || running == 0); });
-                held_total += grow;
-                held += grow;
-                shared = running > 0;
-                ++running;
             }
             if (!ctx) {
                 rc = alb_create(I.scene, opt->device, &ctx);
@@ -1396,9 +1420,16 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                 }
             }
             // Device memory is admitted on an estimate: an instance that failed for memory
-            // (an allocation or a map build) while others were running is run once more, alone.
+            // (an allocation or a map build) while others were running is run once more,
+            // alone, once every other worker has released its context.
             const bool memory = rc == ALB_ERR_CUDA || rc == ALB_ERR_CAPACITY;
+            const bool was_alone = alone;
             alone = memory && shared && !alone && cudaGetLastError() != cudaErrorIllegalAddress;
+            if (alone || was_alone) {
+                std::lock_guard<std::mutex> m(mem_mu);
+                exclusive += alone ? 1 : -1;
+                mem_cv.notify_all();
+            }
         }
         if (ctx) alb_destroy(ctx);
         {
