@@ -22,3 +22,44 @@ def test_secondary_measurement_failure_is_recorded():
 
     assert bench.measured(lambda a, b: a + b, 2, 3) == 5
     assert bench.measured(boom, 7) == {"error": "RuntimeError: no device 7"}
+
+
+def test_reference_config_carries_every_field():
+    """The reference's own SimulationConfig built from the bench workload's has the same
+    value in every field the reference defines (it is what the reference arm times)."""
+    import dataclasses
+    import sys
+
+    import pytest
+
+    from fixtures import reference_src
+
+    src = reference_src()
+    if not src:
+        pytest.skip("reference sources not present")
+    sys.path.insert(0, src)
+    bench = _bench()
+    from pyalbsim_gb300.workloads import large
+
+    ours = large()
+    ref = bench._reference_config(ours)
+    assert type(ref).__module__.startswith("alb_sim.")
+
+    def compare(a, b):
+        if dataclasses.is_dataclass(b):
+            for f in dataclasses.fields(b):
+                compare(getattr(a, f.name), getattr(b, f.name))
+        elif isinstance(b, tuple):
+            assert len(a) == len(b)
+            for x, y in zip(a, b):
+                compare(x, y)
+        else:
+            assert a == b
+
+    compare(ours, ref)
+    with pytest.raises(ValueError):  # an extension field set has no counterpart in the reference
+        bench._reference_config(large(hg=0.9))
+
+
+def test_cpu_model_is_reported():
+    assert isinstance(_bench().cpu_model(), str) and _bench().cpu_model()
