@@ -260,7 +260,10 @@ int alb_export_map_scores(AlbCtx* ctx, int channel, float* scores, size_t n);
  * traced and gathered (Philox streams keyed by seed, photon ids from 0). `streams` host
  * workers each own a context on its own non-blocking CUDA stream and take instances from a
  * shared queue, largest (n_forward + n_backward) first, so small instances overlap on the
- * GPU; a context keeps its device buffers from one instance to the next. Results: the
+ * GPU; a context keeps its device buffers from one instance to the next. Device memory is
+ * admitted on an estimate of each instance's footprint; an instance that fails for device
+ * memory while others were running is run once more alone, after every other worker has
+ * released its buffers. Results: the
  * float64 waveform [ALB_CHANNELS][2*steps] of each instance and, with adjoint set, its
  * Jacobian [ALB_ADJ_PARAMS-1][ALB_CHANNELS][2*steps] (parameters 1..5; nullable). The
  * call returns ALB_OK once every instance has run; each instance's own result is in
