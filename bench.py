@@ -660,8 +660,11 @@ def sweep_measure(every: int = 32, streams: int = 8):
     torch.cuda.synchronize()
     _, _, st, _, wall = run_batch(inst, streams=streams)
     photons = sum(x.n_forward + x.n_backward for x in inst)
+    codes = {-1: "invalid", -2: "too_few_records_for_k", -3: "capacity", -4: "cuda", -5: "iteration_cap"}
+    failed = {codes.get(int(c), str(int(c))): int((st == c).sum()) for c in np.unique(st) if c != 0}
     out = {"instances": len(inst), "of": 4096, "photons": int(photons), "wall_s": wall,
-           "value": photons / wall, "unit": "photons/s", "failed": int((st != 0).sum()), "streams": streams}
+           "value": photons / wall, "unit": "photons/s", "failed": int((st != 0).sum()), "failed_by_status": failed,
+           "streams": streams}
     smalls = hypercube_instances(base, 64, seed=7, photons=(1e5, 1e5 + 1))
     t1 = run_batch(smalls, streams=1)[4]
     tn = run_batch(smalls, streams=streams)[4]
