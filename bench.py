@@ -673,9 +673,10 @@ def sweep_measure(every: int = 32, streams: int = 8):
     return out
 
 
-def e2e_measure(cfg, nf, nb):
+def e2e_measure(cfg, nf, nb, repeats: int = 3):
     """Throughput through the public drop-in call run_linear (context creation, table
-    upload, traces, gathers and the host copy of the float32 waveforms inside the clock)."""
+    upload, traces, gathers and the host copy of the float32 waveforms inside the clock):
+    the median of ``repeats`` calls, each one timed step, with every call's rate listed."""
     from pyalbsim_gb300.config import RunConfig
     from pyalbsim_gb300.execution.linear import run_linear
     from pyalbsim_gb300.scene import build_scene
@@ -684,14 +685,17 @@ def e2e_measure(cfg, nf, nb):
     import io
 
     rc = RunConfig(photons_per_batch_forward=nf, photons_per_batch_backward=nb, batches_forward=1, batches_backward=1)
-    t0 = time.perf_counter()
-    with contextlib.redirect_stdout(io.StringIO()):
-        w = run_linear(cfg, rc, rng=np.random.default_rng(1))
-    dt = time.perf_counter() - t0
+    rates = []
+    for r in range(repeats):
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            w = run_linear(cfg, rc, rng=np.random.default_rng(1 + r))
+        rates.append((nf + nb) / (time.perf_counter() - t0))
     scene = build_scene(cfg)
     h2d = len(scene.layers) * (3 * 18000 * 8 + 18000 * 8)  # phase theta, cdf, slope, weight tables
     d2h = sum(a.nbytes for a in w.values())
-    return {"value": (nf + nb) / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+    return {"value": float(np.median(rates)), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "runs": rates}
 
 
 if __name__ == "__main__":
