@@ -99,11 +99,16 @@ typedef struct AlbLayer {
     /* Adjoint (extension, no counterpart in the reference). d ln(alpha)/d theta and
      * d ln(ssa)/d theta for theta = (a, b, g) of this layer, g the Henyey-Greenstein
      * asymmetry; hg_g != 0 marks an HG layer (its phase sampling and gather weight depend
-     * on g); dlog_weight_g (ALB_PHASE_DIVISIONS, nullable) = d ln(scatter_weight)/dg. */
+     * on g); dlog_weight_g (ALB_PHASE_DIVISIONS, nullable) = d ln(scatter_weight)/dg.
+     * dlog_sample_g (ALB_PHASE_DIVISIONS, nullable) = d ln(mass)/dg of each interval of the
+     * sampling table, interval i holding the angles in (phase_theta[i-1], phase_theta[i]]
+     * (i = 0: phase_theta[0]): the score of a drawn angle. NULL falls back to the analytic
+     * d ln p_HG(mu)/dg, which is biased when the HG peak is narrow against the grid. */
     double dlog_alpha[3];
     double dlog_ssa[3];
     double hg_g;
     const double* dlog_weight_g;
+    const double* dlog_sample_g;
 } AlbLayer;
 
 /* Scene constants derived on the host from SimulationConfig. */

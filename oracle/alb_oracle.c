@@ -234,16 +234,22 @@ static float water_ssa(const Model* m, double y) {
 static double schlick(double f0, double c) { return f0 + (1.0 - f0) * pow(1.0 - c, 5.0); }
 
 /* numpy.interp(u, cdf, theta) */
-static double interp(const AlbLayer* L, double u) {
+/* numpy.interp(u, cdf, theta); *interval gets the table interval of the result: 0 below
+ * cdf[0], i + 1 for cdf[i] <= u < cdf[i + 1] (the index of dlog_sample_g, the score of an
+ * angle drawn from the tabulated CDF) */
+static double interp(const AlbLayer* L, double u, int* interval) {
     const double* xp = L->phase_cdf;
     const double* fp = L->phase_theta;
+    *interval = 0;
     if (u < xp[0]) return fp[0];
+    *interval = NDIV - 1;
     if (u >= xp[NDIV - 1]) return fp[NDIV - 1];
     int lo = 0, hi = NDIV - 1;
     while (hi - lo > 1) {
         int mid = (lo + hi) / 2;
         if (xp[mid] <= u) lo = mid; else hi = mid;
     }
+    *interval = lo + 1;
     if (u == xp[lo]) return fp[lo];
     double slope = (fp[lo + 1] - fp[lo]) / (xp[lo + 1] - xp[lo]);
     return slope * (u - xp[lo]) + fp[lo];
@@ -428,13 +434,16 @@ static void trace_one(const Model* m, int pass, Src* s, Ph* ph, int photon, OrBu
                     phi = TWO_PI * u01(b.y);
                     nt = tau_of(u01(b.z));
                 }
-                double th = interp(&P->layers[L], uth);
+                int interval;
+                double th = interp(&P->layers[L], uth, &interval);
                 double lv[3] = {sin(th) * cos(phi), sin(th) * sin(phi), cos(th)};
                 double nd[3];
                 rot_apply(ph->d, lv, nd);
                 for (int i = 0; i < 3; ++i) ph->d[i] = nd[i];
                 for (int i = 0; i < 3; ++i) ph->sc[i] += P->layers[L].dlog_ssa[i];
-                if (P->layers[L].hg_g != 0.0) ph->sc[2] += hg_dlogp(P->layers[L].hg_g, cos(th));
+                if (P->layers[L].hg_g != 0.0)
+                    ph->sc[2] += P->layers[L].dlog_sample_g ? P->layers[L].dlog_sample_g[interval]
+                                                            : hg_dlogp(P->layers[L].hg_g, cos(th));
                 ph->E = ph->E * water_ssa(m, ph->p[1]);
                 ph->tau = ph->tau - ph->taut;
                 ph->taut = nt;

@@ -66,6 +66,7 @@ class AlbLayer(C.Structure):
         ("dlog_ssa", C.c_double * 3),
         ("hg_g", C.c_double),
         ("dlog_weight_g", C.POINTER(C.c_double)),
+        ("dlog_sample_g", C.POINTER(C.c_double)),
     ]
 
 
@@ -303,6 +304,10 @@ def scene_struct(scene: SceneModel):
             dw = np.ascontiguousarray(layer.dlog_weight_g, dtype=np.float64)
             keep.append(dw)
             L.dlog_weight_g = dw.ctypes.data_as(C.POINTER(C.c_double))
+        if getattr(layer, "dlog_sample_g", None) is not None:
+            ds = np.ascontiguousarray(layer.dlog_sample_g, dtype=np.float64)
+            keep.append(ds)
+            L.dlog_sample_g = ds.ctypes.data_as(C.POINTER(C.c_double))
     return p, keep
 
 

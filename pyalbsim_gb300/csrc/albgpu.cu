@@ -126,7 +126,7 @@ struct AlbCtx {
     int64_t wf_bins = 0, jac_bins = 0, hm_cells = 0, hm_radius_cells = 0;  // accumulator capacities
     // per-layer scene tables (device), reused when the context takes a new scene
     struct LayerTables {
-        void *th = nullptr, *cdf = nullptr, *sl = nullptr, *w = nullptr, *dlw = nullptr, *inv = nullptr;
+        void *th = nullptr, *cdf = nullptr, *sl = nullptr, *w = nullptr, *dlw = nullptr, *dsg = nullptr, *inv = nullptr;
     } lt[ALB_MAX_LAYERS];
     bool keep_records = false;  // keep the append stores after indexing (batched runs)
     // exit states
@@ -330,6 +330,16 @@ static std::string set_scene(AlbCtx* ctx, const AlbSceneParams* p) {
             cudaStreamSynchronize(ctx->st);
             s.layer_dlw_g[l] = dd;
         }
+        s.layer_dsg[l] = nullptr;
+        if (L.dlog_sample_g) {
+            std::vector<float> d(N);
+            for (int i = 0; i < N; ++i) d[i] = (float)L.dlog_sample_g[i];
+            float* dd = (float*)table_buf(ctx->lt[l].dsg, N * sizeof(float));
+            if (!dd) return std::string("table allocation failed");
+            cudaMemcpyAsync(dd, d.data(), N * sizeof(float), cudaMemcpyHostToDevice, ctx->st);
+            cudaStreamSynchronize(ctx->st);
+            s.layer_dsg[l] = dd;
+        }
         s.layer_bottom[l] = L.bottom_depth;
         s.layer_speed[l] = L.speed;
         s.layer_alpha[l] = L.alpha;
@@ -500,7 +510,7 @@ extern "C" void alb_destroy(AlbCtx* ctx) {
     }
     cudaFree(ctx->wf); cudaFree(ctx->hm); cudaFree(ctx->hm_radius); cudaFree(ctx->jac);
     for (auto& t : ctx->lt) {
-        cudaFree(t.th); cudaFree(t.cdf); cudaFree(t.sl); cudaFree(t.w); cudaFree(t.dlw); cudaFree(t.inv);
+        cudaFree(t.th); cudaFree(t.cdf); cudaFree(t.sl); cudaFree(t.w); cudaFree(t.dlw); cudaFree(t.dsg); cudaFree(t.inv);
     }
     cudaFree(ctx->ex_pos); cudaFree(ctx->ex_dir); cudaFree(ctx->ex_f);
     cudaFree(ctx->d_rec_count); cudaFree(ctx->d_q_count); cudaFree(ctx->d_err); cudaFree(ctx->d_stats);

@@ -70,6 +70,7 @@ struct SceneDev {
     float adj_dls[ALB_MAX_LAYERS][3];  // d ln(ssa) / d theta
     float layer_hg_g[ALB_MAX_LAYERS];  // HG asymmetry (0: not an HG layer)
     const float* layer_dlw_g[ALB_MAX_LAYERS];  // d ln(scatter weight) / dg per bin
+    const float* layer_dsg[ALB_MAX_LAYERS];    // d ln(mass) / dg per sampling interval (nullable)
     float inv_albedo;                  // 1 / seafloor albedo (0 when the albedo is 0)
     float dla2_drough;                 // d (GGX alpha^2) / d roughness = 4 roughness^3
 };

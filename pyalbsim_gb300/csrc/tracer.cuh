@@ -74,11 +74,23 @@ ALB_DEVICE void score_scatter_density(const SceneDev& sc, Score& s, int L) {
     s.b += sc.adj_dla[L][1];
     s.g += sc.adj_dla[L][2];
 }
-ALB_DEVICE void score_scatter_after(const SceneDev& sc, Score& s, int L, float mu) {
+// An HG angle is drawn from the tabulated CDF: its score is the g-derivative of the log-mass
+// of the table interval it fell in (`interval`, from the CDF search or the angle); the
+// analytic d ln p_HG(mu)/dg only when the scene carries no such table.
+ALB_DEVICE void score_scatter_after(const SceneDev& sc, Score& s, int L, float mu, int interval) {
     s.a += sc.adj_dls[L][0];
     s.b += sc.adj_dls[L][1];
     s.g += sc.adj_dls[L][2];
-    if (sc.layer_hg_g[L] != 0.f) s.g += hg_dlogp_dg(sc.layer_hg_g[L], mu);
+    if (sc.layer_hg_g[L] != 0.f)
+        s.g += sc.layer_dsg[L] ? __ldg(sc.layer_dsg[L] + interval) : hg_dlogp_dg(sc.layer_hg_g[L], mu);
+}
+
+// Table interval of an angle drawn by the float32 tracer (from the angle: interval i holds
+// (theta_{i-1}, theta_i] on the uniform angle grid).
+ALB_DEVICE int sample_interval_of_angle(const SceneDev& sc, int L, float th) {
+    const double t0 = sc.layer_theta[L][0], dt = sc.layer_theta[L][1] - t0;
+    const int i = (int)ceil(((double)th - t0) / dt);
+    return min(max(i, 0), ALB_PHASE_DIVISIONS - 1);
 }
 
 ALB_DEVICE void set_err(int* err, int code) { atomicCAS(err, 0, code); }
@@ -389,18 +401,23 @@ ALB_DEVICE int64_t tau_run(float& tau, double inc, float target, int64_t nmax) {
 
 // numpy.interp(u, cdf, theta) restated: linear interpolation with the reference's slope
 // table, left/right clamping (alb_sim/physics/scatter/direction.py:35-36).
-ALB_DEVICE double interp_theta(const SceneDev& sc, int layer, double u) {
+// numpy.interp(u, cdf, theta); `interval` receives the table interval of the result (see
+// score_scatter_after): 0 below cdf[0], i + 1 for cdf[i] <= u < cdf[i + 1].
+ALB_DEVICE double interp_theta(const SceneDev& sc, int layer, double u, int& interval) {
     const double* cdf = sc.layer_cdf[layer];
     const double* th = sc.layer_theta[layer];
     const double* sl = sc.layer_slope[layer];
     const int n = ALB_PHASE_DIVISIONS;
+    interval = 0;
     if (u < cdf[0]) return th[0];
+    interval = n - 1;
     if (u >= cdf[n - 1]) return th[n - 1];
     int lo = 0, hi = n - 1;  // invariant cdf[lo] <= u < cdf[hi]
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
         if (cdf[mid] <= u) lo = mid; else hi = mid;
     }
+    interval = lo + 1;
     if (u == cdf[lo]) return th[lo];
     return __dadd_rn(__dmul_rn(sl[lo], __dsub_rn(u, cdf[lo])), th[lo]);
 }
@@ -663,7 +680,8 @@ ALB_DEVICE void handle_scatter(const SceneDev& sc, const TraceOut& out, Ph& ph, 
     double uth, phi;
     float new_target;
     draw_scatter(src, uth, phi, new_target);
-    double th = interp_theta(sc, L, uth);
+    int interval;
+    double th = interp_theta(sc, L, uth, interval);
     double st, ct, sp, cp;
     sincos(th, &st, &ct);
     sincos(phi, &sp, &cp);
@@ -671,7 +689,7 @@ ALB_DEVICE void handle_scatter(const SceneDev& sc, const TraceOut& out, Ph& ph, 
     double ox, oy, oz;
     rotate_from_z(ph.dx, ph.dy, ph.dz, l0, l1, l2, ox, oy, oz);
     ph.dx = ox; ph.dy = oy; ph.dz = oz;
-    if (sc.adjoint) score_scatter_after(sc, ph.sc, L, (float)ct);
+    if (sc.adjoint) score_scatter_after(sc, ph.sc, L, (float)ct, interval);
     ph.E = __fmul_rn(ph.E, water_ssa(sc, ph.py));
     ph.tau = __fsub_rn(ph.tau, ph.taut);
     ph.taut = new_target;

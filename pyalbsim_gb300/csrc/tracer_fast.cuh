@@ -232,7 +232,7 @@ ALB_DEVICE void trace_photon_fast(const SceneDev& sc, const FastScene& fs, const
             ph.dx = fmaf(ctt, ph.dx, st * ux);
             ph.dy = fmaf(ctt, ph.dy, st * uy);
             ph.dz = fmaf(ctt, ph.dz, st * uz);
-            if (sc.adjoint) score_scatter_after(sc, ph.sc, L2, ctt);
+            if (sc.adjoint) score_scatter_after(sc, ph.sc, L2, ctt, sample_interval_of_angle(sc, L2, th));
             ph.E *= sc.layer_prof[L2] ? water_ssa(sc, (double)ph.py) : sc.layer_ssa[L2];
             ph.tau = fmaxf(ph.tau - ph.taut, 0.f);
             ph.taut = -__logf(uf(b.z));

@@ -389,3 +389,37 @@ def test_oracle_columns_match_reference_simulator_differences(job):
     r = oracle_run(scene, int(d["n_fwd"]), int(d["n_bwd"]), replay_fwd=replay_streams(d, "fwd"),
                    replay_bwd=replay_streams(d, "bwd"), adjoint=True)
     assert_columns_match_reference_differences(r["jacobian"], d, job)
+
+
+@pytest.mark.parametrize("g", [0.8, 0.9, 0.99])
+def test_hg_sample_score_is_the_table_score(g):
+    """The HG angle score is d ln(mass)/dg of the drawn table interval: its mean under the
+    table's own distribution is zero, and it equals a central difference of the interval
+    log-masses. The analytic d ln p_HG(mu)/dg averages +0.70 per scatter there at g = 0.99."""
+    from pyalbsim_gb300.scene import hg_sample_dlog_g
+
+    s = hg_sample_dlog_g(g)
+    _, _, cdf = henyey_greenstein_table(g)
+    mass = np.diff(np.r_[0.0, cdf])
+    assert abs((mass * s).sum()) < 1e-9 * np.sqrt((mass * s * s).sum())
+    h = 1e-6
+    mp = np.diff(np.r_[0.0, henyey_greenstein_table(g + h)[2]])
+    mm = np.diff(np.r_[0.0, henyey_greenstein_table(g - h)[2]])
+    # the real difference of masses taken from CDF values near 1 loses digits where the
+    # mass is small (the complex step does not): compare where it keeps ~6 of them
+    ok = mass > 1e-6
+    fd = (np.log(mp[ok]) - np.log(mm[ok])) / (2 * h)
+    np.testing.assert_allclose(s[ok], fd, rtol=1e-5, atol=1e-5 * np.abs(fd).max())
+
+
+def test_oracle_hg_scores_use_the_table():
+    """HG records carry the table score: a scene whose layer has no table falls back to the
+    analytic score, and at g = 0.99 the two differ in the mean per scatter."""
+    cfg = _hg_cfg(0.99)
+    scene = build_scene(cfg)
+    assert scene.layers[0].dlog_sample_g is not None
+    with_table = oracle_run(scene, 400, 10, seed=5, adjoint=True)["maps"][1]["score"][:, 2]
+    scene.layers[0].dlog_sample_g = None
+    analytic = oracle_run(scene, 400, 10, seed=5, adjoint=True)["maps"][1]["score"][:, 2]
+    assert len(with_table) == len(analytic) > 100
+    assert not np.allclose(with_table, analytic)
