@@ -856,7 +856,7 @@ extern "C" int alb_trace(AlbCtx* ctx, int pass, uint64_t n, uint64_t seed, uint6
             q.retries = ctx->d_stats + 30;
             if (ctx->sort_q) {
                 PhaseTimer ps(ctx, 3);
-                const int src = sort_queries(ctx->ws, ctx->qa[k], nq, ctx->map[c].grid, ctx->qperm[k], ctx->st);
+                const int src = sort_queries(ctx->ws, ctx->qa[k], nq, ctx->qperm[k], ctx->st);
                 ps.stop();
                 if (src != 0) return fail(ctx, ALB_ERR_CUDA, "query sort: device memory allocation failed");
                 q.perm = ctx->qperm[k];

@@ -53,7 +53,6 @@ struct MapIndex {
     uint32_t* id = nullptr;
     float4* sco = nullptr;
     uint64_t a_cap = 0, b_cap = 0, fwi_cap = 0, sfi_cap = 0, id_cap = 0, sco_cap = 0;
-    KeyGrid grid{};
     float4* box_lo = nullptr;
     float4* box_hi = nullptr;
     uint64_t box_cap = 0, box_cap_hi = 0, nboxes = 0;
@@ -130,15 +129,14 @@ class Workspace {
 };
 
 // ---- map build (mapbuild.cu)
-KeyGrid make_key_grid(const float lo[3], const float hi[3]);
+KeyGrid make_key_grid(const float lo[3], const float hi[3], int bits3, int bits2);
 int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
                      uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st);
 int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st);
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st);
 void release_map_index(MapIndex& m);
 int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st);
-int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, uint32_t* perm,
-                 cudaStream_t st);
+int sort_queries(Workspace& ws, const float4* qa, uint64_t n, uint32_t* perm, cudaStream_t st);
 
 // ---- tracer (tracer.cu)
 struct FastScene;

@@ -1,11 +1,13 @@
 // Photon-map index build: the GPU replacement of build_photon_map_data + PhotonMapIndex
 // (alb_sim/photon_mapping/build_photon_map_data.py:8-62, photon_map_index.py:6-17).
 //
-// Records are ordered along a Morton curve of a uniform grid over the map's bounding box
-// (cell key = interleaved cell coordinates, 32 bits) by an LSD radix sort, permuted into
-// that order as two float4 streams, and cut into buckets of 32 consecutive records. A
-// bucket's bounding box is a leaf; 32 consecutive boxes form the next level up, until 32
-// or fewer boxes remain. The gather walks this implicit 32-ary box tree warp-wide.
+// Records are put in an exact left-balanced k-d order (median splits on each node's widest
+// axis, 32-record leaves; streaming partition passes over the whole map for the upper levels,
+// one CTA per node of at most 4096 records for the rest), permuted into that order as two
+// float4 streams, and cut into leaves of 32 consecutive records. A leaf's bounding box is a
+// leaf box; 32 consecutive boxes form the next level up, until 32 or fewer boxes remain. The
+// gather walks this implicit 32-ary box tree warp-wide. The same file sorts the gather
+// queries along a Morton curve (LSD radix sort of interleaved cell coordinates).
 #include <atomic>
 #include <algorithm>
 #include <cstdio>
@@ -993,6 +995,9 @@ __global__ void __launch_bounds__(kCellThreads) k_local_kd(float4* X, const unsi
 // from segmented warp reductions.
 constexpr int kFullCell = 4096;
 constexpr int kFullThreads = 512;
+// levels whose nodes hold at least this many records are split by a radix partition, the
+// smaller ones by a bitonic sort inside a warp
+constexpr unsigned kPartitionMin = 512;
 
 struct FullCellSmem {
     float X[kFullCell], Y[kFullCell], Z[kFullCell];
@@ -1000,6 +1005,79 @@ struct FullCellSmem {
     uint32_t sk[kFullCell];
     unsigned blo[3 * 64], bhi[3 * 64];
 };
+
+// Bitonic compare-exchange of a thread's 8 consecutive keys at a stride JJ < 8 (partners in
+// the same thread; a compile-time stride keeps the keys in registers).
+template <int JJ>
+ALB_DEVICE void exchange_in_thread(uint32_t (&key)[8], int t, unsigned kk, unsigned S) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        if ((e & JJ) == 0) {
+            const int f = e | JJ;
+            const unsigned i = (unsigned)(t * 8 + e);
+            const bool up = kk == S || (i & kk) == 0;
+            const uint32_t a = key[e], b = key[f];
+            if ((a > b) == up) {
+                key[e] = b;
+                key[f] = a;
+            }
+        }
+    }
+}
+
+// One warp: the bin of the need-th (1-based) entry of a 256-bin histogram h; need becomes the
+// entry's rank inside that bin.
+ALB_DEVICE unsigned pick_bin256(const uint32_t* h, unsigned& need) {
+    const int lane = threadIdx.x & 31;
+    uint32_t c[8], run = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        c[i] = h[lane * 8 + i];
+        run += c[i];
+    }
+    uint32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    uint32_t before = inc - run;
+    int bin = -1;
+    uint32_t below = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (bin < 0 && before + c[i] >= need) {
+            bin = lane * 8 + i;
+            below = before;
+        }
+        before += c[i];
+    }
+    const unsigned who = __ballot_sync(0xffffffffu, bin >= 0);
+    const int src = __ffs(who) - 1;
+    bin = __shfl_sync(0xffffffffu, bin, src);
+    below = __shfl_sync(0xffffffffu, below, src);
+    need -= below;
+    return (unsigned)bin;
+}
+
+// Exclusive prefix of v over the threads of this thread's node (an aligned block of tpn >= 64
+// threads, whole warps), in thread order. wsum: 16 words of shared scratch.
+ALB_DEVICE unsigned node_exclusive_scan(unsigned v, uint32_t* wsum, unsigned tpn) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    unsigned inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    const int w0 = (int)((t / tpn) * (tpn / 32));
+    unsigned before = 0;
+    for (int i = w0; i < w; ++i) before += wsum[i];
+    __syncthreads();  // wsum is reused by the next scan
+    return before + inc - v;
+}
 
 __global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, const unsigned* __restrict__ cstart) {
     extern __shared__ unsigned char smraw[];
@@ -1066,6 +1144,89 @@ __global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, c
             if (ext > 0.f) q = (uint32_t)fminf(fmaxf((V[j] - lo) / ext * 65535.f, 0.f), 65535.f);
             key[e] = (q << 13) | (uint32_t)j;
         }
+        if (S >= kPartitionMin) {
+            // Radix partition: the node's first half takes the S/2 records of smallest
+            // (coordinate, position) key, the same set a sort of the keys puts there, in
+            // position order; the second half the others. Two 256-bin histogram passes find
+            // the cut coordinate; records AT the cut go left in position order until the left
+            // half is full.
+            const unsigned nodes = (unsigned)kFullCell / S, tpn = S / 8, nstart = node * S;
+            uint32_t* h1 = s.sk;          // nodes x 256
+            uint32_t* h2 = s.sk + 2048;   // nodes x 256
+            uint32_t* sel = s.blo;        // per node: cut, records at the cut that go left
+            uint32_t* wsum = s.bhi;       // scan scratch (the boxes are consumed)
+            for (int i = t; i < (int)(nodes * 256); i += kFullThreads) {
+                h1[i] = 0u;
+                h2[i] = 0u;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int e = 0; e < 8; ++e) atomicAdd(&h1[node * 256 + (key[e] >> 21)], 1u);
+            __syncthreads();
+            const int w = t >> 5;
+            if (w < (int)nodes) {
+                unsigned need = S / 2;
+                const unsigned b = pick_bin256(h1 + w * 256, need);
+                if (lane == 0) {
+                    sel[2 * w] = b;
+                    sel[2 * w + 1] = need;
+                }
+            }
+            __syncthreads();
+            const unsigned hb = sel[2 * node];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                if ((key[e] >> 21) == hb) atomicAdd(&h2[node * 256 + ((key[e] >> 13) & 255u)], 1u);
+            __syncthreads();
+            if (w < (int)nodes) {
+                unsigned need = sel[2 * w + 1];
+                const unsigned lb = pick_bin256(h2 + w * 256, need);
+                __syncwarp();
+                if (lane == 0) {
+                    sel[2 * w] = (sel[2 * w] << 8) | lb;
+                    sel[2 * w + 1] = need;
+                }
+            }
+            __syncthreads();
+            const unsigned cut = sel[2 * node], at_left = sel[2 * node + 1];
+            unsigned nt = 0;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) nt += (key[e] >> 13) == cut ? 1u : 0u;
+            unsigned tr = node_exclusive_scan(nt, wsum, tpn);  // ties before this thread's
+            unsigned lmask = 0u;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const unsigned qe = key[e] >> 13;
+                bool left = qe < cut;
+                if (qe == cut) left = tr++ < at_left;
+                lmask |= (left ? 1u : 0u) << e;
+            }
+            unsigned lb4 = node_exclusive_scan((unsigned)__popc(lmask), wsum, tpn);  // lefts before
+            float rx[8], ry[8], rz[8];
+            uint32_t rid[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int j = t * 8 + e;
+                rx[e] = s.X[j];
+                ry[e] = s.Y[j];
+                rz[e] = s.Z[j];
+                rid[e] = s.ID[j];
+            }
+            __syncthreads();
+            const unsigned pos0 = (unsigned)(t * 8) - nstart;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const bool left = (lmask >> e) & 1u;
+                const unsigned dst = left ? nstart + lb4 : nstart + S / 2 + (pos0 + (unsigned)e - lb4);
+                lb4 += left ? 1u : 0u;
+                s.X[dst] = rx[e];
+                s.Y[dst] = ry[e];
+                s.Z[dst] = rz[e];
+                s.ID[dst] = rid[e];
+            }
+            __syncthreads();
+            continue;
+        }
         // bitonic sort of every node's block of S keys, ascending
         for (unsigned kk = 2; kk <= S; kk <<= 1) {
             for (unsigned jj = kk >> 1; jj > 0; jj >>= 1) {
@@ -1089,20 +1250,12 @@ __global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, c
                         const bool lower = (i & jj) == 0, up = kk == S || (i & kk) == 0;
                         key[e] = (lower == up) ? min(key[e], o) : max(key[e], o);
                     }
+                } else if (jj == 4) {
+                    exchange_in_thread<4>(key, t, kk, S);
+                } else if (jj == 2) {
+                    exchange_in_thread<2>(key, t, kk, S);
                 } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        if ((e & (int)jj) == 0) {
-                            const int f = e | (int)jj;
-                            const unsigned i = (unsigned)(t * 8 + e);
-                            const bool up = kk == S || (i & kk) == 0;
-                            const uint32_t a = key[e], b = key[f];
-                            if ((a > b) == up) {
-                                key[e] = b;
-                                key[f] = a;
-                            }
-                        }
-                    }
+                    exchange_in_thread<1>(key, t, kk, S);
                 }
             }
         }
@@ -1355,7 +1508,7 @@ __global__ void k_parent_boxes(const float4* __restrict__ clo, const float4* __r
 // host drivers
 // ------------------------------------------------------------------------------------------
 
-KeyGrid make_key_grid(const float lo[3], const float hi[3]) {
+KeyGrid make_key_grid(const float lo[3], const float hi[3], int bits3, int bits2) {
     KeyGrid g{};
     float ext[3], emax = 0.f;
     for (int k = 0; k < 3; ++k) {
@@ -1369,7 +1522,7 @@ KeyGrid make_key_grid(const float lo[3], const float hi[3]) {
         if (ext[k] > 1e-6f * std::max(emax, 1e-30f) && ext[k] > 0.f) g.ax[na++] = k;
     }
     g.naxes = na;
-    int bits = na == 3 ? 21 : 32;  // 63-bit keys in 3-D, 64-bit for planar maps
+    const int bits = na == 3 ? bits3 : bits2;
     for (int k = 0; k < 3; ++k) {
         bool active = false;
         for (int j = 0; j < na; ++j) active |= (g.ax[j] == k);
@@ -1472,7 +1625,6 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     if (n >= (1ull << 32)) return -1;  // record ids are 32-bit
     float lo[3], hi[3];
     if (compute_bbox(ws, rec.a, n, lo, hi, st) != 0) return -1;
-    m.grid = make_key_grid(lo, hi);
     cudaStreamSynchronize(st);
     if (n > m.a_cap) release_map_index(m);  // else every array is reused in place
     m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);
@@ -1525,9 +1677,16 @@ void launch_single_cell_index(const float4* pts, uint32_t n, const uint32_t* per
 }
 
 // Spatial order of gather queries under a map's key grid (for cache locality).
-int sort_queries(Workspace& ws, const float4* qa, uint64_t n, const KeyGrid& g, uint32_t* perm,
-                 cudaStream_t st) {
+// The queries are ordered along a Morton curve over their own bounding box: over the map's
+// box, queries far from a compact map (surface-reflection queries around the laser spot)
+// would clamp to its edge and lose their order. 10 bits per axis in 3-D and 16 in 2-D make
+// cells far finer than any k-th-neighbour distance with half the radix passes of full-width
+// keys; the order only steers the search bounds, never the result.
+int sort_queries(Workspace& ws, const float4* qa, uint64_t n, uint32_t* perm, cudaStream_t st) {
     if (n == 0) return 0;
+    float qlo[3], qhi[3];
+    if (compute_bbox(ws, qa, n, qlo, qhi, st) != 0) return -1;
+    const KeyGrid g = make_key_grid(qlo, qhi, 10, 16);
     size_t mark = ws.mark();
     uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
     uint32_t* vals = perm;
