@@ -24,11 +24,13 @@
 namespace alb {
 
 constexpr int kGatherWarps = 8;   // 8-warp CTAs, 4 per SM: 32 warps hide the gather's latency
+constexpr int kGatherBlocksPerSM = 4;
 constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one warp
 constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
 constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
 constexpr int kBand = 32;         // near-tie entries resolved in float64
+constexpr int kLeafList = 2 * kBand;  // leaf list of a search under a guess (aliases the band)
 // Squared widening of the previous query's k-th distance that the scatter-map search first
 // admits within (1.1^2): consecutive sorted queries' k-th distances differ by less than 10%
 // for 97% of them; a guess that does not hold is detected and the search redone (measured
@@ -48,7 +50,10 @@ struct WarpSmem {
     uint32_t ci[kCap];
     int16_t cl[kCap];
     uint32_t hist[128];  // 256 radix bins, two 16-bit counters per word
-    double bd[kBand];    // near-tie band: float64 distances
+    union {
+        double bd[kBand];               // near-tie band: float64 distances (after the search)
+        uint32_t leafl[kLeafList];      // leaves to screen (during a search under a guess)
+    };
     uint32_t bi[kBand];  // map positions
     uint64_t bt[kBand];  // tie keys from the record's content (or 0)
     float prev_rk2;      // squared k-th distance of the warp's previous query (kept out of registers)
@@ -398,7 +403,7 @@ ALB_DEVICE double select_refined(const MapDev& m, WarpSmem& s, int off, int n, i
 // holds entries within one float32 ulp of the k-th: needed where many points sit at nearly
 // the same distance (queries far from a dense planar map). Without it candidates carry the
 // float32 screening distance and only a crowded final band is refined.
-template <bool REFINE>
+template <bool REFINE, bool QSPLIT = false>
 ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double qy, double qz, float fx,
                          float fy, float fz, float lx, float ly, float lz, float thr0, float thr_safe,
                          const float4* tie_rec, KnnResult& res) {
@@ -445,21 +450,67 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
             __syncwarp();
         }
         int guard = 0;
-        // Under a guessed threshold, the leaves of an expanded leaf parent are visited straight
-        // from its ballot (lmask, leaf index lbase + bit) instead of through the stack.
-        unsigned lmask = 0u;
-        uint32_t lbase = 0u;
-        while (sp > 0 || lmask) {
+        // Under a guessed threshold the threshold rarely shrinks, so the order of the boxes
+        // does not change which leaves are opened: the leaves of expanded leaf parents are
+        // collected in s.leafl and screened in batches, with the next leaf's records loaded
+        // while the current leaf is screened, so the leaf visits do not form one chain of
+        // dependent loads. The ordered search (a safe bound, or none) takes its leaves from
+        // the stack, nearest first.
+        const bool listed = !REFINE && start < thr_safe;
+        int nlist = 0;
+        // screen the 32 records of leaf `leaf` (p = this lane's record) against the threshold
+        auto admit = [&](uint32_t leaf, float4 p) {
+            ++res.leaves;
+            const uint64_t r = (uint64_t)leaf * 32 + l;
+            const bool real = r < m.n;  // the last leaf may be partial
+            const float d = real ? point_dist2(fx, fy, fz, lx, ly, lz, p) : FLT_MAX;
+            const bool take = real && d <= thr;
+            const unsigned b = __ballot_sync(0xffffffffu, take);
+            if (take) {
+                const int pos = cnt + __popc(b & lanemask_lt());
+                s.ci[pos] = (uint32_t)r;
+                if (REFINE) {
+                    float hi, lo;
+                    point_dist2_df(fx, fy, fz, lx, ly, lz, p, hi, lo);
+                    s.cd[pos] = hi;
+                    s.cl[pos] = frac16(hi, lo);
+                } else {
+                    s.cd[pos] = d;
+                }
+            }
+            cnt += __popc(b);
+            __syncwarp();
+            if (cnt >= k && (thr == FLT_MAX || cnt > kSelectAt)) {
+                ++res.selects;
+                const float kth = warp_kth32(s, 0, cnt, k);
+                thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
+                // REFINE: refined distances within one float32 ulp of the k-th can still
+                // rank among the k nearest, nothing beyond can; otherwise the float32
+                // screening margin decides
+                cnt = warp_compact(s, cnt, REFINE ? __uint_as_float(__float_as_uint(kth) + 1u) : thr);
+                if (cnt > kCap - 32) {  // mass ties
+                    cnt = warp_compact(s, cnt, kth);
+                    res.clipped = 1;
+                }
+                if (cnt > kCap - 32) cnt = kCap - 32;  // keeps the buffer in bounds
+            }
+        };
+        auto load_leaf = [&](uint32_t leaf) {
+            const uint64_t r = (uint64_t)leaf * 32 + l;
+            return r < m.n ? m.a[r] : make_float4(0.f, 0.f, 0.f, 0.f);
+        };
+        auto flush = [&]() {
+#pragma unroll 1
+            for (int i = 0; i < nlist; ++i) admit(s.leafl[i], load_leaf(s.leafl[i]));
+            nlist = 0;
+        };
+        while (sp > 0) {
             if (++guard > (1 << 22)) {  // reported, never a silent partial answer
                 res.fail = ALB_ERR_ITER_CAP;
                 break;
             }
             uint32_t etop;
-            if (lmask) {
-                const int b = __ffs(lmask) - 1;
-                lmask &= lmask - 1u;
-                etop = lbase + (uint32_t)b;  // a leaf: level bits 0
-            } else {
+            {
                 // the top 32 stack entries, one per lane (lane 0 = top)
                 const int i = sp - 1 - l;
                 uint32_t e = 0u;
@@ -480,43 +531,8 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 __syncwarp();
             }
             if ((etop >> 29) == 0) {
-                // a leaf: admit its points within the threshold
-                ++res.leaves;
-                const uint64_t r = (uint64_t)etop * 32 + l;
-                const bool real = r < m.n;  // the last leaf may be partial
-                float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (real) p = m.a[r];
-                const float d = real ? point_dist2(fx, fy, fz, lx, ly, lz, p) : FLT_MAX;
-                const bool take = real && d <= thr;
-                const unsigned b = __ballot_sync(0xffffffffu, take);
-                if (take) {
-                    const int pos = cnt + __popc(b & lanemask_lt());
-                    s.ci[pos] = (uint32_t)r;
-                    if (REFINE) {
-                        float hi, lo;
-                        point_dist2_df(fx, fy, fz, lx, ly, lz, p, hi, lo);
-                        s.cd[pos] = hi;
-                        s.cl[pos] = frac16(hi, lo);
-                    } else {
-                        s.cd[pos] = d;
-                    }
-                }
-                cnt += __popc(b);
-                __syncwarp();
-                if (cnt >= k && (thr == FLT_MAX || cnt > kSelectAt)) {
-                    ++res.selects;
-                    const float kth = warp_kth32(s, 0, cnt, k);
-                    thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
-                    // REFINE: refined distances within one float32 ulp of the k-th can still
-                    // rank among the k nearest, nothing beyond can; otherwise the float32
-                    // screening margin decides
-                    cnt = warp_compact(s, cnt, REFINE ? __uint_as_float(__float_as_uint(kth) + 1u) : thr);
-                    if (cnt > kCap - 32) {  // mass ties
-                        cnt = warp_compact(s, cnt, kth);
-                        res.clipped = 1;
-                    }
-                    if (cnt > kCap - 32) cnt = kCap - 32;  // keeps the buffer in bounds
-                }
+                // a leaf of the ordered search: admit its points within the threshold
+                admit(etop, load_leaf(etop));
             } else {
                 ++res.nodes;
                 const int lev = (int)(etop >> 29);
@@ -531,19 +547,21 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 uint32_t cc = (uint32_t)c;
                 const unsigned vm = __ballot_sync(0xffffffffu, d < FLT_MAX);
                 int nv = __popc(vm);
-                if (!REFINE && start < thr_safe) {
-                    // Under a guessed threshold the search rarely shrinks its threshold, so
-                    // the order of the boxes does not change which leaves are opened:
-                    // children are taken as they come, without ordering them; leaves go
-                    // straight to the visit.
+                if (listed) {
+                    // children are taken as they come, without ordering them; leaves go to
+                    // the list
+                    if (d < FLT_MAX) {
+                        const int pos = __popc(vm & lanemask_lt());
+                        if (cl == 0) {
+                            s.leafl[nlist + pos] = cc;
+                        } else {
+                            s.stk[sp + pos] = ((uint32_t)cl << 29) | cc;
+                            s.stk_d[sp + pos] = d;
+                        }
+                    }
                     if (cl == 0) {
-                        lmask = vm;
-                        lbase = (uint32_t)(node * 32u);
+                        nlist += nv;
                         nv = 0;
-                    } else if (d < FLT_MAX) {
-                        const int pos = sp + __popc(vm & lanemask_lt());
-                        s.stk[pos] = ((uint32_t)cl << 29) | cc;
-                        s.stk_d[pos] = d;
                     }
                 } else if (nv <= 16) {
                     // few children within the threshold: extract them nearest first
@@ -567,8 +585,10 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
                 }
                 sp += nv;
                 __syncwarp();
+                if (nlist > kLeafList - 32) flush();  // room for the next parent's 32 leaves
             }
         }
+        if (!res.fail) flush();
         if (res.fail || start == FLT_MAX) break;
         if (cnt < k) continue;
         if (REFINE || start >= thr_safe) break;
@@ -582,6 +602,13 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
     }
     if (!res.fail && cnt < k) res.fail = ALB_ERR_INVALID;
     if (res.fail) return true;
+    if (QSPLIT) {
+        // the float64 query is exactly its float32 split (f + l): rebuilt here rather than
+        // held in registers through the search
+        qx = (double)fx + (double)lx;
+        qy = (double)fy + (double)ly;
+        qz = (double)fz + (double)lz;
+    }
     double rk2;
     if (REFINE) {
         rk2 = select_refined(m, s, 0, cnt, k, qx, qy, qz, tie_rec, res.clipped);
@@ -887,7 +914,7 @@ ALB_DEVICE void heat_add(const SceneDev& sc, const MapDev& m, const Accum& acc, 
 constexpr int kModeKnn = 0, kModeKnnAdjoint = 1, kModeRadius = 2, kModeKnnHeat = 3;
 
 template <int CHANNEL, int MODE>
-__global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
+__global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gather(SceneDev sc, MapDev m, QueryDev q, Accum acc, int k,
                                                               int* err) {
     __shared__ WarpSmem smem[kGatherWarps];
     __shared__ BinCache bc;
@@ -908,9 +935,11 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
         bool have_prev = false;  // s.ci[0 .. k) holds the previous query's neighbours
         for (uint64_t qi = ch * kQueryChunk; qi < q_end; ++qi) {
             uint64_t src = q.perm ? q.perm[qi] : qi;
-            float4 qa = q.a[src], qb = q.b[src], qc = q.c[src];
-            double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y, qz = (double)qa.z + (double)qc.z;
+            const float4 qa = q.a[src], qc = q.c[src];
             if (MODE == kModeRadius) {
+                const float4 qb = q.b[src];
+                const double qx = (double)qa.x + (double)qc.x, qy = (double)qa.y + (double)qc.y,
+                             qz = (double)qa.z + (double)qc.z;
                 // extension: every record within the fixed radius contributes at once
                 KnnResult r;
                 const float Es = qa.w, ts = qb.w;
@@ -959,9 +988,12 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             if (have_prev) {
                 // the float32 screening error (below 2^-21) is far inside the 2^-14 inflation
                 unsigned mx = 0u;
+                float4 pn = l < k ? m.a[s.ci[l]] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1  // rolled: the kernel is bound by instruction fetch, and these loops run 4 times
                 for (int j = l; j < k; j += 32) {
-                    const float d = point_dist2(qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, m.a[s.ci[j]]);
+                    const float4 p = pn;
+                    if (j + 32 < k) pn = m.a[s.ci[j + 32]];  // in flight during this neighbour
+                    const float d = point_dist2(qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, p);
                     mx = max(mx, __float_as_uint(d));  // non-negative floats order like their bits
                 }
                 const float t = __uint_as_float(__reduce_max_sync(0xffffffffu, mx)) * (1.f + 1.f / 16384.f);
@@ -975,8 +1007,8 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 thr0 = (CHANNEL == ALB_SCATTER) ? fminf(thr_safe, s.prev_rk2 * kGuessWiden2) : thr_safe;
             }
             KnnResult r;
-            if (!warp_knn<CHANNEL != ALB_SCATTER>(m, s, k, qx, qy, qz, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z, thr0,
-                                                   thr_safe, m.b, r)) {
+            if (!warp_knn<CHANNEL != ALB_SCATTER, true>(m, s, k, 0.0, 0.0, 0.0, qa.x, qa.y, qa.z, qc.x, qc.y, qc.z,
+                                                         thr0, thr_safe, m.b, r)) {
                 if (l == 0) atomicCAS(err, 0, ALB_ERR_TOO_FEW);
                 failed = true;
                 break;
@@ -986,6 +1018,9 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
                 failed = true;
                 break;
             }
+            // the query's direction and time, and its float64 depth, are needed from here on
+            const float4 qb = q.b[src];
+            const double qy = (double)qa.y + (double)qc.y;
             have_prev = true;
             if (l == 0) s.prev_rk2 = (float)r.rk2;  // read after the next query's __syncwarp
             if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
@@ -1010,15 +1045,29 @@ __global__ void __launch_bounds__(kGatherWarps * 32, 4) k_gather(SceneDev sc, Ma
             const int layer = (CHANNEL == ALB_SCATTER) ? layer_of(sc, qy) : 0;
             float4 sq = make_float4(0.f, 0.f, 0.f, 0.f);
             if (MODE == kModeKnnAdjoint && q.s) sq = q.s[src];
+            // the next neighbour's record is loaded while this one is weighted
+            uint32_t idx_n = l < k ? s.ci[l] : 0u;
+            float4 pb_n = make_float4(0.f, 0.f, 0.f, 0.f);
+            float e_n = 0.f;
+            if (l < k) {
+                pb_n = m.b[idx_n];
+                e_n = m.a[idx_n].w;
+            }
 #pragma unroll 1
             for (int j = l; j < k; j += 32) {
-                const uint32_t idx = s.ci[j];
-                const float4 pb = m.b[idx];
+                const uint32_t idx = idx_n;
+                const float4 pb = pb_n;
+                const float Ep = e_n;
+                if (j + 32 < k) {
+                    idx_n = s.ci[j + 32];
+                    pb_n = m.b[idx_n];
+                    e_n = m.a[idx_n].w;
+                }
                 float w;
                 if (CHANNEL == ALB_BOTTOM_REFLECTION || CHANNEL == ALB_SURFACE_TRANSMISSION_UP) w = wconst;
                 else if (CHANNEL == ALB_SCATTER) w = scatter_weight(sc, layer, pb.x, pb.y, pb.z, vx, vy, vz);
                 else w = ggx_weight(sc.ggx_a2, (float)sc.f0, -pb.x, -pb.y, -pb.z, vx, vy, vz);
-                const float c = ((Es * m.a[idx].w) * norm) * w;
+                const float c = ((Es * Ep) * norm) * w;
                 const int bin = (int)((ts + pb.w) / (float)sc.mult) - (int)sc.gate_lo;
                 if (bin >= 0 && bin < acc.nbins) {
                     bin_add(bc, acc, CHANNEL, bin, f32_to_fix(c));
