@@ -1303,7 +1303,7 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const double budget = 0.8 * (double)free_b;
-    const double bytes_per_record = opt->adjoint ? 160.0 : 128.0;
+    const double bytes_per_record = opt->adjoint ? 162.0 : 130.0;
     std::mutex mem_mu;
     std::condition_variable mem_cv;
     double held_total = 0.0, rpp_seen = 0.0;

@@ -57,6 +57,7 @@ struct WarpSmem {
     uint32_t bi[kBand];  // map positions
     uint64_t bt[kBand];  // tie keys from the record's content (or 0)
     float prev_rk2;      // squared k-th distance of the warp's previous query (kept out of registers)
+    unsigned long long st[5];  // the warp's search counters: leaves, nodes, selects, queries, inexact
 };
 
 // Lower bound of the squared distance from the float64 query (qx + lx, ...) to a box:
@@ -929,7 +930,10 @@ __global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gathe
     const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
     const uint64_t chunks = (q.n + kQueryChunk - 1) / kQueryChunk;
     bool failed = false;
-    unsigned long long st_leaves = 0, st_nodes = 0, st_selects = 0, st_queries = 0, st_inexact = 0;
+    // search counters accumulate in the warp's shared memory, not in registers held through
+    // every search
+    if (l < 5) s.st[l] = 0ull;
+    __syncwarp();
     for (uint64_t ch = (uint64_t)blockIdx.x * kGatherWarps + w; ch < chunks && !failed; ch += warps) {
         const uint64_t q_end = min((ch + 1) * kQueryChunk, q.n);
         bool have_prev = false;  // s.ci[0 .. k) holds the previous query's neighbours
@@ -976,10 +980,12 @@ __global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gathe
                     failed = true;
                     break;
                 }
-                st_leaves += r.leaves;
-                st_nodes += r.nodes;
-                st_inexact += r.clipped;
-                ++st_queries;
+                if (l == 0) {
+                    s.st[0] += r.leaves;
+                    s.st[1] += r.nodes;
+                    s.st[3] += 1;
+                    s.st[4] += r.clipped;
+                }
                 if (q.rk_out && l == 0) q.rk_out[src] = sc.radius;
                 __syncwarp();
                 continue;
@@ -1024,12 +1030,14 @@ __global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gathe
             have_prev = true;
             if (l == 0) s.prev_rk2 = (float)r.rk2;  // read after the next query's __syncwarp
             if (q.rk_out && l == 0) q.rk_out[src] = sqrt(r.rk2);
-            st_leaves += r.leaves;
-            st_nodes += r.nodes;
-            st_selects += r.selects;
-            st_inexact += r.clipped;
+            if (l == 0) {
+                s.st[0] += r.leaves;
+                s.st[1] += r.nodes;
+                s.st[2] += r.selects;
+                s.st[3] += 1;
+                s.st[4] += r.clipped;
+            }
             if (r.retried && l == 0 && q.retries) atomicAdd(q.retries, 1ull);  // rare: no register kept
-            ++st_queries;
             const float Es = qa.w, ts = qb.w;
             const float rk = r.rkf;
             float norm;
@@ -1095,13 +1103,13 @@ __global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gathe
         }
     }
     if (l == 0) {
-        if (q.stats && st_queries) {
-            atomicAdd(q.stats + 0, st_leaves);
-            atomicAdd(q.stats + 1, st_nodes);
-            atomicAdd(q.stats + 2, st_selects);
-            atomicAdd(q.stats + 3, st_queries);
+        if (q.stats && s.st[3]) {
+            atomicAdd(q.stats + 0, s.st[0]);
+            atomicAdd(q.stats + 1, s.st[1]);
+            atomicAdd(q.stats + 2, s.st[2]);
+            atomicAdd(q.stats + 3, s.st[3]);
         }
-        if (q.inexact && st_inexact) atomicAdd(q.inexact, st_inexact);
+        if (q.inexact && s.st[4]) atomicAdd(q.inexact, s.st[4]);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kBinCache; i += blockDim.x) {

@@ -622,12 +622,15 @@ ALB_DEVICE int slot_of(unsigned* tag, unsigned key) {
     return t == key ? sl : -1;
 }
 
-// PASS 1: per node, 256-bin histogram of the top byte of the 16-bit coordinate.
-// PASS 2: per node, histogram of the low byte inside the bucket holding the cut.
+// PASS 1: per node, 256-bin histogram of the top byte of the 16-bit coordinate; the
+//         coordinates go to Q (level 0 only: later levels get Q from the split).
+// PASS 2: per node, histogram of the low byte inside the bucket holding the cut, from Q
+//         (2 bytes per record instead of the 16 of X).
 template <int PASS>
-__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restrict__ X, uint64_t n, uint64_t L,
-                                                          int d, LevelNodes nb, const uint2* __restrict__ sel,
-                                                          unsigned* hist, uint64_t per) {
+__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restrict__ X, uint16_t* Q, uint64_t n,
+                                                          uint64_t L, int d, LevelNodes nb,
+                                                          const uint2* __restrict__ sel, unsigned* hist,
+                                                          uint64_t per) {
     __shared__ unsigned tag[kSlots];
     __shared__ unsigned sh[kSlots * 256];
     for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) sh[j] = 0u;
@@ -636,16 +639,22 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     // kHistItems records per thread and iteration, all loads issued before any is used:
     // the pass streams the records once, so loads in flight set its speed
-    const uint64_t stride = (uint64_t)blockDim.x * kHistItems;
+    // the second pass reads 2 bytes per record: more records in flight per thread
+    constexpr int kItems = PASS == 1 ? kHistItems : 4 * kHistItems;
+    const uint64_t stride = (uint64_t)blockDim.x * kItems;
     for (uint64_t base0 = r0 + (threadIdx.x & ~31u); base0 < r1; base0 += stride) {
-        float4 pv[kHistItems];
+        float4 pv[PASS == 1 ? kItems : 1];
+        uint32_t qv[PASS == 1 ? 1 : kItems];
 #pragma unroll
-        for (int t = 0; t < kHistItems; ++t) {
+        for (int t = 0; t < kItems; ++t) {
             const uint64_t i = base0 + (uint64_t)t * blockDim.x + lane_id();
-            if (i < r1) pv[t] = X[i];
+            if (i < r1) {
+                if (PASS == 1) pv[t] = X[i];
+                else qv[t] = Q[i];
+            }
         }
 #pragma unroll
-        for (int t = 0; t < kHistItems; ++t) {
+        for (int t = 0; t < kItems; ++t) {
             const uint64_t base = base0 + (uint64_t)t * blockDim.x;
             const uint64_t i = base + lane_id();
             bool act = false;
@@ -655,7 +664,13 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
                 int r;
                 kd_node_path(i / 32, L, d, a, c, path, r);
                 if (r == d && c > 1) {
-                    const uint32_t q = kd_quant16(pv[t], nb, path);
+                    uint32_t q;
+                    if (PASS == 1) {
+                        q = kd_quant16(pv[t], nb, path);
+                        Q[i] = (uint16_t)q;
+                    } else {
+                        q = qv[t];
+                    }
                     if (PASS == 1) {
                         act = true;
                         h = q >> 8;
@@ -791,9 +806,10 @@ __global__ void k_kdl_select2(const unsigned* __restrict__ hist2, uint32_t nodes
 // boxes (for the next level's axis choice) are reduced in shared memory over the block's
 // whole range and flushed once.
 constexpr int kSplitItems = 4;
+constexpr uint32_t kNoQ = 0xffffffffu;
 
 __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
-                                                           uint64_t n, uint64_t L, int d, LevelNodes nb,
+                                                           uint16_t* Q, uint64_t n, uint64_t L, int d, LevelNodes nb,
                                                            const uint2* __restrict__ cut, unsigned* cursors,
                                                            unsigned* ties, unsigned* err, uint64_t per,
                                                            LevelNodes nbn, unsigned* hist_next) {
@@ -819,6 +835,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
         uint64_t dst0[kSplitItems];  // start of the record's child range
         uint64_t dend[kSplitItems];  // end of that range (bounds check)
         uint32_t path[kSplitItems], rank[kSplitItems];
+        uint32_t qn[kSplitItems];    // the child's 16-bit coordinate, or kNoQ when not split again
         int code[kSplitItems];       // slot * 2 + side while the tile reservation is pending, else -1
 #pragma unroll
         for (int t = 0; t < kSplitItems; ++t) {  // every load in flight before the first use
@@ -833,6 +850,7 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             dend[t] = 0;
             path[t] = 0;
             rank[t] = 0;
+            qn[t] = kNoQ;
             bool moves = false, counts_next = false;
             unsigned side = 0, hbin = 0;
             uint64_t a = 0, c = 0, left = 0;
@@ -852,7 +870,8 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                     // the child node is split again at the next level if it has > 1 leaf
                     if (hist_next && (side ? c - left : left) > 1) {
                         counts_next = true;
-                        hbin = kd_quant16(p[t], nbn, (path[t] << 1) | side) >> 8;
+                        qn[t] = kd_quant16(p[t], nbn, (path[t] << 1) | side);
+                        hbin = qn[t] >> 8;
                     }
                 } else {
                     X2[i] = p[t];  // already in place (a leaf of an earlier level)
@@ -887,8 +906,12 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
                 rank[t] = b + lrank;
                 if (cd < 0) {  // global cursor: final position known now
                     const uint64_t dst = dst0[t] + rank[t];
-                    if (dst < dend[t]) X2[dst] = p[t];
-                    else atomicOr(err, 1u);
+                    if (dst < dend[t]) {
+                        X2[dst] = p[t];
+                        if (qn[t] != kNoQ) Q[dst] = (uint16_t)qn[t];
+                    } else {
+                        atomicOr(err, 1u);
+                    }
                 }
             }
             if (counts_next) {
@@ -909,8 +932,12 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
         for (int t = 0; t < kSplitItems; ++t) {
             if (code[t] >= 0) {
                 const uint64_t dst = dst0[t] + nbase[code[t]] + rank[t];
-                if (dst < dend[t]) X2[dst] = p[t];
-                else atomicOr(err, 1u);
+                if (dst < dend[t]) {
+                    X2[dst] = p[t];
+                    if (qn[t] != kNoQ) Q[dst] = (uint16_t)qn[t];
+                } else {
+                    atomicOr(err, 1u);
+                }
             }
         }
         __syncthreads();
@@ -1349,8 +1376,12 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         float4* par = (float4*)ws.take_bytes(maxnodes * 16);
         float4* cpar = (float4*)ws.take_bytes(maxnodes * 16);  // children's parameters
         unsigned* hist1n = ws.take_u32(maxnodes * 256);       // children's first histogram
+        // each record's 16-bit coordinate on its node's axis, in position order: written by
+        // the level-0 histogram and by every split for the next level, read by the second
+        // histogram instead of the whole record
+        uint16_t* Q = (uint16_t*)ws.take_bytes(n * 2);
         if (!hist1 || !hist2 || !sel || !cut || !cursors || !ties || !lo || !hi || !clo || !chi || !par || !cpar ||
-            !hist1n) {
+            !hist1n || !Q) {
             ws.release(mark);
             return -1;
         }
@@ -1379,7 +1410,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         k_kdl_params<<<1, 256, 0, st>>>(lo, hi, 1u, par);
         note_launch();
         cudaMemsetAsync(hist1, 0, 256 * 4, st);
-        k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, n, L, 0, LevelNodes{par}, nullptr, hist1, per);
+        k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, Q, n, L, 0, LevelNodes{par}, nullptr, hist1, per);
         note_launch();
         for (int d = 0; d < D; ++d) {
             const uint32_t nodes = 1u << d;
@@ -1390,7 +1421,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
             LevelNodes nb{par};
             k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
             note_launch();
-            k_kdl_hist<2><<<lb, kLvlThreads, 0, st>>>(X, n, L, d, nb, sel, hist2, per);
+            k_kdl_hist<2><<<lb, kLvlThreads, 0, st>>>(X, Q, n, L, d, nb, sel, hist2, per);
             note_launch();
             k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
             note_launch();
@@ -1401,7 +1432,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
                 note_launch();
                 cudaMemsetAsync(hist1n, 0, (size_t)nodes * 2 * 256 * 4, st);
             }
-            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, n, L, d, nb, cut, cursors, ties, err, per,
+            k_kdl_split<<<lb, kLvlThreads, 0, st>>>(X, X2, Q, n, L, d, nb, cut, cursors, ties, err, per,
                                                      LevelNodes{cpar}, more ? hist1n : nullptr);
             note_launch();
             std::swap(X, X2);
