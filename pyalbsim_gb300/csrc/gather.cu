@@ -249,6 +249,55 @@ ALB_DEVICE float warp_kth32(WarpSmem& s, int off, int cnt, int k) {
     return __uint_as_float(prefix);
 }
 
+// k-th smallest (1-based) float32 part cd[0 .. cnt), for candidates that mostly lie in
+// [0, hi]: one pass of 256 linear bins over [0, hi] (bin = d * 256 / hi, truncated and
+// clamped, which is monotone in d, so the bins keep the order), then an exact rank among the
+// entries of the bin that holds the k-th (usually one to three). Falls back to the four-pass
+// radix select when hi gives no spread or that bin holds more than 32 entries.
+ALB_DEVICE float warp_kth32_lin(WarpSmem& s, int cnt, int k, float hi) {
+    const float scale = 256.f / hi;
+    if (!(hi > 0.f) || !(scale < 1.0e30f)) return warp_kth32(s, 0, cnt, k);
+    const int l = lane_id();
+#pragma unroll 1
+    for (int i = l; i < 128; i += 32) s.hist[i] = 0u;
+    __syncwarp();
+#pragma unroll 1
+    for (int i = l; i < cnt; i += 32) {
+        const uint32_t d = (uint32_t)min((int)(s.cd[i] * scale), 255);
+        atomicAdd(&s.hist[d >> 1], 1u << ((d & 1u) * 16u));
+    }
+    __syncwarp();
+    int need = k;
+    const uint32_t B = radix_pick(s, need);  // need: rank inside bin B (1-based)
+    __syncwarp();
+    int m = 0;
+#pragma unroll 1
+    for (int base = 0; base < cnt; base += 32) {
+        const int i = base + l;
+        const float d = i < cnt ? s.cd[i] : 0.f;
+        const bool in = i < cnt && (uint32_t)min((int)(d * scale), 255) == B;
+        const unsigned b = __ballot_sync(0xffffffffu, in);
+        if (in) {
+            const int pos = m + __popc(b & lanemask_lt());
+            if (pos < 32) s.hist[pos] = __float_as_uint(d);
+        }
+        m += __popc(b);
+    }
+    __syncwarp();
+    if (m > 32) return warp_kth32(s, 0, cnt, k);
+    const float v = l < m ? __uint_as_float(s.hist[l]) : FLT_MAX;
+    int rank = 0;
+#pragma unroll 1
+    for (int j = 0; j < m; ++j) {
+        const float o = __shfl_sync(0xffffffffu, v, j);
+        rank += (o < v || (o == v && j < l)) ? 1 : 0;
+    }
+    const unsigned own = __ballot_sync(0xffffffffu, l < m && rank == need - 1);
+    const float kth = __shfl_sync(0xffffffffu, v, __ffs(own) - 1);
+    __syncwarp();
+    return kth;
+}
+
 // k-th smallest (1-based) 48-bit candidate key by warp radix select over its top
 // 8 * PASSES bits (PASSES = 4: the float32 part only; the lower bits return as 0).
 template <int PASSES>
@@ -483,7 +532,8 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
             __syncwarp();
             if (cnt >= k && (thr == FLT_MAX || cnt > kSelectAt)) {
                 ++res.selects;
-                const float kth = warp_kth32(s, 0, cnt, k);
+                // planar maps (REFINE) crowd their candidates into one linear bin: radix select
+                const float kth = REFINE ? warp_kth32(s, 0, cnt, k) : warp_kth32_lin(s, cnt, k, thr);
                 thr = fminf(thr, kth * (1.0f + 2.0f * kRelMargin));
                 // REFINE: refined distances within one float32 ulp of the k-th can still
                 // rank among the k nearest, nothing beyond can; otherwise the float32
@@ -595,7 +645,7 @@ ALB_DEVICE bool warp_knn(const MapDev& m, WarpSmem& s, int k, double qx, double 
         if (REFINE || start >= thr_safe) break;
         // a guess: accepted when the k-th with its band margin lies within it
         ++res.selects;
-        const float kth = warp_kth32(s, 0, cnt, k);
+        const float kth = warp_kth32_lin(s, cnt, k, start);
         if (kth * (1.0f + 2.0f * kRelMargin) <= start) {
             kth_known = kth;
             break;
