@@ -496,18 +496,19 @@ __global__ void k_permute_u32_pad(const uint32_t* __restrict__ src, const uint32
 
 // ------------------------------------------------------------------------------------------
 // Exact left-balanced k-d order by streaming partitions (the photon-map build).
-// Global levels 0..D-1 (nodes larger than one CTA's cell) each take three passes over
-// X = float4(x, y, z, record id) in position order:
+// Global levels 0..D-1 (nodes larger than one CTA's cell) each take these passes over
+// X = float4(x, y, z, record id) in position order (and Q, each record's 16-bit coordinate):
 //   hist1: per node, 256-bin histogram of the top byte of a 16-bit coordinate quantised
-//          on the node's widest axis;
+//          on the node's widest axis (level 0 from X; every later level gets it from the
+//          split above, which also writes the coordinates to Q);
 //   hist2: per node, 256-bin histogram of the low byte inside the bucket that holds the
-//          cut (the node's left child takes exactly its power-of-two leaf count);
+//          cut (the node's left child takes exactly its power-of-two leaf count), from Q;
 //   split: every record goes left or right of that cut (ties at the 16-bit cut resolved
-//          by an atomic ticket), with warp-aggregated cursors, into X2; the children's
-//          boxes are reduced on the way for the next level's axis choice.
+//          by an atomic ticket), with warp-aggregated cursors, into X2, its coordinate on
+//          its child's axis into Q, and the children's first histogram on the way.
 // The remaining levels (nodes of <= kCellMax records) run in one CTA per node in shared
-// memory (k_local_kd). The result is the same tree shape as kd_order, with the cut placed
-// at 16-bit resolution.
+// memory (k_local_kd_full for perfect cells, k_local_kd for the rest). The cut is placed at
+// 16-bit resolution.
 // ------------------------------------------------------------------------------------------
 
 // (start leaf a, leaf count c, path bits) of the depth-d node holding `leaf`
@@ -622,15 +623,11 @@ ALB_DEVICE int slot_of(unsigned* tag, unsigned key) {
     return t == key ? sl : -1;
 }
 
-// PASS 1: per node, 256-bin histogram of the top byte of the 16-bit coordinate; the
-//         coordinates go to Q (level 0 only: later levels get Q from the split).
-// PASS 2: per node, histogram of the low byte inside the bucket holding the cut, from Q
-//         (2 bytes per record instead of the 16 of X).
-template <int PASS>
-__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restrict__ X, uint16_t* Q, uint64_t n,
-                                                          uint64_t L, int d, LevelNodes nb,
-                                                          const uint2* __restrict__ sel, unsigned* hist,
-                                                          uint64_t per) {
+// Level 0's first pass: per node, 256-bin histogram of the top byte of the 16-bit
+// coordinate, which goes to Q (later levels get both from the split of the level above).
+__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist1(const float4* __restrict__ X, uint16_t* Q, uint64_t n,
+                                                           uint64_t L, int d, LevelNodes nb, unsigned* hist,
+                                                           uint64_t per) {
     __shared__ unsigned tag[kSlots];
     __shared__ unsigned sh[kSlots * 256];
     for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) sh[j] = 0u;
@@ -639,22 +636,16 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     // kHistItems records per thread and iteration, all loads issued before any is used:
     // the pass streams the records once, so loads in flight set its speed
-    // the second pass reads 2 bytes per record: more records in flight per thread
-    constexpr int kItems = PASS == 1 ? kHistItems : 4 * kHistItems;
-    const uint64_t stride = (uint64_t)blockDim.x * kItems;
+    const uint64_t stride = (uint64_t)blockDim.x * kHistItems;
     for (uint64_t base0 = r0 + (threadIdx.x & ~31u); base0 < r1; base0 += stride) {
-        float4 pv[PASS == 1 ? kItems : 1];
-        uint32_t qv[PASS == 1 ? 1 : kItems];
+        float4 pv[kHistItems];
 #pragma unroll
-        for (int t = 0; t < kItems; ++t) {
+        for (int t = 0; t < kHistItems; ++t) {
             const uint64_t i = base0 + (uint64_t)t * blockDim.x + lane_id();
-            if (i < r1) {
-                if (PASS == 1) pv[t] = X[i];
-                else qv[t] = Q[i];
-            }
+            if (i < r1) pv[t] = X[i];
         }
 #pragma unroll
-        for (int t = 0; t < kItems; ++t) {
+        for (int t = 0; t < kHistItems; ++t) {
             const uint64_t base = base0 + (uint64_t)t * blockDim.x;
             const uint64_t i = base + lane_id();
             bool act = false;
@@ -664,20 +655,10 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
                 int r;
                 kd_node_path(i / 32, L, d, a, c, path, r);
                 if (r == d && c > 1) {
-                    uint32_t q;
-                    if (PASS == 1) {
-                        q = kd_quant16(pv[t], nb, path);
-                        Q[i] = (uint16_t)q;
-                    } else {
-                        q = qv[t];
-                    }
-                    if (PASS == 1) {
-                        act = true;
-                        h = q >> 8;
-                    } else if ((q >> 8) == sel[path].x) {
-                        act = true;
-                        h = q & 255u;
-                    }
+                    const uint32_t q = kd_quant16(pv[t], nb, path);
+                    Q[i] = (uint16_t)q;
+                    act = true;
+                    h = q >> 8;
                 }
             }
             const unsigned am = __ballot_sync(0xffffffffu, act);
@@ -703,6 +684,51 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_hist(const float4* __restri
                         else atomicAdd(hist + (uint64_t)path * 256 + h, (unsigned)__popc(peers));
                     }
                 }
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) {
+        const unsigned t = tag[j >> 8];
+        if (t != kNoTag && sh[j]) atomicAdd(hist + (uint64_t)t * 256 + (j & 255), sh[j]);
+    }
+}
+
+// PASS 2 from the coordinate stream: per node, 256-bin histogram of the low byte of the
+// 16-bit coordinates inside the bucket that holds the cut. Each thread takes 8 consecutive
+// records (one 16-byte load of Q), which lie in one 32-record leaf and so in one node: one
+// node lookup and one slot claim per 8 records.
+__global__ void __launch_bounds__(kLvlThreads) k_kdl_hist2q(const uint16_t* __restrict__ Q, uint64_t n, uint64_t L,
+                                                            int d, const uint2* __restrict__ sel, unsigned* hist,
+                                                            uint64_t per) {
+    __shared__ unsigned tag[kSlots];
+    __shared__ unsigned sh[kSlots * 256];
+    for (int j = threadIdx.x; j < kSlots * 256; j += blockDim.x) sh[j] = 0u;
+    if (threadIdx.x < kSlots) tag[threadIdx.x] = kNoTag;
+    __syncthreads();
+    const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);  // per is a multiple of 1024
+    for (uint64_t i0 = r0 + (uint64_t)threadIdx.x * 8; i0 < r1; i0 += (uint64_t)blockDim.x * 8) {
+        uint32_t q[8];
+        if (i0 + 8 <= r1) {
+            const uint4 v = *reinterpret_cast<const uint4*>(Q + i0);  // i0 % 8 == 0: 16-byte aligned
+            q[0] = v.x & 0xffffu; q[1] = v.x >> 16; q[2] = v.y & 0xffffu; q[3] = v.y >> 16;
+            q[4] = v.z & 0xffffu; q[5] = v.z >> 16; q[6] = v.w & 0xffffu; q[7] = v.w >> 16;
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) q[e] = i0 + e < r1 ? (uint32_t)Q[i0 + e] : 0u;
+        }
+        uint64_t a, c;
+        uint32_t path;
+        int r;
+        kd_node_path(i0 / 32, L, d, a, c, path, r);
+        if (r != d || c <= 1) continue;  // no split of this node at this level
+        const unsigned bucket = sel[path].x;
+        const int sl = slot_of(tag, path);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            if (i0 + e < r1 && (q[e] >> 8) == bucket) {
+                if (sl >= 0) atomicAdd(&sh[sl * 256 + (q[e] & 255u)], 1u);
+                else atomicAdd(hist + (uint64_t)path * 256 + (q[e] & 255u), 1u);
             }
         }
     }
@@ -1015,21 +1041,23 @@ __global__ void __launch_bounds__(kCellThreads) k_local_kd(float4* X, const unsi
         X[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
 }
 
-// Full cells (128 leaves = 4096 records, the bulk of every large map): the same k-d order as
-// k_local_kd, with the sort keys (16-bit coordinate : 13-bit slot) held in registers, 8
-// consecutive per thread. Bitonic strides below 8 swap inside a thread, strides 8..128 use
-// warp shuffles, and only strides of 256 or more go through shared memory; node boxes come
+// Full cells (perfect subtrees of 32, 64 or 128 whole leaves: 1024, 2048 or 4096 records,
+// the bulk of every large map; which size a map's cells take depends on its leaf count): the
+// same k-d order as k_local_kd, with the sort keys (16-bit coordinate : 13-bit slot) held in
+// registers, 8 consecutive per thread. Levels of nodes of at least kPartitionMin records are
+// split by a radix partition; below it a bitonic sort runs with strides under 8 inside a
+// thread, 8..128 in warp shuffles and 256 or more through shared memory; node boxes come
 // from segmented warp reductions.
-constexpr int kFullCell = 4096;
-constexpr int kFullThreads = 512;
+constexpr int kFullCell = 4096;  // the largest full cell (kCellMax)
 // levels whose nodes hold at least this many records are split by a radix partition, the
 // smaller ones by a bitonic sort inside a warp
 constexpr unsigned kPartitionMin = 512;
 
+template <int CELL>
 struct FullCellSmem {
-    float X[kFullCell], Y[kFullCell], Z[kFullCell];
-    uint32_t ID[kFullCell];
-    uint32_t sk[kFullCell];
+    float X[CELL], Y[CELL], Z[CELL];
+    uint32_t ID[CELL];
+    uint32_t sk[CELL];
     unsigned blo[3 * 64], bhi[3 * 64];
 };
 
@@ -1106,21 +1134,24 @@ ALB_DEVICE unsigned node_exclusive_scan(unsigned v, uint32_t* wsum, unsigned tpn
     return before + inc - v;
 }
 
-__global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, const unsigned* __restrict__ cstart) {
+template <int CELL>
+__global__ void __launch_bounds__(CELL / 8, 8192 / CELL) k_local_kd_full(float4* Xg, const unsigned* __restrict__ cstart) {
+    constexpr int kFullThreads = CELL / 8;
+    constexpr int kLevels = CELL == 4096 ? 7 : (CELL == 2048 ? 6 : 5);  // log2(CELL / 32)
     extern __shared__ unsigned char smraw[];
-    FullCellSmem& s = *reinterpret_cast<FullCellSmem*>(smraw);
+    FullCellSmem<CELL>& s = *reinterpret_cast<FullCellSmem<CELL>*>(smraw);
     const uint64_t s0 = cstart[blockIdx.x];
     const int t = threadIdx.x;
     const int lane = t & 31;
-    for (int j = t; j < kFullCell; j += kFullThreads) {
+    for (int j = t; j < CELL; j += kFullThreads) {
         const float4 p = Xg[s0 + j];
         s.X[j] = p.x;
         s.Y[j] = p.y;
         s.Z[j] = p.z;
         s.ID[j] = __float_as_uint(p.w);
     }
-    for (int d = 0; d < 7; ++d) {
-        const unsigned S = (unsigned)kFullCell >> d;  // records per node at this level
+    for (int d = 0; d < kLevels; ++d) {
+        const unsigned S = (unsigned)CELL >> d;  // records per node at this level
         for (int i = t; i < 3 * 64; i += kFullThreads) {
             s.blo[i] = 0xffffffffu;
             s.bhi[i] = 0u;
@@ -1177,9 +1208,9 @@ __global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, c
             // position order; the second half the others. Two 256-bin histogram passes find
             // the cut coordinate; records AT the cut go left in position order until the left
             // half is full.
-            const unsigned nodes = (unsigned)kFullCell / S, tpn = S / 8, nstart = node * S;
-            uint32_t* h1 = s.sk;          // nodes x 256
-            uint32_t* h2 = s.sk + 2048;   // nodes x 256
+            const unsigned nodes = (unsigned)CELL / S, tpn = S / 8, nstart = node * S;
+            uint32_t* h1 = s.sk;              // nodes x 256 (nodes <= CELL / 512)
+            uint32_t* h2 = s.sk + CELL / 2;   // nodes x 256
             uint32_t* sel = s.blo;        // per node: cut, records at the cut that go left
             uint32_t* wsum = s.bhi;       // scan scratch (the boxes are consumed)
             for (int i = t; i < (int)(nodes * 256); i += kFullThreads) {
@@ -1308,7 +1339,7 @@ __global__ void __launch_bounds__(kFullThreads, 2) k_local_kd_full(float4* Xg, c
         }
         __syncthreads();
     }
-    for (int j = t; j < kFullCell; j += kFullThreads)
+    for (int j = t; j < CELL; j += kFullThreads)
         Xg[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
 }
 
@@ -1319,14 +1350,15 @@ __global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) 
     }
 }
 
-// nodes of depth D (or leaves above it): full 128-leaf cells go to `full`, the rest to
-// (st, ct)
-static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n, std::vector<unsigned>& full,
+// nodes of depth D (or leaves above it): perfect cells of 128, 64 or 32 whole leaves go to
+// full[0], full[1] or full[2], the rest to (st, ct)
+static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n, std::vector<unsigned> (&full)[3],
                             std::vector<unsigned>& st, std::vector<unsigned>& ct) {
     if (depth == D || c <= 1) {
         uint64_t s = a * 32, e = std::min<uint64_t>((a + c) * 32, n);
-        if (e - s == (uint64_t)kFullCell && c * 32 == (uint64_t)kFullCell) {
-            full.push_back((unsigned)s);
+        const int fi = c == 128 ? 0 : (c == 64 ? 1 : (c == 32 ? 2 : -1));
+        if (fi >= 0 && e - s == c * 32) {
+            full[fi].push_back((unsigned)s);
         } else if (e > s) {
             st.push_back((unsigned)s);
             ct.push_back((unsigned)(e - s));
@@ -1410,7 +1442,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         k_kdl_params<<<1, 256, 0, st>>>(lo, hi, 1u, par);
         note_launch();
         cudaMemsetAsync(hist1, 0, 256 * 4, st);
-        k_kdl_hist<1><<<lb, kLvlThreads, 0, st>>>(X, Q, n, L, 0, LevelNodes{par}, nullptr, hist1, per);
+        k_kdl_hist1<<<lb, kLvlThreads, 0, st>>>(X, Q, n, L, 0, LevelNodes{par}, hist1, per);
         note_launch();
         for (int d = 0; d < D; ++d) {
             const uint32_t nodes = 1u << d;
@@ -1421,7 +1453,7 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
             LevelNodes nb{par};
             k_kdl_select1<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist1, L, d, nodes, sel);
             note_launch();
-            k_kdl_hist<2><<<lb, kLvlThreads, 0, st>>>(X, Q, n, L, d, nb, sel, hist2, per);
+            k_kdl_hist2q<<<lb, kLvlThreads, 0, st>>>(Q, n, L, d, sel, hist2, per);
             note_launch();
             k_kdl_select2<<<(nodes * 32 + 255) / 256, 256, 0, st>>>(hist2, nodes, sel, cut);
             note_launch();
@@ -1443,16 +1475,18 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
         }
     }
     // local levels: one CTA per remaining node
-    std::vector<unsigned> fs, cs, cc;
+    std::vector<unsigned> fs[3], cs, cc;
     enumerate_cells(0, L, 0, D, n, fs, cs, cc);
-    unsigned* dfs = ws.take_u32(fs.size() + 1);
+    unsigned* dfs[3];
+    for (int f = 0; f < 3; ++f) dfs[f] = ws.take_u32(fs[f].size() + 1);
     unsigned* dcs = ws.take_u32(cs.size() + 1);
     unsigned* dcc = ws.take_u32(cc.size() + 1);
-    if (!dfs || !dcs || !dcc) {
+    if (!dfs[0] || !dfs[1] || !dfs[2] || !dcs || !dcc) {
         ws.release(mark);
         return -1;
     }
-    if (!fs.empty()) cudaMemcpyAsync(dfs, fs.data(), fs.size() * 4, cudaMemcpyHostToDevice, st);
+    for (int f = 0; f < 3; ++f)
+        if (!fs[f].empty()) cudaMemcpyAsync(dfs[f], fs[f].data(), fs[f].size() * 4, cudaMemcpyHostToDevice, st);
     if (!cs.empty()) {
         cudaMemcpyAsync(dcs, cs.data(), cs.size() * 4, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(dcc, cc.data(), cc.size() * 4, cudaMemcpyHostToDevice, st);
@@ -1462,11 +1496,24 @@ static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float
     cudaGetDevice(&dev);
     if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
         cudaFuncSetAttribute(k_local_kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem_bytes());
-        cudaFuncSetAttribute(k_local_kd_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FullCellSmem));
+        cudaFuncSetAttribute(k_local_kd_full<4096>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(FullCellSmem<4096>));
+        cudaFuncSetAttribute(k_local_kd_full<2048>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(FullCellSmem<2048>));
+        cudaFuncSetAttribute(k_local_kd_full<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(FullCellSmem<1024>));
         attr_set[dev].store(true, std::memory_order_release);
     }
-    if (!fs.empty()) {
-        k_local_kd_full<<<(unsigned)fs.size(), kFullThreads, sizeof(FullCellSmem), st>>>(X, dfs);
+    if (!fs[0].empty()) {
+        k_local_kd_full<4096><<<(unsigned)fs[0].size(), 512, sizeof(FullCellSmem<4096>), st>>>(X, dfs[0]);
+        note_launch();
+    }
+    if (!fs[1].empty()) {
+        k_local_kd_full<2048><<<(unsigned)fs[1].size(), 256, sizeof(FullCellSmem<2048>), st>>>(X, dfs[1]);
+        note_launch();
+    }
+    if (!fs[2].empty()) {
+        k_local_kd_full<1024><<<(unsigned)fs[2].size(), 128, sizeof(FullCellSmem<1024>), st>>>(X, dfs[2]);
         note_launch();
     }
     if (!cs.empty()) {
