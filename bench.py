@@ -34,7 +34,7 @@ UNIT = "photons/s"
 ALG_BYTES_PER_GATHER = 16 + 100 * 32  # query record + k neighbour records (pos 12, dir 12, E 4, t 4)
 # DRAM bytes per scatter-map query measured by ncu on the same kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_gather<1, 0> launch / its queries; 1e6-photon case of this scene)
-DRAM_BYTES_PER_SCATTER_QUERY = 905
+DRAM_BYTES_PER_SCATTER_QUERY = 893
 
 
 def workload_config(name: str):
