@@ -22,6 +22,13 @@ common-random-number objective.
 The loss has no depth slope while the simulated seafloor return does not overlap the
 target's, so ``depth_grid`` (depths in m) starts every target at the grid depth of lowest
 loss, the other parameters at the initial guess. Those runs form one more batch.
+``depth_init="bottom_peak"`` starts it from the target itself instead, the way a
+bathymetric lidar reads a depth: the time of the seafloor return's peak in the target's
+seafloor channel, converted to a depth by the peak shift of two model runs at the initial
+guess and 5 m deeper (the seafloor return moves about 2 n / c seconds per metre; the
+calibration carries the scene's bin width, refractive index and view angles). A target
+whose seafloor return holds too few counts to locate keeps its start and is reported as
+undetectable.
 """
 
 from __future__ import annotations
@@ -86,12 +93,16 @@ def fit(
     fixed: Optional[Sequence[bool]] = None,
     prior_sigma: Optional[Sequence[Optional[float]]] = None,
     depth_difference: str = "forward",
+    depth_init: Optional[str] = None,
 ) -> Dict:
     """Fit every row of ``targets`` (n x 6). Returns final parameters, depth errors and the
     per-iteration mean data loss.
 
     depth_difference: "forward" (one plain instance at depth + depth_step per target) or
     "central" (two, at depth +- depth_step) for the depth column of the gradient.
+
+    depth_init: None, or "bottom_peak" to start each target's depth from the peak of its
+    seafloor channel (module docstring); the result then holds ``depth_detectable``.
 
     loss: "log" (squared difference of log(1 + counts)), "mse", or "poisson" (the negative
     log-likelihood of the Poisson counts, sum(lambda - counts ln lambda), lambda the scaled
@@ -153,6 +164,12 @@ def fit(
         r = np.log1p(sw) - np.log1p(counts[i])
         return float((r ** 2).sum()), 2.0 * r * scale[i] / (1.0 + sw)
 
+    detectable = np.ones(n, dtype=bool)
+    if depth_init is not None:
+        if depth_init != "bottom_peak":
+            raise ValueError(f"unknown depth_init {depth_init!r}")
+        if free[0]:
+            detectable = _bottom_peak_start(base, theta0, counts, scale, photons, nb, seed, streams, u)
     if depth_grid is not None:
         grid = np.asarray(depth_grid, dtype=np.float64)
         key = (seed << 40) + (1 << 32)
@@ -166,7 +183,8 @@ def fit(
         for i in range(n):
             ls = [loss_of(gw[i * len(grid) + j], i) if gst[i * len(grid) + j] == 0 else np.inf
                   for j in range(len(grid))]
-            if free[0]:
+            # a depth read from the target's own seafloor return takes precedence
+            if free[0] and not (depth_init is not None and detectable[i]):
                 u[i, 0] = math.log(grid[int(np.argmin(ls))] / theta0[0])
     m_ = np.zeros((n, 6))
     v_ = np.zeros((n, 6))
@@ -209,9 +227,55 @@ def fit(
         u -= lr * mh / (np.sqrt(vh) + eps)
         history.append(float(losses.mean()))
     final = _clip(theta0 * np.exp(u))
-    return {
+    out = {
         "params": final,
         "targets": targets,
         "depth_error": final[:, 0] - targets[:, 0],
         "loss_history": np.array(history),
     }
+    if depth_init is not None:
+        out["depth_detectable"] = detectable
+    return out
+
+
+# counts at the smoothed seafloor peak below which a target's seafloor return is not located
+BOTTOM_PEAK_MIN_COUNTS = 5.0
+CALIBRATION_STEP = 5.0  # m between the two model runs that convert a peak shift to a depth
+
+
+def _smoothed_peak(w: np.ndarray, width: int = 5) -> tuple:
+    """(bin, height) of the maximum of w after a centred box filter of ``width`` bins."""
+    k = np.ones(width) / width
+    sm = np.convolve(w, k, mode="same")
+    b = int(np.argmax(sm))
+    return b, float(sm[b])
+
+
+def _bottom_peak_start(base, theta0, counts, scale, photons, nb, seed, streams, u) -> np.ndarray:
+    """Sets u[i, 0] from the seafloor-channel peak of each target's counts (channel 0);
+    returns which targets had a locatable seafloor return. One batch: the model at the
+    initial guess and 5 m deeper, on one Philox key."""
+    n = len(counts)
+    d0 = float(theta0[0])
+    key = (seed << 40) + (3 << 32)
+    q0 = theta0.copy()
+    q1 = theta0.copy()
+    q1[0] = d0 + CALIBRATION_STEP
+    cw, _, cst, _, _ = run_batch([Instance(with_parameters(base, q0), photons, nb, key, q0),
+                                  Instance(with_parameters(base, q1), photons, nb, key, q1)], streams=streams)
+    if np.any(cst != 0):
+        raise RuntimeError(f"depth calibration runs failed: {cst}")
+    b0, _ = _smoothed_peak(np.asarray(cw[0])[0])
+    b1, _ = _smoothed_peak(np.asarray(cw[1])[0])
+    bins_per_m = (b1 - b0) / CALIBRATION_STEP
+    ok = np.zeros(n, dtype=bool)
+    if not bins_per_m > 0:
+        return ok
+    for i in range(n):
+        bt, h = _smoothed_peak(np.asarray(counts[i])[0])
+        if h < BOTTOM_PEAK_MIN_COUNTS:
+            continue
+        depth = max(d0 + (bt - b0) / bins_per_m, 0.2)
+        u[i, 0] = math.log(depth / d0)
+        ok[i] = True
+    return ok

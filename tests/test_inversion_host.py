@@ -119,3 +119,53 @@ def test_prior_holds_a_parameter_near_its_start(fake):
     assert abs(flat["params"][0, 2] / b0 - 1.0) > 0.15, flat["params"]
     with pytest.raises(ValueError):
         inversion.fit(target, prior_sigma=[0.0] * 6, **kw)
+
+
+def _toy_channels(theta):
+    """The toy with its seafloor peak alone in channel 0, as the simulator's seafloor
+    channel holds it, and the volume tail and surface peak in channels 1 and 2."""
+    D, a, b, g, alb, r = theta
+    peak = np.exp(-((T - 20.0 - 8.0 * D) ** 2) / 50.0)
+    surf = np.exp(-((T - 10.0) ** 2) / 8.0)
+    tail = np.exp(-T / 50.0)
+    att = np.exp(-2.0 * a * D)
+    w = np.zeros((4, NB))
+    w[0] = alb * att * peak
+    w[1] = 0.5 * b * g * tail
+    w[2] = 3.0 * r * surf
+    j = np.zeros((5, 4, NB))
+    j[0, 0] = -2.0 * D * alb * att * peak
+    j[1, 1] = 0.5 * g * tail
+    j[2, 1] = 0.5 * b * tail
+    j[3, 0] = att * peak
+    j[4, 2] = 3.0 * surf
+    return w * 1e3, j * 1e3
+
+
+def _fake_run_batch_channels(instances, streams=8, adjoint=False, precise=False, device=0, jacobian_mask=None):
+    ws, js = [], []
+    for k, x in enumerate(instances):
+        w, j = _toy_channels(np.asarray(x.params, dtype=np.float64))
+        ws.append(w)
+        js.append(j if adjoint and (jacobian_mask is None or jacobian_mask[k]) else None)
+    return ws, (js if adjoint else None), np.zeros(len(instances), np.int32), np.zeros(len(instances)), 0.0
+
+
+def test_depth_start_from_the_seafloor_peak(monkeypatch):
+    """A 30 m target is 20 m from the 10 m start, where the loss has no depth slope: the
+    start read from the target's own seafloor peak (calibrated by two model runs) lands
+    next to it and the fit closes in. A target with no visible seafloor return keeps its
+    start and is reported as undetectable."""
+    monkeypatch.setattr(inversion, "run_batch", _fake_run_batch_channels)
+    monkeypatch.setattr(inversion, "with_parameters", lambda base, p: None)
+    target = np.array([[30.0, 0.10, 0.30, 0.90, 0.20, float(np.sqrt(0.1))],
+                       [25.0, 0.10, 0.30, 0.90, 1e-9, float(np.sqrt(0.1))]])
+    kw = dict(photons=100, peak=1e6, base=object(), loss="log", depth_init="bottom_peak")
+    start = inversion.fit(target, iters=0, **kw)  # the starts themselves
+    assert start["depth_detectable"].tolist() == [True, False]
+    assert abs(start["depth_error"][0]) < 0.5, start["params"]
+    assert start["params"][1, 0] == inversion.INITIAL[0]
+    r = inversion.fit(target, iters=150, lr=2e-2, **kw)
+    assert abs(r["depth_error"][0]) < 0.1, r["params"]
+    with pytest.raises(ValueError):
+        inversion.fit(target, iters=1, photons=100, base=object(), depth_init="centroid")
