@@ -158,6 +158,50 @@ def test_knn_neighbour_sets_bit_exact(gpu_available):
         eng.close()
 
 
+@pytest.mark.parametrize("leaves,kinds_expected", [(2048 + 512 + 5, {128, 64}), (2048 + 256 + 5, {128, 32}),
+                                                   (2048 + 100, {128, 8})])
+def test_knn_every_cell_kind_matches_kdtree(gpu_available, leaves, kinds_expected):
+    """Map sizes whose left-balanced k-d tree ends in perfect cells of 128 leaves and of 64
+    (2048 + 512 + 5 leaves) or 32 (2048 + 256 + 5), or in multi-leaf general cells
+    (2048 + 100), plus single leaves and a partial last leaf, so every kind of per-CTA cell
+    kernel orders records. A third of the points sit on
+    a coarse lattice and a tenth are exact duplicates, so many records share a node's 16-bit
+    coordinate at its cut (the ties the partition ranks by position). Neighbour sets match
+    scipy's cKDTree except for exact ties at the k-th distance."""
+    sp = pytest.importorskip("scipy.spatial")
+
+    def cells(c, depth, D):  # leaf counts of the per-CTA cells: nodes at depth D, or single leaves
+        if depth == D or c <= 1:
+            return [c]
+        left = 1 << ((c - 1).bit_length() - 1)
+        return cells(left, depth + 1, D) + cells(c - left, depth + 1, D)
+
+    kinds = set(cells(leaves, 0, (leaves - 1).bit_length() - 7))
+    assert kinds_expected <= kinds and kinds - {32, 64, 128}, kinds
+    rng = np.random.default_rng(leaves)
+    m = 32 * leaves - 11
+    pts = rng.normal(scale=[0.5, 3.0, 0.5], size=(m, 3)) + [0.0, -405.0, 0.0]
+    lat = rng.random(m) < 0.33
+    pts[lat] = np.round(pts[lat] * 10.0) / 10.0
+    dup = rng.random(m) < 0.1
+    pts[dup] = pts[rng.integers(0, m, int(dup.sum()))]
+    pts = pts.astype(np.float32)
+    near = pts[rng.integers(0, m, 800)].astype(np.float64) + rng.normal(scale=0.03, size=(800, 3))
+    far = np.stack([rng.uniform(-20, 20, 200), rng.uniform(-420, -390, 200), rng.uniform(-20, 20, 200)], 1)
+    qs = np.concatenate([near, far])
+    eng = GpuEngine(config_from_fixture(load("replay_small.npz")))
+    try:
+        for k in (100, 7):
+            dist, idx = eng.ctx.knn(pts, qs, k)
+            ref_d, ref_i = sp.cKDTree(pts.astype(np.float64)).query(qs, k)
+            np.testing.assert_allclose(dist, ref_d, rtol=1e-12, atol=0)
+            for i in range(len(qs)):
+                strict = set(ref_i[i][ref_d[i] < ref_d[i][-1]])
+                assert strict <= set(idx[i]), (leaves, k, i)
+    finally:
+        eng.close()
+
+
 @pytest.mark.parametrize("shape", ["cloud", "planar"])
 def test_knn_large_map_matches_kdtree(gpu_available, shape):
     """Maps large enough for the streaming partition levels of the index build (3e6 points:
