@@ -54,13 +54,21 @@ __global__ void k_bbox(const float4* __restrict__ a, const float4* __restrict__ 
             hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
         }
     }
+    // the block's warps meet in shared memory: one set of global atomics per block (they
+    // all land on the same six words)
+    __shared__ unsigned sb[6];
+    if (threadIdx.x < 6) sb[threadIdx.x] = threadIdx.x < 3 ? 0xffffffffu : 0u;
+    __syncthreads();
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            atomicMin(box + k, f2ord(lo[k]));
-            atomicMax(box + 3 + k, f2ord(hi[k]));
+            atomicMin(sb + k, f2ord(lo[k]));
+            atomicMax(sb + 3 + k, f2ord(hi[k]));
         }
     }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(box + threadIdx.x, sb[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(box + threadIdx.x, sb[threadIdx.x]);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -834,7 +842,7 @@ __global__ void k_kdl_select2(const unsigned* __restrict__ hist2, uint32_t nodes
 constexpr int kSplitItems = 4;
 constexpr uint32_t kNoQ = 0xffffffffu;
 
-__global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
+__global__ void __launch_bounds__(kLvlThreads, 4) k_kdl_split(const float4* __restrict__ X, float4* __restrict__ X2,
                                                            uint16_t* Q, uint64_t n, uint64_t L, int d, LevelNodes nb,
                                                            const uint2* __restrict__ cut, unsigned* cursors,
                                                            unsigned* ties, unsigned* err, uint64_t per,
@@ -853,6 +861,13 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
     __syncthreads();  // the slots are read by every thread, whatever the block's range holds
     const uint64_t r0 = blockIdx.x * per, r1 = min(r0 + per, n);
     const uint64_t tile = (uint64_t)kSplitItems * blockDim.x;
+    // this thread's last node lookup: leaves [cn_a, cn_a + cn_c), its path, depth reached,
+    // cut and parameters
+    uint64_t cn_a = 0, cn_c = 0;
+    uint32_t cn_path = 0;
+    int cn_r = -1;
+    uint2 cn_cut = make_uint2(0u, 0u);
+    float4 cn_par = make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint64_t t0 = r0; t0 < r1; t0 += tile) {
         if (threadIdx.x < kSlots) ntag[threadIdx.x] = kNoTag;
         if (threadIdx.x < kSlots * 2) ncnt[threadIdx.x] = 0u;
@@ -881,13 +896,26 @@ __global__ void __launch_bounds__(kLvlThreads) k_kdl_split(const float4* __restr
             unsigned side = 0, hbin = 0;
             uint64_t a = 0, c = 0, left = 0;
             if (i < r1) {
-                int r;
-                kd_node_path(i / 32, L, d, a, c, path[t], r);
-                if (r == d && c > 1) {
+                // the node of the previous item usually holds this one too (items are 8
+                // leaves apart, split nodes at least 128 leaves wide): reuse its lookup
+                const uint64_t leaf = i / 32;
+                if (!(leaf >= cn_a && leaf - cn_a < cn_c)) {
+                    kd_node_path(leaf, L, d, cn_a, cn_c, cn_path, cn_r);
+                    if (cn_r == d && cn_c > 1) {
+                        cn_cut = cut[cn_path];
+                        cn_par = nb.par[cn_path];
+                    }
+                }
+                a = cn_a;
+                c = cn_c;
+                path[t] = cn_path;
+                if (cn_r == d && c > 1) {
                     moves = true;
                     left = 1ull << (63 - __clzll((long long)(c - 1)));
-                    const uint2 ct = cut[path[t]];
-                    const uint32_t q = kd_quant16(p[t], nb, path[t]);
+                    const uint2 ct = cn_cut;
+                    const int axis = __float_as_int(cn_par.x);
+                    const float v = axis == 0 ? p[t].x : (axis == 1 ? p[t].y : p[t].z);
+                    const uint32_t q = axis < 0 ? 0u : (uint32_t)fminf(fmaxf((v - cn_par.y) * cn_par.z, 0.f), 65535.f);
                     if (q < ct.x) side = 0;
                     else if (q > ct.x) side = 1;
                     else side = (atomicAdd(ties + path[t], 1u) < ct.y) ? 0u : 1u;
@@ -1652,7 +1680,10 @@ int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float 
     if (!box) return -1;
     unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
     cudaMemcpyAsync(box, init, sizeof(init), cudaMemcpyHostToDevice, st);
-    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 4096);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
     if (blocks == 0) blocks = 1;
     k_bbox<<<blocks, 256, 0, st>>>(a, nullptr, n, box);
     note_launch();
