@@ -130,8 +130,6 @@ class Workspace {
 
 // ---- map build (mapbuild.cu)
 KeyGrid make_key_grid(const float lo[3], const float hi[3], int bits3, int bits2);
-int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
-                     uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st);
 int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st);
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st);
 void release_map_index(MapIndex& m);

@@ -110,13 +110,15 @@ ALB_DEVICE uint64_t morton_key(const KeyGrid& g, float x, float y, float z) {
     return 0ull;
 }
 
-__global__ void k_keys(const float4* __restrict__ a, uint64_t n, KeyGrid g, uint64_t* keys, uint32_t* vals,
+// Query sort keys: 32-bit Morton codes (the query grid has at most 10 bits per axis in 3-D
+// and 16 in 2-D).
+__global__ void k_keys(const float4* __restrict__ a, uint64_t n, KeyGrid g, uint32_t* keys, uint32_t* vals,
                        unsigned long long* or_and) {
     unsigned long long o = 0ull, an = ~0ull;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         float4 p = a[i];
-        uint64_t key = morton_key(g, p.x, p.y, p.z);
+        const uint32_t key = (uint32_t)morton_key(g, p.x, p.y, p.z);
         keys[i] = key;
         vals[i] = (uint32_t)i;
         o |= key;
@@ -280,8 +282,9 @@ static int exclusive_scan(Workspace& ws, uint32_t* data, uint64_t n, cudaStream_
     return 0;
 }
 
-int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*& keys_alt,
-                     uint32_t*& vals_alt, uint64_t n, uint64_t varying_bits, cudaStream_t st) {
+template <class K>
+static int radix_sort_pairs(Workspace& ws, K*& keys, uint32_t*& vals, K*& keys_alt, uint32_t*& vals_alt, uint64_t n,
+                            uint64_t varying_bits, cudaStream_t st) {
     if (n <= 1) return 0;
     const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
     size_t mark = ws.mark();
@@ -291,7 +294,7 @@ int radix_sort_pairs(Workspace& ws, uint64_t*& keys, uint32_t*& vals, uint64_t*&
         return -1;
     }
     int passes = 0;
-    for (int shift = 0; shift < 64; shift += 8) {
+    for (int shift = 0; shift < (int)(8 * sizeof(K)); shift += 8) {
         if (((varying_bits >> shift) & 255ull) == 0ull) continue;  // digit constant over all keys
         k_rs_hist<<<ntiles, kRsThreads, 0, st>>>(keys, n, shift, hist, ntiles);
         note_launch();
@@ -1797,9 +1800,9 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, uint32_t* perm, cu
     if (compute_bbox(ws, qa, n, qlo, qhi, st) != 0) return -1;
     const KeyGrid g = make_key_grid(qlo, qhi, 10, 16);
     size_t mark = ws.mark();
-    uint64_t* keys = (uint64_t*)ws.take_bytes(n * 8);
+    uint32_t* keys = ws.take_u32(n);
     uint32_t* vals = perm;
-    uint64_t* keys2 = (uint64_t*)ws.take_bytes(n * 8);
+    uint32_t* keys2 = ws.take_u32(n);
     uint32_t* vals2 = ws.take_u32(n);
     unsigned long long* oa = (unsigned long long*)ws.scratch_box();
     if (!keys || !keys2 || !vals2 || !oa) {  // nothing launched on a failed allocation
@@ -1814,9 +1817,9 @@ int sort_queries(Workspace& ws, const float4* qa, uint64_t n, uint32_t* perm, cu
     unsigned long long h[2];
     cudaMemcpyAsync(h, oa, sizeof(h), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
-    uint64_t* k0 = keys;
+    uint32_t* k0 = keys;
     uint32_t* v0 = vals;
-    if (radix_sort_pairs(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st) < 0) {
+    if (radix_sort_pairs<uint32_t>(ws, k0, v0, keys2, vals2, n, h[0] ^ h[1], st) < 0) {
         ws.release(mark);
         return -1;
     }
