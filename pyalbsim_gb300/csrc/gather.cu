@@ -25,7 +25,11 @@ namespace alb {
 
 constexpr int kGatherWarps = 8;   // 8-warp CTAs, 4 per SM: 32 warps hide the gather's latency
 constexpr int kGatherBlocksPerSM = 4;
-constexpr int kQueryChunk = 64;  // consecutive sorted queries handled by one warp
+// consecutive sorted queries handled by one warp: each chunk's first search runs without a
+// bound, longer chunks balance worse (scatter map at 1e7 photons: 32 -> 546 ms, 64 -> 529 ms,
+// 128 -> 524 ms; the planar maps' gathers lose 2-3% at 128)
+constexpr int kQueryChunk = 64;
+constexpr int kQueryChunkScatter = 128;
 constexpr int kStack = 32 * kMaxLevels;
 constexpr int kCap = 288;         // candidate buffer (k <= kCap - 32)
 constexpr int kSelectAt = 192;    // shrink the buffer once it holds more than this
@@ -978,16 +982,17 @@ __global__ void __launch_bounds__(kGatherWarps * 32, kGatherBlocksPerSM) k_gathe
     const int w = threadIdx.x >> 5, l = lane_id();
     WarpSmem& s = smem[w];
     const uint64_t warps = (uint64_t)gridDim.x * kGatherWarps;
-    const uint64_t chunks = (q.n + kQueryChunk - 1) / kQueryChunk;
+    constexpr int kChunk = CHANNEL == ALB_SCATTER ? kQueryChunkScatter : kQueryChunk;
+    const uint64_t chunks = (q.n + kChunk - 1) / kChunk;
     bool failed = false;
     // search counters accumulate in the warp's shared memory, not in registers held through
     // every search
     if (l < 5) s.st[l] = 0ull;
     __syncwarp();
     for (uint64_t ch = (uint64_t)blockIdx.x * kGatherWarps + w; ch < chunks && !failed; ch += warps) {
-        const uint64_t q_end = min((ch + 1) * kQueryChunk, q.n);
+        const uint64_t q_end = min((ch + 1) * kChunk, q.n);
         bool have_prev = false;  // s.ci[0 .. k) holds the previous query's neighbours
-        for (uint64_t qi = ch * kQueryChunk; qi < q_end; ++qi) {
+        for (uint64_t qi = ch * kChunk; qi < q_end; ++qi) {
             uint64_t src = q.perm ? q.perm[qi] : qi;
             const float4 qa = q.a[src], qc = q.c[src];
             if (MODE == kModeRadius) {
