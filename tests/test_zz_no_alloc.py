@@ -144,53 +144,3 @@ def test_knn_noalloc_rejects_oversize_input():
                              C.c_void_p(i.data_ptr()), C.c_void_p(x.data_ptr()), None)
     assert rc == -1
     assert b"at most 4096 points" in lib.alb_last_error(None)
-
-
-def test_knn_noalloc_replays_from_a_cuda_graph():
-    """The reason the entry point allocates nothing: captured once into a CUDA graph (after
-    a first call outside the capture), the graph replays the index build and the query on
-    whatever the captured buffers hold when it is launched."""
-    torch = pytest.importorskip("torch")
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
-    from fixtures import config_from_fixture, load
-    from pyalbsim_gb300._native import load_library
-    from pyalbsim_gb300.engine import GpuEngine
-
-    lib = load_library()
-    rng = np.random.default_rng(7)
-    m, q, k = 2048, 300, 64
-    d_pts = torch.empty(3 * m, dtype=torch.float32, device="cuda")
-    d_q = torch.empty(3 * q, dtype=torch.float64, device="cuda")
-    d_idx = torch.empty(q * k, dtype=torch.int32, device="cuda")
-    d_dist = torch.empty(q * k, dtype=torch.float64, device="cuda")
-
-    def call(stream):
-        return lib.alb_knn_noalloc(
-            C.c_void_p(d_pts.data_ptr()), m, C.c_void_p(d_q.data_ptr()), q, k,
-            C.c_void_p(d_idx.data_ptr()), C.c_void_p(d_dist.data_ptr()), C.c_void_p(stream),
-        )
-
-    pts0 = _points(rng, m)
-    d_pts.copy_(torch.from_numpy(pts0.reshape(-1)))
-    d_q.copy_(torch.from_numpy(_queries(rng, pts0, q).reshape(-1)))
-    assert call(torch.cuda.current_stream().cuda_stream) == 0  # first call: outside any capture
-    torch.cuda.synchronize()
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        rc = call(torch.cuda.current_stream().cuda_stream)
-    assert rc == 0, lib.alb_last_error(None).decode()
-    eng = GpuEngine(config_from_fixture(load("replay_small.npz")))
-    try:
-        for _ in range(2):  # new points and queries in the captured buffers, then a replay
-            pts = _points(rng, m)
-            qs = _queries(rng, pts, q)
-            d_pts.copy_(torch.from_numpy(pts.reshape(-1)))
-            d_q.copy_(torch.from_numpy(qs.reshape(-1)))
-            g.replay()
-            torch.cuda.synchronize()
-            ref_d, ref_i = eng.ctx.knn(pts, qs, k)
-            _assert_same_neighbours(d_dist.cpu().numpy().reshape(-1, k), d_idx.cpu().numpy().reshape(-1, k),
-                                    ref_d, ref_i)
-    finally:
-        eng.close()
