@@ -498,7 +498,7 @@ extern "C" void alb_destroy(AlbCtx* ctx) {
     cudaDeviceSynchronize();
     for (void* p : ctx->tables) cudaFree(p);
     for (int c = 0; c < ALB_CHANNELS; ++c) {
-        cudaFree(ctx->rec[c].a); cudaFree(ctx->rec[c].b); cudaFree(ctx->rec[c].fwi); cudaFree(ctx->rec[c].sfi);
+        cudaFree(ctx->rec[c].a); cudaFree(ctx->rec[c].fwi); cudaFree(ctx->rec[c].sfi);
         cudaFree(ctx->rec[c].id); cudaFree(ctx->rec[c].sco);
         MapIndex& m = ctx->map[c];
         cudaFree(m.a); cudaFree(m.b); cudaFree(m.fwi); cudaFree(m.sfi); cudaFree(m.id); cudaFree(m.sco);
@@ -564,24 +564,24 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
     uint64_t cap = std::max<uint64_t>(need + need / 16, 1024);
     if (!keep) {  // nothing to copy: release the old store first, so the peak is one store
         CK(cudaStreamSynchronize(ctx->st));
-        cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
+        cudaFree(r.a); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
         r = RecordStore{};
     }
-    float4 *a = nullptr, *b = nullptr, *fwi = nullptr, *sfi = nullptr, *sco = nullptr;
+    float4 *a = nullptr, *fwi = nullptr, *sfi = nullptr, *sco = nullptr;
     uint32_t* id = nullptr;
-    // every allocation is checked, and a failure frees what this call had taken
-    bool ok = cudaMalloc(&a, cap * 16) == cudaSuccess && cudaMalloc(&b, cap * 16) == cudaSuccess;
+    // every allocation is checked, and a failure frees what this call had taken; the two
+    // record halves are interleaved in one allocation (RecordStore)
+    bool ok = cudaMalloc(&a, cap * 32) == cudaSuccess;
     if (ok && want_hm) ok = cudaMalloc(&fwi, cap * 16) == cudaSuccess && cudaMalloc(&sfi, cap * 16) == cudaSuccess;
     if (ok && want_id) ok = cudaMalloc(&id, cap * 4) == cudaSuccess;
     if (ok && want_sco) ok = cudaMalloc(&sco, cap * 16) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
-        cudaFree(a); cudaFree(b); cudaFree(fwi); cudaFree(sfi); cudaFree(id); cudaFree(sco);
+        cudaFree(a); cudaFree(fwi); cudaFree(sfi); cudaFree(id); cudaFree(sco);
         return fail(ctx, ALB_ERR_CUDA, "photon-map store: out of device memory");
     }
     if (keep) {
-        CK(cudaMemcpyAsync(a, r.a, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
-        CK(cudaMemcpyAsync(b, r.b, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        CK(cudaMemcpyAsync(a, r.a, keep * 32, cudaMemcpyDeviceToDevice, ctx->st));
         if (want_hm && r.fwi) {
             CK(cudaMemcpyAsync(fwi, r.fwi, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
             CK(cudaMemcpyAsync(sfi, r.sfi, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
@@ -590,14 +590,14 @@ static int ensure_records(AlbCtx* ctx, int c, uint64_t need, uint64_t keep) {
         if (want_sco && r.sco) CK(cudaMemcpyAsync(sco, r.sco, keep * 16, cudaMemcpyDeviceToDevice, ctx->st));
     }
     CK(cudaStreamSynchronize(ctx->st));
-    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
-    r.a = a; r.b = b; r.fwi = fwi; r.sfi = sfi; r.id = id; r.sco = sco; r.cap = cap;
+    cudaFree(r.a); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
+    r.a = a; r.b = a + 1; r.fwi = fwi; r.sfi = sfi; r.id = id; r.sco = sco; r.cap = cap;
     return ALB_OK;
 }
 
 static void release_records(AlbCtx* ctx, int c) {
     RecordStore& r = ctx->rec[c];
-    cudaFree(r.a); cudaFree(r.b); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
+    cudaFree(r.a); cudaFree(r.fwi); cudaFree(r.sfi); cudaFree(r.id); cudaFree(r.sco);
     r = RecordStore{};
 }
 
@@ -610,8 +610,9 @@ static int restore_records(AlbCtx* ctx, int c, uint64_t need) {
     const MapIndex& m = ctx->map[c];
     RecordStore& r = ctx->rec[c];
     if (n) {
-        CK(cudaMemcpyAsync(r.a, m.a, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
-        CK(cudaMemcpyAsync(r.b, m.b, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
+        // the index holds the halves in two arrays; the store interleaves them (32-byte pitch)
+        CK(cudaMemcpy2DAsync(r.a, 32, m.a, 16, 16, n, cudaMemcpyDeviceToDevice, ctx->st));
+        CK(cudaMemcpy2DAsync(r.b, 32, m.b, 16, 16, n, cudaMemcpyDeviceToDevice, ctx->st));
         if (r.fwi && m.fwi) {
             CK(cudaMemcpyAsync(r.fwi, m.fwi, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
             CK(cudaMemcpyAsync(r.sfi, m.sfi, n * 16, cudaMemcpyDeviceToDevice, ctx->st));
@@ -910,16 +911,20 @@ extern "C" int alb_export_map(AlbCtx* ctx, int c, float* pos, float* dir, float*
     if (m == 0) return ALB_OK;
     const float4 *a, *b, *fw, *sf;
     const uint32_t* id;
-    // records in append order, or in index order once the channel has been indexed
+    size_t pitch;  // bytes between consecutive records' a (and b) halves
+    // records in append order (the interleaved store), or in index order once the channel
+    // has been indexed
     if (ctx->rec_released[c]) {
         const MapIndex& mi = ctx->map[c];
         a = mi.a; b = mi.b; id = mi.id; fw = mi.fwi; sf = mi.sfi;
+        pitch = 16;
     } else {
         a = ctx->rec[c].a; b = ctx->rec[c].b; id = ctx->rec[c].id; fw = ctx->rec[c].fwi; sf = ctx->rec[c].sfi;
+        pitch = 32;
     }
     std::vector<float4> ha(m), hb(m), hf, hs;
-    CK(cudaMemcpy(ha.data(), a, m * 16, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hb.data(), b, m * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy2D(ha.data(), 16, a, pitch, 16, m, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy2D(hb.data(), 16, b, pitch, 16, m, cudaMemcpyDeviceToHost));
     if (fw && (fwi || sfi)) {
         hf.resize(m);
         hs.resize(m);
@@ -1158,14 +1163,14 @@ extern "C" int alb_knn(AlbCtx* ctx, const float* pts, uint64_t m, const double* 
     }
     RecordStore r{};
     size_t mark = ctx->ws.mark();
-    r.a = (float4*)ctx->ws.take_bytes(m * 16);
-    r.b = (float4*)ctx->ws.take_bytes(m * 16);
+    r.a = (float4*)ctx->ws.take_bytes(m * 32);  // interleaved store (RecordStore)
+    r.b = r.a ? r.a + 1 : nullptr;
     double* dq = (double*)ctx->ws.take_bytes(nq * 24);
     int32_t* di = (int32_t*)ctx->ws.take_bytes(nq * k * 4);
     double* dd = (double*)ctx->ws.take_bytes(nq * k * 8);
-    if (!r.a || !r.b || !dq || !di || !dd) return fail(ctx, ALB_ERR_CUDA, "knn allocation failed");
-    CK(cudaMemcpyAsync(r.a, ha.data(), m * 16, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemsetAsync(r.b, 0, m * 16, ctx->st));
+    if (!r.a || !dq || !di || !dd) return fail(ctx, ALB_ERR_CUDA, "knn allocation failed");
+    CK(cudaMemsetAsync(r.a, 0, m * 32, ctx->st));
+    CK(cudaMemcpy2DAsync(r.a, 32, ha.data(), 16, 16, m, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(dq, qs, nq * 24, cudaMemcpyHostToDevice, ctx->st));
     MapIndex mi;
     if (build_map_index(ctx->ws, r, m, mi, ctx->st) != 0) return fail(ctx, ALB_ERR_CAPACITY, "knn index build failed");

@@ -32,9 +32,12 @@ struct KeyGrid {
 };
 
 // Unsorted records of one channel as appended by the forward tracer.
+// The two halves of a record are interleaved in one allocation owned by `a`: record r is
+// a[2 r] = (x, y, z, energy) and b[2 r] = a[2 r + 1] = (dx, dy, dz, time), so a record is one
+// aligned 32-byte sector (written once by the tracer, gathered once by the index build).
 struct RecordStore {
-    float4* a = nullptr;    // x, y, z, energy
-    float4* b = nullptr;    // dx, dy, dz, time
+    float4* a = nullptr;    // x, y, z, energy (stride 2)
+    float4* b = nullptr;    // dx, dy, dz, time (stride 2; a + 1, not a separate allocation)
     float4* fwi = nullptr;  // optional
     float4* sfi = nullptr;
     uint32_t* id = nullptr; // optional
@@ -130,7 +133,8 @@ class Workspace {
 
 // ---- map build (mapbuild.cu)
 KeyGrid make_key_grid(const float lo[3], const float hi[3], int bits3, int bits2);
-int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st);
+int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st,
+                 uint64_t stride = 1);
 int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex& m, cudaStream_t st);
 void release_map_index(MapIndex& m);
 int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st);

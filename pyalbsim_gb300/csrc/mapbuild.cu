@@ -33,16 +33,12 @@ ALB_HOST_DEVICE float ord2f(unsigned u) {
 }
 
 // box[0..2] = ordered-min of x,y,z, box[3..5] = ordered-max; initialised to (~0, 0).
-__global__ void k_bbox(const float4* __restrict__ a, const float4* __restrict__ c, uint64_t n,
-                       unsigned* box) {
+__global__ void k_bbox(const float4* __restrict__ a, uint64_t stride, uint64_t n, unsigned* box) {
     float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        float4 p = a[i];
+        float4 p = a[i * stride];
         float x = p.x, y = p.y, z = p.z;
-        if (c) {  // query streams carry a low part; the box only needs the float part
-            (void)c;
-        }
         lo[0] = fminf(lo[0], x); hi[0] = fmaxf(hi[0], x);
         lo[1] = fminf(lo[1], y); hi[1] = fmaxf(hi[1], y);
         lo[2] = fminf(lo[2], z); hi[2] = fmaxf(hi[2], z);
@@ -1374,9 +1370,10 @@ __global__ void __launch_bounds__(CELL / 8, 8192 / CELL) k_local_kd_full(float4*
         Xg[s0 + j] = make_float4(s.X[j], s.Y[j], s.Z[j], __uint_as_float(s.ID[j]));
 }
 
+// positions of the interleaved store (stride 2) with each record's index in the w lane
 __global__ void k_pack_ids(const float4* __restrict__ a, uint64_t n, float4* X) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        float4 p = a[i];
+        float4 p = a[2 * i];
         X[i] = make_float4(p.x, p.y, p.z, __uint_as_float((uint32_t)i));
     }
 }
@@ -1678,7 +1675,8 @@ int build_box_tree(Workspace& ws, MapIndex& m, cudaStream_t st) {
     return 0;
 }
 
-int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st) {
+int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float hi[3], cudaStream_t st,
+                 uint64_t stride) {
     unsigned* box = ws.scratch_box();
     if (!box) return -1;
     unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
@@ -1688,7 +1686,7 @@ int compute_bbox(Workspace& ws, const float4* a, uint64_t n, float lo[3], float 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
     if (blocks == 0) blocks = 1;
-    k_bbox<<<blocks, 256, 0, st>>>(a, nullptr, n, box);
+    k_bbox<<<blocks, 256, 0, st>>>(a, stride, n, box);
     note_launch();
     unsigned h[6];
     cudaMemcpyAsync(h, box, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -1706,14 +1704,14 @@ __global__ void k_finalize(float4* a, float4* __restrict__ b, float4* __restrict
                            uint32_t* __restrict__ id, float4* __restrict__ sco, RecordStore rec, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t r = __float_as_uint(a[i].w);
-        b[i] = rec.b[r];
+        b[i] = rec.b[2 * (uint64_t)r];  // the record's two halves share one 32-byte sector
         if (fwi) {
             fwi[i] = rec.fwi[r];
             sfi[i] = rec.sfi[r];
         }
         if (id) id[i] = rec.id[r];
         if (sco) sco[i] = rec.sco[r];
-        a[i] = rec.a[r];
+        a[i] = rec.a[2 * (uint64_t)r];
     }
 }
 
@@ -1736,7 +1734,7 @@ int build_map_index(Workspace& ws, const RecordStore& rec, uint64_t n, MapIndex&
     }
     if (n >= (1ull << 32)) return -1;  // record ids are 32-bit
     float lo[3], hi[3];
-    if (compute_bbox(ws, rec.a, n, lo, hi, st) != 0) return -1;
+    if (compute_bbox(ws, rec.a, n, lo, hi, st, 2) != 0) return -1;
     cudaStreamSynchronize(st);
     if (n > m.a_cap) release_map_index(m);  // else every array is reused in place
     m.a = (float4*)ws.alloc_persistent(m.a, m.a_cap, n);

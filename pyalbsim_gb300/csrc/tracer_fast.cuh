@@ -48,8 +48,8 @@ ALB_DEVICE void emit_event_f(const TraceOut& out, int channel, int qkind, const 
     if (PASS == ALB_FORWARD) {
         unsigned long long slot = warp_append(out.rec_count, channel);
         if (slot < out.rec_cap[channel]) {
-            out.rec_a[channel][slot] = make_float4(x, y, z, ph.E);
-            out.rec_b[channel][slot] = make_float4(ph.dx, ph.dy, ph.dz, t);
+            out.rec_a[channel][2 * slot] = make_float4(x, y, z, ph.E);
+            out.rec_b[channel][2 * slot] = make_float4(ph.dx, ph.dy, ph.dz, t);
             if (out.rec_fwi[channel]) {
                 out.rec_fwi[channel][slot] = make_float4(ph.fwi[0], ph.fwi[1], ph.fwi[2], 0.f);
                 out.rec_sfi[channel][slot] = make_float4(ph.sfi[0], ph.sfi[1], ph.sfi[2], 0.f);
