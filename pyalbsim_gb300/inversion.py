@@ -169,7 +169,7 @@ def fit(
         if depth_init != "bottom_peak":
             raise ValueError(f"unknown depth_init {depth_init!r}")
         if free[0]:
-            detectable = _bottom_peak_start(base, theta0, counts, scale, photons, nb, seed, streams, u)
+            detectable = _bottom_peak_start(base, theta0, counts, photons, nb, seed, streams, u)
     if depth_grid is not None:
         grid = np.asarray(depth_grid, dtype=np.float64)
         key = (seed << 40) + (1 << 32)
@@ -251,7 +251,7 @@ def _smoothed_peak(w: np.ndarray, width: int = 5) -> tuple:
     return b, float(sm[b])
 
 
-def _bottom_peak_start(base, theta0, counts, scale, photons, nb, seed, streams, u) -> np.ndarray:
+def _bottom_peak_start(base, theta0, counts, photons, nb, seed, streams, u) -> np.ndarray:
     """Sets u[i, 0] from the seafloor-channel peak of each target's counts (channel 0);
     returns which targets had a locatable seafloor return. One batch: the model at the
     initial guess and 5 m deeper, on one Philox key."""
