@@ -1398,7 +1398,8 @@ static void enumerate_cells(uint64_t a, uint64_t c, int depth, int D, uint64_t n
     enumerate_cells(a + left, c - left, depth + 1, D, n, full, st, ct);
 }
 
-// out[i] <- (position, record id) of the i-th record of `a` in exact left-balanced k-d order.
+// out[i] <- (position, record id) of the i-th record of `a` (the interleaved record store:
+// record i at a[2 i]) in exact left-balanced k-d order.
 // `out` (n float4) is one of the two ping-pong buffers, so the build needs one temporary of
 // the same size besides it.
 static int kd_order_fast(Workspace& ws, const float4* a, uint64_t n, const float blo[3], const float bhi[3],
