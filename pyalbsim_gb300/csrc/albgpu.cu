@@ -1356,7 +1356,12 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                     const double grow = std::max(0.0, need - held);
                     mem_cv.wait(g, [&] {
                         if (!alone && exclusive > 0) return true;
-                        return alone ? running == 0 : (held_total + grow <= budget || running == 0);
+                        // a rerun alone waits until no instance runs and every other worker
+                        // has released its context (a worker that has just finished an
+                        // instance still holds its buffers until it comes back here); this
+                        // worker's own holding does not count
+                        return alone ? (running == 0 && held_total - held <= 0.5)
+                                     : (held_total + grow <= budget || running == 0);
                     });
                     if (!alone && exclusive > 0) continue;
                     held_total += grow;
@@ -1428,6 +1433,8 @@ extern "C" int alb_batch_run(AlbBatchInstance* inst, uint64_t n, const AlbBatchO
                 if (ctx && (rc == ALB_ERR_CUDA || rc == ALB_ERR_ITER_CAP || rc == ALB_ERR_CAPACITY)) {
                     alb_destroy(ctx);  // start the next instance clean
                     ctx = nullptr;
+                }
+                if (!ctx) {  // no context (destroyed, or never created): this worker holds nothing
                     std::lock_guard<std::mutex> m(mem_mu);
                     held_total -= held;
                     held = 0.0;
