@@ -35,6 +35,10 @@ ALG_BYTES_PER_GATHER = 16 + 100 * 32  # query record + k neighbour records (pos 
 # DRAM bytes per scatter-map query measured by ncu on the same kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_gather<1, 0> launch / its queries; 1e6-photon case of this scene)
 DRAM_BYTES_PER_SCATTER_QUERY = 893
+# Warp instructions per scatter-map query of the same capture (smsp__inst_executed.sum of one
+# k_gather<1, 0> launch / its queries): the kernel is bound by instruction issue, so its issue
+# rate is reported beside the HBM convention
+INST_PER_SCATTER_QUERY = 4615
 
 
 def workload_config(name: str):
@@ -398,6 +402,7 @@ def main():
             "per_step": gstats["forward_events"] + gstats["events"]},
         "last_step_counters": gstats,
         "tracer_roofline": tracer_roofline(gstats, phases, args.steps),
+        "gather_issue_roofline": measured(gather_issue_roofline, sc_queries, sc_ms),
         "clocks": clk.summary(),
         "waveform_total": float(wf.sum()),
     }
@@ -420,6 +425,34 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def sm_count_and_clock():
+    """(SMs, maximum SM clock in MHz): the device's SM count, MEASURED_PEAKS.json's clock."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            mhz = float(json.load(fh).get("sm_max_mhz", mhz))
+    except Exception:
+        pass
+    return sms, mhz
+
+
+def gather_issue_roofline(queries, ms, sms_mhz=None):
+    """The scatter-map gather against instruction issue, the bound its counters show: warp
+    instructions per second (INST_PER_SCATTER_QUERY x queries over its CUDA-event time)
+    against one issue per scheduler per cycle (SMs x 4 schedulers x the maximum SM clock)."""
+    sms, mhz = sms_mhz if sms_mhz is not None else sm_count_and_clock()
+    peak = sms * 4 * mhz * 1e6
+    achieved = INST_PER_SCATTER_QUERY * queries / (ms / 1e3) if ms > 0 else 0.0
+    return {"bound": "issue", "kernel": "k_gather<1, 0> (scatter map, k-NN)", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak if peak else None,
+            "instructions_per_query": INST_PER_SCATTER_QUERY,
+            "source": "instructions per query from the ncu capture of a 1e6-photon launch; peak derived: "
+                      f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz"}
 
 
 def tracer_roofline(gstats, phases, steps):

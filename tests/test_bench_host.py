@@ -63,3 +63,14 @@ def test_reference_config_carries_every_field():
 
 def test_cpu_model_is_reported():
     assert isinstance(_bench().cpu_model(), str) and _bench().cpu_model()
+
+
+def test_gather_issue_roofline_arithmetic():
+    """The issue roofline of the scatter gather: instructions per query x queries over the
+    kernel time, against SMs x 4 schedulers x the clock."""
+    bench = _bench()
+    r = bench.gather_issue_roofline(1_000_000, 10.0, sms_mhz=(152, 2070.0))
+    assert r["peak"] == 152 * 4 * 2070.0e6
+    assert abs(r["achieved"] - bench.INST_PER_SCATTER_QUERY * 1e6 / 0.01) < 1e-3
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-15
+    assert bench.gather_issue_roofline(5, 0.0, sms_mhz=(152, 2070.0))["achieved"] == 0.0
