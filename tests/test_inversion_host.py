@@ -169,3 +169,24 @@ def test_depth_start_from_the_seafloor_peak(monkeypatch):
     assert abs(r["depth_error"][0]) < 0.1, r["params"]
     with pytest.raises(ValueError):
         inversion.fit(target, iters=1, photons=100, base=object(), depth_init="centroid")
+
+
+def test_depth_start_without_a_calibration_shift_keeps_every_start(monkeypatch):
+    """If the two calibration runs put the seafloor peak in the same bin (no usable depth
+    scale), no target's depth start is changed and none is reported detectable."""
+    def flat(instances, streams=8, adjoint=False, precise=False, device=0, jacobian_mask=None):
+        ws, js = [], []
+        for x in instances:
+            w, j = _toy_channels(np.asarray(x.params, dtype=np.float64))
+            w[0] = 0.0
+            w[0, 300] = 1e3  # the same peak bin whatever the depth
+            ws.append(w)
+            js.append(j if adjoint else None)
+        return ws, (js if adjoint else None), np.zeros(len(instances), np.int32), np.zeros(len(instances)), 0.0
+
+    monkeypatch.setattr(inversion, "run_batch", flat)
+    monkeypatch.setattr(inversion, "with_parameters", lambda base, p: None)
+    target = np.array([[30.0, 0.10, 0.30, 0.90, 0.20, float(np.sqrt(0.1))]])
+    r = inversion.fit(target, iters=0, photons=100, peak=1e6, base=object(), depth_init="bottom_peak")
+    assert r["depth_detectable"].tolist() == [False]
+    assert r["params"][0, 0] == inversion.INITIAL[0]
